@@ -1,0 +1,165 @@
+/*
+ * fpm_capi.h -- C ABI of the GB300 FlowFPM++ hot path (libfpm_gb300.so).
+ *
+ * Each entry point replaces one procedure of the reference's Fortran API and
+ * keeps its argument meaning, order and array layout, so that a Fortran
+ * ISO_C_BINDING interface (or ctypes, or any C caller) can pass its arrays
+ * through unchanged.  The reference procedure each one replaces is cited as
+ * path:line in the reference repository.
+ *
+ * Conventions
+ *  - Arrays are Fortran column-major (x fastest) with the reference's bounds:
+ *      padded 3-D  (0:nx+1, 0:ny+1, 1:nz)   phi, solid of the stair-step API
+ *      interior    (1:nx, 1:ny, 1:nz)        rhs and all flow / output fields
+ *      faces       xlo,xhi(ny,nz) ylo,yhi(nx,nz) zlo,zhi(nx,ny)
+ *      axes        xc(0:nx+1) yc(0:ny+1) zc(nz) dx(nx) dy(ny) dz(nz)
+ *    solid is int32 (1 solid, 0 fluid).
+ *  - One GPU, one rank: every side of the grid is a physical boundary (the
+ *    reference's west..north == MPI_PROC_NULL).  Domain decomposition is not
+ *    supported; a Fortran shim rejects a communicator with more than one rank.
+ *  - Plain entry points take HOST pointers, copy to the GPU, run, copy back
+ *    and return when the results are on the host.  Entry points ending in
+ *    _dev take DEVICE pointers (cudaMalloc'd) and a cudaStream_t passed as
+ *    void* (NULL = default stream); they return after the stream has drained,
+ *    with scalar results on the host.
+ *  - Every entry point returns FPM_OK (0) or a status code below; the
+ *    message is available from fpm_last_error() on the calling thread.  The
+ *    reference stops the program (error stop) in the same situations.
+ *    Non-convergence is not an error: check the returned residual/sweeps.
+ *  - There is no CPU fallback: without a usable GPU every entry point returns
+ *    FPM_E_CUDA or FPM_E_NO_DEVICE.
+ */
+#ifndef FPM_CAPI_H
+#define FPM_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FPM_OK 0
+#define FPM_E_METHOD 1        /* 'stair-step method must be pcg or jacobi'                 (fpm_stairstep_mpi_3d.f90:127) */
+#define FPM_E_SIZE 2          /* 'stair-step solve needs nz>=2 and nonempty ranks'         (fpm_stairstep_mpi_3d.f90:130),
+                                 'nonuniform 3-D FPM kernel requires at least two cells'   (fpm_terms_3d.f90:54) */
+#define FPM_E_ISOLATED 3      /* 'stair-step fluid cell has no fluid neighbour'            (fpm_stairstep_mpi_3d.f90:151) */
+#define FPM_E_NO_OUTER_FACE 4 /* 'stair-step compatibility needs at least one fluid outer face' (fpm_stairstep_mpi_3d.f90:56) */
+#define FPM_E_ARG 5           /* null pointer or invalid argument */
+#define FPM_E_CUDA 6          /* CUDA runtime error (message has the CUDA error string) */
+#define FPM_E_NO_DEVICE 7     /* no CUDA device visible */
+#define FPM_E_LIMIT 8         /* a size exceeds a documented limit */
+
+/* ---- solver methods (the reference's method='pcg' | 'jacobi') ---------- */
+#define FPM_METHOD_PCG 0        /* diagonal PCG, FP64 throughout (reference 'pcg') */
+#define FPM_METHOD_JACOBI 1     /* weighted Jacobi 0.2/0.8, FP64, bit-identical per sweep to a serial
+                                   -ffp-contract=off evaluation (reference 'jacobi') */
+#define FPM_METHOD_JACOBI_DF 2  /* weighted Jacobi in double-float (f32 pair, 48-bit significand)
+                                   arithmetic with FP64 residual checks: same iteration, HBM-bound on GB300 */
+
+/* ---- diagnostics -------------------------------------------------------- */
+const char* fpm_last_error(void);
+/* Library version as 10000*major + 100*minor + patch. */
+int fpm_version(void);
+/* Pinned (page-locked) host memory for fast transfers; NULL on failure. */
+void* fpm_host_alloc(size_t bytes);
+void fpm_host_free(void* p);
+
+/* ---- fpm_stairstep_mpi_3d ----------------------------------------------
+ * exchange_solid_halo_3d (src/fpm_stairstep_mpi_3d.f90:25-36): zeroes the
+ * physical-boundary halo of solid (padded, host array). */
+int fpm_exchange_solid_halo_3d(int32_t* solid, int nx, int ny, int nz);
+
+/* enforce_stairstep_compatibility_3d (src/fpm_stairstep_mpi_3d.f90:41-92):
+ * shifts the six outer-face arrays in place by one uniform correction so the
+ * outer plus body flux balances the fluid source. */
+int fpm_enforce_stairstep_compatibility_3d(const double* rhs, const int32_t* solid, const double* body_grad,
+                                           double* xlo, double* xhi, double* ylo, double* yhi, double* zlo,
+                                           double* zhi, const double* dx, const double* dy, const double* dz, int nx,
+                                           int ny, int nz, double* correction, double* imbalance);
+int fpm_enforce_stairstep_compatibility_3d_dev(const double* rhs, const int32_t* solid, const double* body_grad,
+                                               double* xlo, double* xhi, double* ylo, double* yhi, double* zlo,
+                                               double* zhi, const double* dx, const double* dy, const double* dz,
+                                               int nx, int ny, int nz, double* correction, double* imbalance,
+                                               void* stream);
+
+/* solve_stairstep_poisson_3d (src/fpm_stairstep_mpi_3d.f90:106-330): solves
+ * the stair-step pure-Neumann problem on fluid cells (phi in: initial guess,
+ * out: solution with the fluid-volume mean removed).  tolerance < 0 runs
+ * exactly max_sweeps iterations.  body_grad has 3 entries (host memory in
+ * both forms).  method: FPM_METHOD_*. */
+int fpm_solve_stairstep_poisson_3d(double* phi, const double* rhs, const int32_t* solid, const double* body_grad,
+                                   const double* xlo, const double* xhi, const double* ylo, const double* yhi,
+                                   const double* zlo, const double* zhi, const double* xc, const double* yc,
+                                   const double* zc, const double* dx, const double* dy, const double* dz, int nx,
+                                   int ny, int nz, double tolerance, int max_sweeps, int check_interval, int method,
+                                   int* sweeps, double* residual);
+int fpm_solve_stairstep_poisson_3d_dev(double* phi, const double* rhs, const int32_t* solid, const double* body_grad,
+                                       const double* xlo, const double* xhi, const double* ylo, const double* yhi,
+                                       const double* zlo, const double* zhi, const double* xc, const double* yc,
+                                       const double* zc, const double* dx, const double* dy, const double* dz, int nx,
+                                       int ny, int nz, double tolerance, int max_sweeps, int check_interval,
+                                       int method, int* sweeps, double* residual, void* stream);
+
+/* stairstep_residual_3d (src/fpm_stairstep_mpi_3d.f90:403-419): independent
+ * max-norm residual of L(phi)-f from face gradients. */
+int fpm_stairstep_residual_3d(const double* phi, const double* rhs, const int32_t* solid, const double* body_grad,
+                              const double* xlo, const double* xhi, const double* ylo, const double* yhi,
+                              const double* zlo, const double* zhi, const double* xc, const double* yc,
+                              const double* zc, const double* dx, const double* dy, const double* dz, int nx, int ny,
+                              int nz, double* value);
+
+/* compute_stairstep_fpm_terms_3d (src/fpm_stairstep_mpi_3d.f90:426-469):
+ * gradients, vortex = -(omega x u).grad(phi), advection = -a.grad(phi) and
+ * their integrals over fluid cells with centres strictly inside bounds(6). */
+int fpm_compute_stairstep_fpm_terms_3d(const double* phi, const double* u, const double* v, const double* w,
+                                       const double* ox, const double* oy, const double* oz, const double* ax,
+                                       const double* ay, const double* az, const int32_t* solid,
+                                       const double* body_grad, const double* xc, const double* yc, const double* zc,
+                                       const double* dx, const double* dy, const double* dz, const double* xlo,
+                                       const double* xhi, const double* ylo, const double* yhi, const double* zlo,
+                                       const double* zhi, const double* bounds, double* gx, double* gy, double* gz,
+                                       double* vortex, double* advection, double* totals, int nx, int ny, int nz);
+int fpm_compute_stairstep_fpm_terms_3d_dev(const double* phi, const double* u, const double* v, const double* w,
+                                           const double* ox, const double* oy, const double* oz, const double* ax,
+                                           const double* ay, const double* az, const int32_t* solid,
+                                           const double* body_grad, const double* xc, const double* yc,
+                                           const double* zc, const double* dx, const double* dy, const double* dz,
+                                           const double* xlo, const double* xhi, const double* ylo,
+                                           const double* yhi, const double* zlo, const double* zhi,
+                                           const double* bounds, double* gx, double* gy, double* gz, double* vortex,
+                                           double* advection, double* totals, int nx, int ny, int nz, void* stream);
+
+
+/* ---- operator-level entry points (device arrays) ------------------------
+ * The private building blocks of solve_stairstep_poisson_3d, exposed so a
+ * caller can keep the operator resident and drive sweeps itself.
+ * build_operator (src/fpm_stairstep_mpi_3d.f90:336-379): src, diag, rdiag
+ * (interior arrays); rdiag = 1/(V diag) if for_pcg else 0.8/diag; *isolated
+ * receives the number of fluid cells without a fluid neighbour. */
+int fpm_stairstep_build_operator_dev(const double* rhs, const int32_t* solid, const double* body_grad,
+                                     const double* xlo, const double* xhi, const double* ylo, const double* yhi,
+                                     const double* zlo, const double* zhi, const double* xc, const double* yc,
+                                     const double* zc, const double* dx, const double* dy, const double* dz, int nx,
+                                     int ny, int nz, int for_pcg, double* src, double* diag, double* rdiag,
+                                     int* isolated, void* stream);
+/* jacobi_sweep (src/fpm_stairstep_mpi_3d.f90:384-399), nsweeps times,
+ * alternating a -> b -> a ...  (padded arrays with zero physical halo and
+ * zero solid cells, as after the solver's init loop).  The latest iterate is
+ * in a when nsweeps is even, else in b.  method FPM_METHOD_JACOBI (FP64,
+ * bit-identical per sweep) or FPM_METHOD_JACOBI_DF (double-float arithmetic;
+ * a and b are converted in and out once per call). */
+int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, const double* rdiag, const double* xc,
+                                    const double* yc, const double* zc, const double* dx, const double* dy,
+                                    const double* dz, int nx, int ny, int nz, int nsweeps, int method, void* stream);
+/* operator_residual (src/fpm_stairstep_mpi_3d.f90:514-530): max over diag>0
+ * of |src + sum(c_nb phi_nb) - diag phi|. */
+int fpm_stairstep_operator_residual_dev(const double* phi, const double* src, const double* diag, const double* xc,
+                                        const double* yc, const double* zc, const double* dx, const double* dy,
+                                        const double* dz, int nx, int ny, int nz, double* value, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FPM_CAPI_H */

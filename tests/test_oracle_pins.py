@@ -1,0 +1,187 @@
+"""Pins the CPU oracle against every known answer the reference's own tests
+and README hold for this path.  CPU only (no GPU): these decide whether the
+oracle can be trusted as the checker of the CUDA kernels.
+
+Sources (reference repository):
+  tests/test_stairstep_exact_3d.f90  thresholds :46-48, :68-70; README.md:114-119
+  tests/test_stairstep_sphere_3d.f90 :45-49;   README.md:127-132 (table)
+  tests/test_fpm_3d.f90 :47-48; tests/test_fpm_3d_nonuniform.f90 :151-153
+  tests/test_fpm_partition_2d.f90 :67;       README.md:134-143
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from cases import (F, exact_expectations, fill_ring, manufactured_nonuniform, manufactured_uniform,
+                   nonuniform_expected, partition_grid, sphere_case, sphere_errors, stairstep_case_exact)
+
+
+def run_stairstep(c, method, tol, max_it, ci=50):
+    phi = c["phi"].copy(order="F")
+    faces = [f.copy(order="F") for f in c["faces"]]
+    corr, imb = orc.enforce_stairstep_compatibility_3d(c["rhs"], c["solid"], c["body"], *faces, c["dx"], c["dy"],
+                                                       c["dz"])
+    sw, res = orc.solve_stairstep_poisson_3d(phi, c["rhs"], c["solid"], c["body"], *faces, c["xc"], c["yc"],
+                                             c["zc"], c["dx"], c["dy"], c["dz"], tol, max_it, ci, method)
+    chk = orc.stairstep_residual_3d(phi, c["rhs"], c["solid"], c["body"], *faces, c["xc"], c["yc"], c["zc"],
+                                    c["dx"], c["dy"], c["dz"])
+    fl = c.get("flow")
+    terms = None
+    if fl is not None:
+        terms = orc.compute_stairstep_fpm_terms_3d(phi, fl["u"], fl["v"], fl["w"], fl["ox"], fl["oy"], fl["oz"],
+                                                   fl["ax"], fl["ay"], fl["az"], c["solid"], c["body"], c["xc"],
+                                                   c["yc"], c["zc"], c["dx"], c["dy"], c["dz"], *faces, c["bounds"])
+    return dict(phi=phi, faces=faces, corr=corr, imb=imb, sweeps=sw, res=res, chk=chk, terms=terms)
+
+
+@pytest.mark.parametrize("method,tol,iters", [("jacobi", 1e-12, 14500), ("pcg", 1e-10, 200)])
+def test_exact_linear_solution(method, tol, iters):
+    """phi = g.x is the exact discrete solution (test_stairstep_exact_3d.f90:40-50);
+    README.md:114-119 reports 14,500 Jacobi sweeps and 200 PCG iterations."""
+    c = stairstep_case_exact(True)
+    out = run_stairstep(c, method, tol, 400000)
+    gx, gy, gz, vortex, adv, totals = out["terms"]
+    errors, ierr = exact_expectations(c, out["phi"], gx, gy, gz, vortex, totals)
+    assert abs(out["corr"]) < 1e-13 and abs(out["imb"]) < 1e-13
+    assert out["res"] <= 2 * tol and out["chk"] < 1e-9
+    assert errors[0] < 1e-9 and errors[1] < 1e-9 and errors[2] < 1e-9 and errors[3] == 0
+    assert ierr < 1e-10
+    assert np.all(np.isfinite([out["res"], out["chk"], *errors, *totals]))
+    # README.md:114-119 prints the counts rounded to three figures; they are
+    # reached at a check boundary (check_interval 50).
+    assert abs(out["sweeps"] - iters) <= 50 and out["sweeps"] % 50 == 0
+
+
+def test_influence_fixed_jacobi_and_pcg():
+    """Influence case (body_grad = e_x): 600 fixed Jacobi sweeps, PCG to 1e-11
+    (test_stairstep_exact_3d.f90:61-81); the two methods agree on the field."""
+    c = stairstep_case_exact(False)
+    j = run_stairstep(c, "jacobi", -1.0, 600)
+    assert j["sweeps"] == 600 and abs(j["imb"]) < 1e-13
+    assert abs(j["chk"] - j["res"]) <= 1e-8 * j["res"] + 1e-12
+    p = run_stairstep(c, "pcg", 1e-11, 100000)
+    assert p["res"] <= 2e-11 and abs(p["imb"]) < 1e-13
+    assert abs(p["chk"] - p["res"]) <= 1e-8 * p["res"] + 1e-12
+    assert np.all(np.isfinite(p["phi"]))
+
+
+# README.md:127-132: N, PCG iterations, RMS error, far-field error, C_m.
+SPHERE_TABLE = [
+    (12, 100, 1.08e-2, 2.24e-2, 0.897),
+    (24, 200, 9.27e-3, 1.87e-2, 0.770),
+    (48, 300, 4.56e-3, 9.21e-3, 0.639),
+    pytest.param(96, 500, 2.14e-3, 4.38e-3, 0.566, marks=pytest.mark.slow),
+]
+
+
+@pytest.mark.parametrize("n,iters,rms_ref,far_ref,cm_ref", SPHERE_TABLE)
+def test_sphere_dipole_table(n, iters, rms_ref, far_ref, cm_ref):
+    """Reproduces the README's sphere-convergence table to its printed digits."""
+    c = sphere_case(n)
+    out = run_stairstep(c, "pcg", 1e-10, 2000000, ci=100)
+    rms, far, cm = sphere_errors(c, out["phi"])
+    assert out["sweeps"] == iters
+    assert f"{rms:.2e}" == f"{rms_ref:.2e}"
+    assert f"{far:.2e}" == f"{far_ref:.2e}"
+    assert round(cm, 3) == pytest.approx(cm_ref, abs=1e-12)
+
+
+def test_manufactured_uniform():
+    """tests/test_fpm_3d.f90:22-48: correction 1/6, phi/grad/fields to 1e-9."""
+    c = manufactured_uniform()
+    nx, ny, nz, dx, dy, dz = c["nx"], c["ny"], c["nz"], c["dx"], c["dy"], c["dz"]
+    faces = [f.copy(order="F") for f in c["faces"]]
+    corr, imb = orc.enforce_neumann_compatibility_3d(c["rhs"], *faces, dx, dy, dz)
+    phi = c["phi"].copy(order="F")
+    it, res = orc.solve_neumann_poisson_3d(phi, c["rhs"], *faces, dx, dy, dz, 1e-10, 50000, 25)
+    one = np.ones((nx, ny, nz), order="F")
+    u, v, w = 1 * one, 2 * one, 3 * one
+    ox, oy, oz = 0.5 * one, -0.25 * one, 0.75 * one
+    ax_, ay_, az_ = 0.2 * one, -0.1 * one, 0.3 * one
+    fluid = np.ones((nx, ny, nz), dtype=np.int32, order="F")
+    gx, gy, gz, vf, af, totals = orc.compute_fpm_terms_uniform_3d(phi, u, v, w, ox, oy, oz, ax_, ay_, az_, fluid,
+                                                                 dx, dy, dz)
+    X, Y, Z = c["X"], c["Y"], c["Z"]
+    sol = np.abs(phi[1:nx + 1, 1:ny + 1, 1:nz + 1] - c["exact"]).max()
+    grad = max(np.abs(gx - (X - .5) / 3).max(), np.abs(gy - (Y - .5) / 3).max(), np.abs(gz - (Z - .5) / 3).max())
+    ev = -((-2.25) * ((X - .5) / 3) - .75 * ((Y - .5) / 3) + 1.25 * ((Z - .5) / 3))
+    ea = -(.2 * ((X - .5) / 3) - .1 * ((Y - .5) / 3) + .3 * ((Z - .5) / 3))
+    field = max(np.abs(vf - ev).max(), np.abs(af - ea).max())
+    assert it < 50000 and res <= 1e-10
+    assert abs(corr - 1.0 / 6) < 1e-12 and abs(imb) < 1e-12
+    assert sol < 1e-9 and grad < 1e-9 and field < 1e-9 and np.abs(totals).max() < 1e-12
+
+
+def test_manufactured_nonuniform():
+    """tests/test_fpm_3d_nonuniform.f90:103-153: correction 0.37/6, fields to 1e-8."""
+    c = manufactured_nonuniform()
+    nx, ny, nz = c["nx"], c["ny"], c["nz"]
+    tf = [f.copy(order="F") for f in c["faces"]]
+    corr, imb = orc.enforce_neumann_compatibility_nonuniform_3d(np.asfortranarray(c["rhs"] + 0.37), *tf, c["dx"],
+                                                                 c["dy"], c["dz"])
+    phi = F((nx, ny, nz))
+    it, res = orc.solve_neumann_poisson_nonuniform_3d(phi, c["rhs"], *c["faces"], c["xc"], c["yc"], c["zc"],
+                                                      c["dx"], c["dy"], c["dz"], 1e-10, 100000, 25)
+    one = np.ones((nx, ny, nz), order="F")
+    fluid = np.ones((nx, ny, nz), dtype=np.int32, order="F")
+    fluid[nx // 2 - 1, ny // 2 - 1, nz // 2 - 1] = 0
+    eps = np.finfo(np.float64).eps
+    xc, yc, zc = c["xc"], c["yc"], c["zc"]
+    bounds = np.array([xc[1] - eps, xc[nx - 2] + eps, yc[1] - eps, yc[ny - 2] + eps, zc[1] - eps, zc[nz - 2] + eps])
+    gx, gy, gz, vf, af, totals = orc.compute_fpm_terms_nonuniform_3d(
+        phi, 1 * one, 2 * one, 3 * one, 0.5 * one, -0.25 * one, 0.75 * one, 0.2 * one, -0.1 * one, 0.3 * one, fluid,
+        xc, yc, zc, c["dx"], c["dy"], c["dz"], *c["faces"], bounds)
+    ge, ef, ie = nonuniform_expected(c, fluid, bounds, gx, gy, gz, vf, af, totals)
+    assert it < 100000 and res <= 1e-10
+    assert abs(corr - 0.37 / 6.0) < 1e-12 and abs(imb) < 1e-12
+    assert np.abs(phi - c["exact"]).max() < 1e-8 and ge < 1e-8 and ef < 1e-8 and ie < 1e-10
+
+
+def test_partition_2d_known_answers():
+    """tests/test_fpm_partition_2d.f90: rotation div N = -2 W^2 and omega = 2W
+    to 1e-10 (README: 3e-14), uniform flow gives exactly zero, and the
+    accelerating cylinder's added-mass coefficient is 1.14 (README.md:139-143)."""
+    n, w0, radius = 160, 0.7, 0.25
+    xf, xc, dx = partition_grid(n)
+    solid = np.zeros((n, n), dtype=np.uint8, order="F")
+    kin = np.zeros(6)
+    X = xc[1:n + 1][:, None] * np.ones((n, n))
+    Y = xc[1:n + 1][None, :] * np.ones((n, n))
+    phi = np.ones((n, n), order="F")
+    u = np.asfortranarray(-w0 * Y)
+    v = np.asfortranarray(w0 * X)
+    terms, dens, omega = orc.fpm_partition_terms_2d(phi, [1.0, 0.0], u, v, solid, xf, xf, kin, fill_ring(u, v), 1.0,
+                                                    1e-3)
+    err1 = max(np.abs(dens[2:n - 2, 2:n - 2] + 2 * w0 ** 2).max(), np.abs(omega[2:n - 2, 2:n - 2] - 2 * w0).max())
+    assert err1 < 1e-10
+    u = np.ones((n, n), order="F")
+    v = np.zeros((n, n), order="F")
+    phi = np.asfortranarray(X - Y)
+    terms, _, _ = orc.fpm_partition_terms_2d(phi, [1.0, 0.0], u, v, solid, xf, xf, kin, fill_ring(u, v), 1.0, 1e-3)
+    assert np.all(terms == 0)
+    # accelerating cylinder
+    nz = 2
+    s2 = (X ** 2 + Y ** 2 < radius ** 2)
+    solid3 = F((n + 2, n + 2, nz), np.int32)
+    for k in range(nz):
+        solid3[1:n + 1, 1:n + 1, k] = s2
+    dz = np.array([0.5, 0.5])
+    zc = np.array([0.25, 0.75])
+    faces = [F((n, nz)), F((n, nz)), F((n, nz)), F((n, nz)), F((n, n)), F((n, n))]
+    rhs = F((n, n, nz))
+    phi3 = F((n + 2, n + 2, nz))
+    body = np.array([1.0, 0.0, 0.0])
+    orc.enforce_stairstep_compatibility_3d(rhs, solid3, body, *faces, dx, dx, dz)
+    sw, res = orc.solve_stairstep_poisson_3d(phi3, rhs, solid3, body, *faces, xc, xc, zc, dx, dx, dz, 1e-10, 200000,
+                                             50, "pcg")
+    u = np.zeros((n, n), order="F")
+    v = np.zeros((n, n), order="F")
+    kin = np.array([0.0, 0.0, 0.0, 1.0, 0.0, 0.0])
+    terms, _, _ = orc.fpm_partition_terms_2d(np.asfortranarray(phi3[1:n + 1, 1:n + 1, 0]), [1.0, 0.0], u, v,
+                                             np.asfortranarray(s2.astype(np.uint8)), xf, xf, kin, fill_ring(u, v), 1.0,
+                                             1e-3)
+    cm = -terms[0] / (math.pi * radius ** 2)
+    assert abs(cm - 1) < 0.2 and np.all(terms[1:] == 0)
+    assert f"{cm:.2f}" == "1.14"

@@ -1,0 +1,199 @@
+"""GPU parity of the stair-step path (libfpm_gb300.so through the C ABI)
+against the CPU oracle on the same inputs.
+
+Tolerances: the FP64 Jacobi sweep and the operator build are bit-identical
+per cell; max-norm residuals are bit-identical (max is order independent);
+the double-float Jacobi must stay within 1e-12 relative of FP64 after 2000
+sweeps; converged PCG potentials within 1e-9 relative max-norm of the
+oracle's; force densities bit-identical for the same phi and integrals within
+1e-12 relative (sum order differs)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from cases import exact_expectations, sphere_case, sphere_errors, stairstep_case_exact
+from gpu_util import from_dev, ptr, stream_ptr, to_dev
+
+pytestmark = pytest.mark.gpu
+
+D, I = ctypes.c_double, ctypes.c_int
+
+
+def gpu_run(c, method, tol, max_it, ci=50):
+    from flowfpmpp_gb300 import stairstep as ss
+    phi = c["phi"].copy(order="F")
+    faces = [f.copy(order="F") for f in c["faces"]]
+    corr, imb = ss.enforce_stairstep_compatibility_3d(c["rhs"], c["solid"], c["body"], *faces, c["dx"], c["dy"],
+                                                      c["dz"])
+    sw, res = ss.solve_stairstep_poisson_3d(phi, c["rhs"], c["solid"], c["body"], *faces, c["xc"], c["yc"], c["zc"],
+                                            c["dx"], c["dy"], c["dz"], tol, max_it, ci, method)
+    chk = ss.stairstep_residual_3d(phi, c["rhs"], c["solid"], c["body"], *faces, c["xc"], c["yc"], c["zc"], c["dx"],
+                                   c["dy"], c["dz"])
+    terms = None
+    fl = c.get("flow")
+    if fl is not None:
+        terms = ss.compute_stairstep_fpm_terms_3d(phi, fl["u"], fl["v"], fl["w"], fl["ox"], fl["oy"], fl["oz"],
+                                                  fl["ax"], fl["ay"], fl["az"], c["solid"], c["body"], c["xc"],
+                                                  c["yc"], c["zc"], c["dx"], c["dy"], c["dz"], *faces, c["bounds"])
+    return dict(phi=phi, faces=faces, corr=corr, imb=imb, sweeps=sw, res=res, chk=chk, terms=terms)
+
+
+def cpu_run(c, method, tol, max_it, ci=50):
+    from test_oracle_pins import run_stairstep
+    return run_stairstep(c, method, tol, max_it, ci)
+
+
+def rel_linf(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_compatibility_matches_oracle(gpu_lib):
+    for exact in (True, False):
+        c = stairstep_case_exact(exact)
+        g = gpu_run(c, "jacobi", -1.0, 2)
+        o = cpu_run(c, "jacobi", -1.0, 2)
+        assert abs(g["corr"] - o["corr"]) <= 1e-15 and abs(g["imb"]) < 1e-13
+        for fg, fo in zip(g["faces"], o["faces"]):
+            assert np.abs(fg - fo).max() <= 1e-15
+
+
+def test_operator_build_and_fp64_sweeps_bit_identical(gpu_lib):
+    """build_operator and 600 FP64 Jacobi sweeps reproduce the oracle bit for bit."""
+    c = stairstep_case_exact(False)
+    nx, ny, nz = c["nx"], c["ny"], c["nz"]
+    faces = [f.copy(order="F") for f in c["faces"]]
+    orc.enforce_stairstep_compatibility_3d(c["rhs"], c["solid"], c["body"], *faces, c["dx"], c["dy"], c["dz"])
+    coefs = orc.stairstep_coefficients(c["xc"], c["yc"], c["zc"], c["dx"], c["dy"], c["dz"])
+    src, diag, rdiag, iso = orc.build_operator(c["rhs"], c["solid"], c["body"], *faces, coefs, c["dx"], c["dy"],
+                                               c["dz"], False)
+    assert iso == 0
+    dfaces = [to_dev(f) for f in faces]
+    dax = [to_dev(c[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    drhs, dsolid = to_dev(c["rhs"]), to_dev(c["solid"])
+    import torch
+    n = nx * ny * nz
+    gsrc, gdiag, grd = (torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3))
+    iso_g = I()
+    bg = np.ascontiguousarray(c["body"])
+    rc = gpu_lib.fpm_stairstep_build_operator_dev(ptr(drhs), ptr(dsolid), bg.ctypes.data_as(ctypes.c_void_p),
+                                                  *[ptr(f) for f in dfaces], *[ptr(a) for a in dax], I(nx), I(ny),
+                                                  I(nz), I(0), ptr(gsrc), ptr(gdiag), ptr(grd), ctypes.byref(iso_g),
+                                                  stream_ptr())
+    assert rc == 0 and iso_g.value == 0
+    for g, o in ((gsrc, src), (gdiag, diag), (grd, rdiag)):
+        assert np.array_equal(from_dev(g, (nx, ny, nz)), o)
+    # 600 sweeps from a nonzero start, both sides in FP64
+    rng = np.random.default_rng(7)
+    a = np.zeros((nx + 2, ny + 2, nz), order="F")
+    a[1:nx + 1, 1:ny + 1, :] = rng.standard_normal((nx, ny, nz)) * (c["solid"][1:nx + 1, 1:ny + 1, :] == 0)
+    b = a.copy(order="F")
+    ga, gb = to_dev(a), to_dev(b)
+    rc = gpu_lib.fpm_stairstep_jacobi_sweeps_dev(ptr(ga), ptr(gb), ptr(gsrc), ptr(grd), *[ptr(x) for x in dax],
+                                                 I(nx), I(ny), I(nz), I(600), I(1), stream_ptr())
+    assert rc == 0
+    for s in range(600):
+        if s % 2 == 0:
+            orc.jacobi_sweep(a, b, src, rdiag, coefs)
+        else:
+            orc.jacobi_sweep(b, a, src, rdiag, coefs)
+    assert np.array_equal(from_dev(ga, a.shape), a)
+    val = D()
+    rc = gpu_lib.fpm_stairstep_operator_residual_dev(ptr(ga), ptr(gsrc), ptr(gdiag), *[ptr(x) for x in dax], I(nx),
+                                                     I(ny), I(nz), ctypes.byref(val), stream_ptr())
+    assert rc == 0 and val.value == orc.operator_residual(a, src, diag, coefs)
+
+
+def test_df_sweeps_within_1e12_after_2000(gpu_lib):
+    """Double-float sweeps stay within 1e-12 relative of FP64 after 2000 sweeps."""
+    c = stairstep_case_exact(False)
+    out_g = gpu_run(c, "jacobi_df", -1.0, 2000, ci=2000)
+    out_o = cpu_run(c, "jacobi", -1.0, 2000, ci=2000)
+    assert out_g["sweeps"] == 2000
+    assert rel_linf(out_g["phi"], out_o["phi"]) <= 1e-12
+    assert abs(out_g["res"] - out_o["res"]) <= 1e-12 * max(out_o["res"], 1e-300) + 1e-14
+
+
+@pytest.mark.parametrize("method", ["jacobi", "jacobi_df", "pcg"])
+def test_exact_linear_solution_gpu(gpu_lib, method):
+    """The reference's exactness test (test_stairstep_exact_3d.f90:40-50) on the GPU."""
+    c = stairstep_case_exact(True)
+    tol = 1e-10 if method == "pcg" else 1e-12
+    g = gpu_run(c, method, tol, 400000)
+    gx, gy, gz, vortex, adv, totals = g["terms"]
+    errors, ierr = exact_expectations(c, g["phi"], gx, gy, gz, vortex, totals)
+    assert abs(g["corr"]) < 1e-13 and abs(g["imb"]) < 1e-13
+    assert g["res"] <= 2 * tol and g["chk"] < 1e-9
+    assert errors[0] < 1e-9 and errors[1] < 1e-9 and errors[2] < 1e-9 and errors[3] == 0
+    assert ierr < 1e-10 and np.all(np.isfinite([g["res"], g["chk"], *errors, *totals]))
+    o = cpu_run(c, method if method != "jacobi_df" else "jacobi", tol, 400000)
+    assert abs(g["sweeps"] - o["sweeps"]) <= 50
+
+
+def test_fixed_jacobi_matches_oracle(gpu_lib):
+    """600 fixed sweeps (test_stairstep_exact_3d.f90:64): the fields agree to
+    the gauge-mean rounding, the max-norm residuals to 1e-13 relative."""
+    c = stairstep_case_exact(False)
+    g = gpu_run(c, "jacobi", -1.0, 600)
+    o = cpu_run(c, "jacobi", -1.0, 600)
+    assert g["sweeps"] == 600
+    assert np.abs(g["phi"] - o["phi"]).max() < 1e-15
+    assert abs(g["res"] - o["res"]) <= 1e-13 * o["res"]
+    assert abs(g["chk"] - o["chk"]) <= 1e-13 * o["chk"]
+
+
+def test_pcg_matches_oracle(gpu_lib):
+    """PCG to 1e-11 (test_stairstep_exact_3d.f90:65): potentials within 1e-9
+    relative max-norm, integrals within 1e-8 (the reference's threshold)."""
+    c = stairstep_case_exact(False)
+    g = gpu_run(c, "pcg", 1e-11, 100000)
+    o = cpu_run(c, "pcg", 1e-11, 100000)
+    assert g["res"] <= 2e-11
+    assert rel_linf(g["phi"], o["phi"]) <= 1e-9
+    assert np.abs(g["terms"][5] - o["terms"][5]).max() < 1e-8
+
+
+def test_terms_bit_identical_for_same_phi(gpu_lib):
+    from flowfpmpp_gb300 import stairstep as ss
+    c = stairstep_case_exact(False)
+    o = cpu_run(c, "pcg", 1e-11, 100000)
+    fl = c["flow"]
+    args = (o["phi"], fl["u"], fl["v"], fl["w"], fl["ox"], fl["oy"], fl["oz"], fl["ax"], fl["ay"], fl["az"],
+            c["solid"], c["body"], c["xc"], c["yc"], c["zc"], c["dx"], c["dy"], c["dz"], *o["faces"], c["bounds"])
+    g = ss.compute_stairstep_fpm_terms_3d(*args)
+    r = orc.compute_stairstep_fpm_terms_3d(*args)
+    for a, b in zip(g[:5], r[:5]):
+        assert np.array_equal(a, b)
+    assert np.abs(g[5] - r[5]).max() <= 1e-12 * np.abs(r[5]).max()
+    chk_g = ss.stairstep_residual_3d(o["phi"], c["rhs"], c["solid"], c["body"], *o["faces"], c["xc"], c["yc"],
+                                     c["zc"], c["dx"], c["dy"], c["dz"])
+    assert chk_g == o["chk"]
+
+
+@pytest.mark.parametrize("n,iters,cm_ref", [(12, 100, 0.897), (24, 200, 0.770)])
+def test_sphere_gpu_matches_table(gpu_lib, n, iters, cm_ref):
+    c = sphere_case(n)
+    g = gpu_run(c, "pcg", 1e-10, 2000000, ci=100)
+    rms, far, cm = sphere_errors(c, g["phi"])
+    assert g["sweeps"] == iters and round(cm, 3) == pytest.approx(cm_ref, abs=1e-12)
+
+
+def test_errors_mirror_reference_error_stops(gpu_lib):
+    from flowfpmpp_gb300 import FpmError
+    from flowfpmpp_gb300 import stairstep as ss
+    c = stairstep_case_exact(False)
+    args = lambda phi, solid: (phi, c["rhs"], solid, c["body"], *c["faces"], c["xc"], c["yc"], c["zc"], c["dx"],
+                               c["dy"], c["dz"], 1e-8, 10, 5)
+    with pytest.raises(FpmError) as e:
+        ss.solve_stairstep_poisson_3d(*args(c["phi"].copy(order="F"), c["solid"]), method="multigrid")
+    assert e.value.code == 1
+    # an isolated fluid cell: fluid (1,1,1) walled in by solid on its three inner faces
+    solid = c["solid"].copy(order="F")
+    solid[2, 1, 0] = 1
+    solid[1, 2, 0] = 1
+    solid[1, 1, 1] = 1
+    solid[1, 1, 0] = 0
+    with pytest.raises(FpmError) as e:
+        ss.solve_stairstep_poisson_3d(*args(c["phi"].copy(order="F"), solid))
+    assert e.value.code == 3
