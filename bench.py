@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark of the stair-step weighted-Jacobi solve (the reference's
+bandwidth benchmark) on a GB300.
+
+Workload (default, 'jacobi256'): 256^3 stretched grid (geometric ratio 1.01),
+four seeded blocked boxes of 8-40 cells per side (one touching the outer
+boundary), the phi_x influence problem (body_grad = e_x, zero outer data,
+compatibility applied), exactly 2000 weighted-Jacobi sweeps (tolerance < 0,
+one residual check at the end), gauge and final residual.  A step is one full
+solve_stairstep_poisson_3d call.
+
+  value  whole-job algorithmic HBM throughput, 32 B/cell/sweep (read phi, src,
+         rdiag; write phi'), device-resident inputs, CUDA events on the
+         solver's stream
+  e2e    the same metric through the host-array C ABI call (pinned host
+         buffers; host->device upload of every input and device->host copy of
+         phi inside the timed region)
+
+--impl reference times the CPU oracle (the reference's algorithm restated in
+C, OpenMP over z-planes, every host core) on a bounded sample of the same
+workload: the oracle is the reference arm because the reference itself is
+Fortran/OpenACC and no Fortran compiler is available.
+
+Multi-GPU: replicas only (each rank solves its own copy; no collective on the
+data path); value is the sum over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL_SWEEP = 32
+SWEEPS = 2000
+METRIC = "Jacobi HBM GB/s (weighted-Jacobi stair-step solve, 32 B/cell/sweep)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(n):
+    from flowfpmpp_gb300 import workloads
+    return workloads.boxes_c2(n=n)
+
+
+def config(n):
+    return {"workload": f"stair-step weighted Jacobi {n}^3, 4 boxes, phi_x, {SWEEPS} sweeps",
+            "grid": [n, n, n], "sweeps": SWEEPS, "method": "jacobi_df", "stretch_ratio": 1.01,
+            "l2_policy": "inputs larger than L2 (phi, src, rdiag, phi' = 4 x 134 MB per sweep)"}
+
+
+def algorithmic_gb(n, sweeps=SWEEPS):
+    return BYTES_PER_CELL_SWEEP * float(n) ** 3 * sweeps / 1e9
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+        return False
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm, smax = float(parts[1]), float(parts[2])
+            except ValueError:
+                continue
+            sms.append(sm)
+            mx = smax
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_sample(n, budget_s=12.0, threads=None):
+    """Oracle sweeps on the host cores: returns (GB/s, cores, sweeps, seconds)."""
+    import oracle as orc
+    f = workload(n)
+    faces = [a.copy(order="F") for a in f["faces"]]
+    orc.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], f["body"], *faces, f["dx"], f["dy"], f["dz"])
+    coefs = orc.stairstep_coefficients(f["xc"], f["yc"], f["zc"], f["dx"], f["dy"], f["dz"])
+    src, diag, rdiag, iso = orc.build_operator(f["rhs"], f["solid"], f["body"], *faces, coefs, f["dx"], f["dy"],
+                                               f["dz"], False)
+    a = f["phi"].copy(order="F")
+    b = a.copy(order="F")
+    cores = threads or orc.max_threads()
+    orc.set_threads(cores)
+    orc.jacobi_sweep(a, b, src, rdiag, coefs)  # warm
+    t0 = time.perf_counter()
+    sweeps = 0
+    while True:
+        for _ in range(5):
+            orc.jacobi_sweep(a, b, src, rdiag, coefs)
+            a, b = b, a
+        sweeps += 5
+        el = time.perf_counter() - t0
+        if el >= budget_s or sweeps >= SWEEPS:
+            break
+    orc.set_threads(1)
+    return BYTES_PER_CELL_SWEEP * float(n) ** 3 * sweeps / el / 1e9, cores, sweeps, el
+
+
+def run_reference(args):
+    """The reference arm: the CPU oracle on every host core, each step a
+    bounded sample (sweeps) of the same 2000-sweep workload."""
+    n = args.n
+    import oracle as orc
+    orc.build()
+    f = workload(n)
+    faces = [a.copy(order="F") for a in f["faces"]]
+    orc.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], f["body"], *faces, f["dx"], f["dy"], f["dz"])
+    coefs = orc.stairstep_coefficients(f["xc"], f["yc"], f["zc"], f["dx"], f["dy"], f["dz"])
+    src, diag, rdiag, iso = orc.build_operator(f["rhs"], f["solid"], f["body"], *faces, coefs, f["dx"], f["dy"],
+                                               f["dz"], False)
+    cores = orc.max_threads()
+    orc.set_threads(cores)
+    a = f["phi"].copy(order="F")
+    b = a.copy(order="F")
+    per_step = 20  # sweeps per step: a bounded sample of the 2000-sweep solve
+    for _ in range(args.warmup):
+        for _ in range(per_step):
+            orc.jacobi_sweep(a, b, src, rdiag, coefs)
+            a, b = b, a
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _ in range(per_step):
+            orc.jacobi_sweep(a, b, src, rdiag, coefs)
+            a, b = b, a
+    el = time.perf_counter() - t0
+    gbs = BYTES_PER_CELL_SWEEP * float(n) ** 3 * per_step * args.steps / el / 1e9
+    sample = f"{per_step} weighted-Jacobi sweeps of the {n}^3 operator per step (oracle, OpenMP over z-planes)"
+    line = {"metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded boxes)",
+            "config": config(n), "impl": "reference",
+            "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    from flowfpmpp_gb300 import build as fbuild
+    fbuild.build()
+    import flowfpmpp_gb300
+    from flowfpmpp_gb300 import stairstep as ss
+    lib = flowfpmpp_gb300.lib()
+    lib.fpm_kernel_launches.restype = ctypes.c_longlong
+
+    n = args.n
+    f = workload(n)
+    faces = [a.copy(order="F") for a in f["faces"]]
+    ss.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], f["body"], *faces, f["dx"], f["dy"], f["dz"])
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    d_phi = dev(f["phi"])
+    d_rhs, d_solid = dev(f["rhs"]), dev(f["solid"])
+    d_faces = [dev(a) for a in faces]
+    d_axes = [dev(f[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    bg = np.ascontiguousarray(f["body"])
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    sw, res = ctypes.c_int(), ctypes.c_double()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        d_phi.zero_()
+        rc = lib.fpm_solve_stairstep_poisson_3d_dev(
+            P(d_phi), P(d_rhs), P(d_solid), bg.ctypes.data_as(ctypes.c_void_p), *[P(t) for t in d_faces],
+            *[P(t) for t in d_axes], n, n, n, ctypes.c_double(-1.0), SWEEPS, SWEEPS, 2, ctypes.byref(sw),
+            ctypes.byref(res), ctypes.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+
+    for _ in range(args.warmup):
+        step()
+    assert sw.value == SWEEPS
+    barrier()
+    torch.cuda.synchronize()
+    lib.fpm_timing_enable(1)
+    lib.fpm_timing_read(0, ctypes.byref(ctypes.c_longlong()), ctypes.byref(ctypes.c_double()), 1)
+    launches0 = lib.fpm_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.fpm_kernel_launches() - launches0
+    lib.fpm_timing_enable(0)
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    nl, tot = ctypes.c_longlong(), ctypes.c_double()
+    lib.fpm_timing_read(0, ctypes.byref(nl), ctypes.byref(tot), 1)
+    sweep_ms = tot.value / max(nl.value, 1)
+    value = world * algorithmic_gb(n) / (ms / 1e3)
+    residual = res.value
+
+    # e2e through the host-array C ABI with pinned buffers
+    def pinned(a):
+        a = np.asarray(a)
+        ptr = lib.fpm_host_alloc(a.nbytes)
+        buf = (ctypes.c_char * a.nbytes).from_address(ptr)
+        out = np.frombuffer(buf, dtype=a.dtype).reshape(a.shape, order="F")
+        out[...] = a
+        return out, ptr
+
+    h_phi, p0 = pinned(f["phi"])
+    h_in = [pinned(x) for x in [f["rhs"], f["solid"], *faces, f["xc"], f["yc"], f["zc"], f["dx"], f["dy"], f["dz"]]]
+    h2d = h_phi.nbytes + sum(x[0].nbytes for x in h_in)
+    d2h = h_phi.nbytes
+
+    def e2e_step():
+        h_phi[...] = 0.0
+        args_ = [h_phi.ctypes.data_as(ctypes.c_void_p), h_in[0][0].ctypes.data_as(ctypes.c_void_p),
+                 h_in[1][0].ctypes.data_as(ctypes.c_void_p), bg.ctypes.data_as(ctypes.c_void_p)]
+        args_ += [x[0].ctypes.data_as(ctypes.c_void_p) for x in h_in[2:]]
+        rc = lib.fpm_solve_stairstep_poisson_3d(*args_, n, n, n, ctypes.c_double(-1.0), SWEEPS, SWEEPS, 2,
+                                                ctypes.byref(sw), ctypes.byref(res))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        e2e_step()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / max(1, args.steps // 2) * 1e3)
+    e2e_value = world * algorithmic_gb(n) / (e2e_ms / 1e3)
+    for x in [p0] + [x[1] for x in h_in]:
+        lib.fpm_host_free(ctypes.c_void_p(x))
+
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = BYTES_PER_CELL_SWEEP * float(n) ** 3 / (sweep_ms / 1e3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "jacobi_df_256cubed.json")
+    if n == 256 and os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    tx, ty, kc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    tuned = None
+    if lib.fpm_jacobi_df_config(n, n, n, ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(kc)) == 0:
+        tuned = {"tile": [tx.value, ty.value], "planes_per_cta": kc.value}
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        gbs, cores, nsw, el = cpu_sample(n)
+        cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
+               "sample": f"{nsw} weighted-Jacobi sweeps of the {n}^3 operator in {el:.1f} s (oracle, OpenMP)"}
+    cfg = config(n)
+    cfg["parallelism"] = f"replicas x{world}"
+    cfg["autotuned"] = tuned
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32x2 (double-float, 48-bit significand) sweeps, f64 residuals",
+            "data": "synthetic (seeded boxes)", "config": cfg,
+            "roofline": {"bound": "hbm", "kernel": "k_jacobi_df_tma", "achieved": achieved, "peak": peak,
+                         "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "avg_launch_us": sweep_ms * 1e3,
+                         "algorithmic_bytes_per_launch": BYTES_PER_CELL_SWEEP * n ** 3},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": e2e_ms},
+            "gpu_launches": int(launches), "clocks": clk.summary(), "final_residual": residual}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

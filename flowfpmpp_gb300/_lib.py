@@ -24,6 +24,7 @@ STATUS = {
     6: "FPM_E_CUDA",
     7: "FPM_E_NO_DEVICE",
     8: "FPM_E_LIMIT",
+    9: "FPM_E_TIMEOUT",
 }
 
 

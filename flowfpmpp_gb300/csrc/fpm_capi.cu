@@ -5,10 +5,15 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -19,6 +24,9 @@ namespace fpm {
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
+
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 struct Error {
   int code;
@@ -111,6 +119,46 @@ struct Trace {
   ~Trace() { nvtxRangePop(); }
 };
 
+// ---------------------------------------------------------------- kernel timing
+// Optional CUDA-event timing of the hot loops, on the stream they run on: one
+// event pair brackets each run of back-to-back launches of one kernel.
+struct KernelTimer {
+  std::mutex mu;
+  bool on = false;
+  struct Pending {
+    int id, launches;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  double ms[FPM_TIMER_COUNT] = {0};
+  long long launches[FPM_TIMER_COUNT] = {0};
+};
+static KernelTimer g_timer;
+
+struct TimedRun {
+  int id, n;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimedRun(int id_, int n_, cudaStream_t st_) : id(id_), n(n_), st(st_) {
+    bool on;
+    {
+      std::lock_guard<std::mutex> g(g_timer.mu);
+      on = g_timer.on;
+    }
+    if (on && n > 0) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, st);
+    }
+  }
+  ~TimedRun() {
+    if (!a) return;
+    cudaEventRecord(b, st);
+    std::lock_guard<std::mutex> g(g_timer.mu);
+    g_timer.pending.push_back({id, n, a, b});
+  }
+};
+
 // ---------------------------------------------------------------- solve
 struct SolveArgs {
   double* phi;
@@ -144,8 +192,11 @@ static double pcg_loop(const SolveArgs& a, const Dims& d, double* p, const doubl
     int chunk = ci - it % ci;
     if (chunk > a.max_sweeps - sw) chunk = a.max_sweeps - sw;
     CUDA_TRY(cudaMemsetAsync(&cm.S->iters, 0, sizeof(int), st));
-    for (int n = 0; n < chunk; n++)
-      CUDA_TRY(launch_pcg_iteration(d, a.phi, p, q, r, diag, rdiag, c, a.ax, cm.S, cm.rb, st));
+    {
+      TimedRun t(FPM_TIMER_PCG_ITER, chunk, st);
+      for (int n = 0; n < chunk; n++)
+        CUDA_TRY(launch_pcg_iteration(d, a.phi, p, q, r, diag, rdiag, c, a.ax, cm.S, cm.rb, st));
+    }
     const SolveScalars& h = read_scalars(cm.S, st);
     const int done = h.iters, halt = h.halt;
     sw += done;
@@ -185,9 +236,12 @@ static void jacobi_loop_f64(const SolveArgs& a, const Dims& d, double* next, con
   const int ci = a.ci < 1 ? 1 : a.ci;
   while (sw < a.max_sweeps && residual > a.tol) {
     int nsteps = ci < a.max_sweeps - sw ? ci : a.max_sweeps - sw;
-    for (int s = 0; s < nsteps; s++) {
-      CUDA_TRY(launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
-      std::swap(cur, oth);
+    {
+      TimedRun t(FPM_TIMER_JACOBI_F64, nsteps, st);
+      for (int s = 0; s < nsteps; s++) {
+        CUDA_TRY(launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
+        std::swap(cur, oth);
+      }
     }
     sw += nsteps;
     CUDA_TRY(launch_operator_residual(d, cur, src, diag, c, cm.S, cm.rb, st));
@@ -197,37 +251,141 @@ static void jacobi_loop_f64(const SolveArgs& a, const Dims& d, double* next, con
   *sweeps = sw;
 }
 
-// Same iteration in double-float: phi lives as f32 pairs between checks and
-// is written back to FP64 phi for each residual check.
-static void jacobi_loop_df(const SolveArgs& a, const Dims& d, double* next, const double* src, const double* diag,
+// ---------------------------------------------------------------- double-float Jacobi plan
+struct DfChoice {
+  int shape, kchunk;
+};
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, DfChoice> g_tune_cache;
+
+static int default_kchunk(const Dims& d, int shape) {
+  int tx, ty;
+  jacobi_df_shape(shape, &tx, &ty);
+  const long long tiles = (long long)((d.nx + tx - 1) / tx) * ((d.ny + ty - 1) / ty);
+  long long nzc = (152LL * 2 * 4) / tiles;  // about four waves of two CTAs per SM
+  if (nzc < 1) nzc = 1;
+  if (nzc > d.nz) nzc = d.nz;
+  int kc = (int)((d.nz + nzc - 1) / nzc);
+  if (kc < 4) kc = d.nz < 4 ? d.nz : 4;
+  return kc;
+}
+
+static JacobiDfPlan make_df_plan(Scratch& A, const Dims& d) {
+  JacobiDfPlan pl;
+  std::memset(&pl, 0, sizeof(pl));
+  pl.nx = d.nx;
+  pl.ny = d.ny;
+  pl.nz = d.nz;
+  pl.px = ((long long)d.nx + 2 + 1) & ~1LL;
+  const size_t nphi = (size_t)pl.px * (d.ny + 2) * d.nz;
+  pl.a = A.get<float2>(nphi);
+  pl.b = A.get<float2>(nphi);
+  pl.sr = A.get<float4>(d.ncell());
+  pl.coef = A.get<float2>(2 * (size_t)(d.nx + d.ny + d.nz));
+  pl.err = A.get<int>(1);
+  pl.shape = 0;
+  pl.kchunk = default_kchunk(d, 0);
+  return pl;
+}
+
+// Picks the tile shape and z-chunk: cached per grid size; otherwise, unless
+// FPM_DF_AUTOTUNE=0, times three sweeps a -> b of every candidate (a is left
+// unchanged, b is overwritten by the first real sweep anyway).
+static void df_choose(JacobiDfPlan& pl, cudaStream_t st) {
+  const Dims d{pl.nx, pl.ny, pl.nz};
+  const auto key = std::make_tuple(pl.nx, pl.ny, pl.nz);
+  // FPM_DF_SHAPE / FPM_DF_KCHUNK pin the choice (tests of every tile shape).
+  if (const char* fs = std::getenv("FPM_DF_SHAPE")) {
+    pl.shape = std::atoi(fs) % jacobi_df_num_shapes();
+    const char* fk = std::getenv("FPM_DF_KCHUNK");
+    pl.kchunk = fk ? std::atoi(fk) : default_kchunk(d, pl.shape);
+    if (pl.kchunk < 1) pl.kchunk = 1;
+    CUDA_TRY(jacobi_df_encode(pl));
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      pl.shape = it->second.shape;
+      pl.kchunk = it->second.kchunk;
+      CUDA_TRY(jacobi_df_encode(pl));
+      return;
+    }
+  }
+  const char* env = std::getenv("FPM_DF_AUTOTUNE");
+  DfChoice best{0, default_kchunk(d, 0)};
+  if (!(env && env[0] == '0')) {
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    for (int s = 0; s < jacobi_df_num_shapes(); s++) {
+      const int cands[5] = {default_kchunk(d, s), 8, 16, 32, 64};
+      for (int c = 0; c < 5; c++) {
+        const int kc = cands[c];
+        if (kc > d.nz || (c > 0 && kc == cands[0])) continue;
+        pl.shape = s;
+        pl.kchunk = kc;
+        CUDA_TRY(jacobi_df_encode(pl));
+        CUDA_TRY(jacobi_df_sweep(pl, pl.a, pl.b, st));
+        CUDA_TRY(cudaEventRecord(e0, st));
+        for (int r = 0; r < 3; r++) CUDA_TRY(jacobi_df_sweep(pl, pl.a, pl.b, st));
+        CUDA_TRY(cudaEventRecord(e1, st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = DfChoice{s, kc};
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune_cache[key] = best;
+  }
+  pl.shape = best.shape;
+  pl.kchunk = best.kchunk;
+  CUDA_TRY(jacobi_df_encode(pl));
+}
+
+static void check_df_err(const JacobiDfPlan& pl, cudaStream_t st) {
+  int h = 0;
+  CUDA_TRY(cudaMemcpyAsync(&h, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (h) throw Error{FPM_E_TIMEOUT, "double-float Jacobi pipeline wait timed out"};
+}
+
+// Same iteration in double-float: phi lives as f32 pairs in the TMA kernel's
+// layout between checks and is unpacked to FP64 phi for each residual check.
+static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src, const double* diag,
                            const double* rdiag, const double* coef, const Coefs& c, Scratch& A, Common& cm,
                            int* sweeps, cudaStream_t st) {
-  (void)next;
-  const long long np = d.npad(), nc = d.ncell(), ncoef = 2LL * (d.nx + d.ny + d.nz);
-  float2* pa = A.get<float2>(np);
-  float2* pb = A.get<float2>(np);
-  float2* sdf = A.get<float2>(nc);
-  float2* rdf = A.get<float2>(nc);
-  float2* cdf = A.get<float2>(ncoef);
-  CUDA_TRY(launch_to_df(a.phi, pa, np, st));
-  CUDA_TRY(launch_to_df(a.phi, pb, np, st));
-  CUDA_TRY(launch_to_df(src, sdf, nc, st));
-  CUDA_TRY(launch_to_df(rdiag, rdf, nc, st));
-  CUDA_TRY(launch_to_df(coef, cdf, ncoef, st));
-  float2 *cur = pa, *oth = pb;
+  JacobiDfPlan pl = make_df_plan(A, d);
+  CUDA_TRY(jacobi_df_pack(pl, a.phi, src, rdiag, coef, st));
+  df_choose(pl, st);
+  float2 *cur = pl.a, *oth = pl.b;
   double residual = HUGE_VAL;
   int sw = 0;
   const int ci = a.ci < 1 ? 1 : a.ci;
   while (sw < a.max_sweeps && residual > a.tol) {
     int nsteps = ci < a.max_sweeps - sw ? ci : a.max_sweeps - sw;
-    for (int s = 0; s < nsteps; s++) {
-      CUDA_TRY(launch_jacobi_df(d, cur, oth, sdf, rdf, cdf, st));
-      std::swap(cur, oth);
+    {
+      TimedRun t(FPM_TIMER_JACOBI_DF, nsteps, st);
+      for (int s = 0; s < nsteps; s++) {
+        CUDA_TRY(jacobi_df_sweep(pl, cur, oth, st));
+        std::swap(cur, oth);
+      }
     }
     sw += nsteps;
-    CUDA_TRY(launch_from_df_interior(d, cur, a.phi, st));
+    CUDA_TRY(jacobi_df_unpack(pl, cur, a.phi, st));
     CUDA_TRY(launch_operator_residual(d, a.phi, src, diag, c, cm.S, cm.rb, st));
     residual = read_scalars(cm.S, st).res;
+    check_df_err(pl, st);
   }
   *sweeps = sw;
 }
@@ -259,7 +417,7 @@ static void solve_dev(const SolveArgs& a, int* sweeps, double* residual, cudaStr
     Trace t1("stair-step iterations");
     if (use_pcg) pcg_loop(a, d, next, src, diag, rdiag, c, A, cm, &sw, st);
     else if (a.method == FPM_METHOD_JACOBI) jacobi_loop_f64(a, d, next, src, diag, rdiag, c, cm, &sw, st);
-    else jacobi_loop_df(a, d, next, src, diag, rdiag, coef, c, A, cm, &sw, st);
+    else jacobi_loop_df(a, d, src, diag, rdiag, coef, c, A, cm, &sw, st);
   }
   Trace t2("stair-step gauge");
   CUDA_TRY(launch_gauge(d, a.solid, a.phi, a.ax, cm.S, cm.rb, st));
@@ -294,6 +452,48 @@ using namespace fpm;
 extern "C" {
 
 const char* fpm_last_error(void) { return g_last_error.c_str(); }
+
+long long fpm_kernel_launches(void) { return g_launches.load(); }
+
+int fpm_timing_enable(int on) {
+  std::lock_guard<std::mutex> g(g_timer.mu);
+  g_timer.on = on != 0;
+  return FPM_OK;
+}
+
+int fpm_timing_read(int which, long long* launches, double* total_ms, int reset) {
+  return guarded([&] {
+    if (which < 0 || which >= FPM_TIMER_COUNT || !launches || !total_ms) throw Error{FPM_E_ARG, "bad timer id"};
+    std::lock_guard<std::mutex> g(g_timer.mu);
+    for (auto& p : g_timer.pending) {
+      CUDA_TRY(cudaEventSynchronize(p.b));
+      float ms = 0;
+      CUDA_TRY(cudaEventElapsedTime(&ms, p.a, p.b));
+      g_timer.ms[p.id] += ms;
+      g_timer.launches[p.id] += p.launches;
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    g_timer.pending.clear();
+    *launches = g_timer.launches[which];
+    *total_ms = g_timer.ms[which];
+    if (reset) {
+      g_timer.launches[which] = 0;
+      g_timer.ms[which] = 0;
+    }
+  });
+}
+
+int fpm_jacobi_df_config(int nx, int ny, int nz, int* tile_x, int* tile_y, int* kchunk) {
+  return guarded([&] {
+    if (!tile_x || !tile_y || !kchunk) throw Error{FPM_E_ARG, "null argument"};
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune_cache.find(std::make_tuple(nx, ny, nz));
+    if (it == g_tune_cache.end()) throw Error{FPM_E_ARG, "no double-float Jacobi run at this size yet"};
+    jacobi_df_shape(it->second.shape, tile_x, tile_y);
+    *kchunk = it->second.kchunk;
+  });
+}
 int fpm_version(void) { return 100; }
 
 void* fpm_host_alloc(size_t bytes) {
@@ -606,29 +806,26 @@ int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, con
     if (method == FPM_METHOD_JACOBI) {
       Coefs c = coef_views(coef, nx, ny, nz);
       double *cur = a, *oth = b;
+      TimedRun t(FPM_TIMER_JACOBI_F64, nsweeps, st);
       for (int s = 0; s < nsweeps; s++) {
         CUDA_TRY(launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
         std::swap(cur, oth);
       }
     } else {
-      const long long np = d.npad(), nc = d.ncell();
-      float2* pa = A.get<float2>(np);
-      float2* pb = A.get<float2>(np);
-      float2* sdf = A.get<float2>(nc);
-      float2* rdf = A.get<float2>(nc);
-      float2* cdf = A.get<float2>(ncoef);
-      CUDA_TRY(launch_to_df(a, pa, np, st));
-      CUDA_TRY(launch_to_df(b, pb, np, st));
-      CUDA_TRY(launch_to_df(src, sdf, nc, st));
-      CUDA_TRY(launch_to_df(rdiag, rdf, nc, st));
-      CUDA_TRY(launch_to_df(coef, cdf, ncoef, st));
-      float2 *cur = pa, *oth = pb;
-      for (int s = 0; s < nsweeps; s++) {
-        CUDA_TRY(launch_jacobi_df(d, cur, oth, sdf, rdf, cdf, st));
-        std::swap(cur, oth);
+      JacobiDfPlan pl = make_df_plan(A, d);
+      CUDA_TRY(jacobi_df_pack(pl, a, src, rdiag, coef, st));
+      df_choose(pl, st);
+      float2 *cur = pl.a, *oth = pl.b;
+      {
+        TimedRun t(FPM_TIMER_JACOBI_DF, nsweeps, st);
+        for (int s = 0; s < nsweeps; s++) {
+          CUDA_TRY(jacobi_df_sweep(pl, cur, oth, st));
+          std::swap(cur, oth);
+        }
       }
-      CUDA_TRY(launch_from_df_interior(d, pa, a, st));
-      CUDA_TRY(launch_from_df_interior(d, pb, b, st));
+      CUDA_TRY(jacobi_df_unpack(pl, pl.a, a, st));
+      CUDA_TRY(jacobi_df_unpack(pl, pl.b, b, st));
+      check_df_err(pl, st);
     }
     CUDA_TRY(cudaStreamSynchronize(st));
   });
@@ -650,6 +847,279 @@ int fpm_stairstep_operator_residual_dev(const double* phi, const double* src, co
     CUDA_TRY(launch_axis_coefs(Axes{xc, yc, zc, dx, dy, dz}, nx, ny, nz, coef, st));
     CUDA_TRY(launch_operator_residual(d, phi, src, diag, coef_views(coef, nx, ny, nz), cm.S, cm.rb, st));
     *value = read_scalars(cm.S, st).res;
+  });
+}
+
+static double read_res_cb(SolveScalars* S, cudaStream_t st, int) { return read_scalars(S, st).res; }
+
+static void face_sizes(int nx, int ny, int nz, size_t nf[6]) {
+  nf[0] = nf[1] = nface_x(ny, nz);
+  nf[2] = nf[3] = nface_y(nx, nz);
+  nf[4] = nf[5] = nface_z(nx, ny);
+}
+
+// Both Neumann compatibility variants (src/fpm_laplace_3d.f90:9-53, :150-217).
+static void neumann_compat_host(const double* rhs, double* const hf[6], const double* dx, const double* dy,
+                                const double* dz, int nx, int ny, int nz, int uniform, double* correction,
+                                double* imbalance) {
+  if (!rhs || !dx || !dy || !dz || !correction || !imbalance) throw Error{FPM_E_ARG, "null argument"};
+  for (int m = 0; m < 6; m++)
+    if (!hf[m]) throw Error{FPM_E_ARG, "null face array"};
+  if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+  require_device();
+  cudaStream_t st = 0;
+  const Dims d{nx, ny, nz};
+  Scratch A(st);
+  Common cm = make_common(A, d, st);
+  size_t nf[6];
+  face_sizes(nx, ny, nz, nf);
+  double* f[6];
+  for (int m = 0; m < 6; m++) f[m] = A.upload(hf[m], nf[m]);
+  const double* drhs = A.upload(rhs, d.ncell());
+  const double *ddx, *ddy, *ddz;
+  double area = 0;
+  if (uniform) {
+    ddx = A.upload(dx, 1);
+    ddy = A.upload(dy, 1);
+    ddz = A.upload(dz, 1);
+    area = 2.0 * ((double)(ny * nz) * *dy * *dz + (double)(nx * nz) * *dx * *dz + (double)(nx * ny) * *dx * *dy);
+  } else {
+    ddx = A.upload(dx, nx);
+    ddy = A.upload(dy, ny);
+    ddz = A.upload(dz, nz);
+  }
+  CUDA_TRY(launch_neumann_compat(nx, ny, nz, drhs, Faces{f[0], f[1], f[2], f[3], f[4], f[5]}, ddx, ddy, ddz,
+                                 uniform, area, cm.S, cm.rb, st));
+  const SolveScalars& h = read_scalars(cm.S, st);
+  *correction = h.corr;
+  *imbalance = h.red[3] - h.red[0];
+  for (int m = 0; m < 6; m++) download(hf[m], f[m], nf[m] * sizeof(double), st);
+  CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+int fpm_enforce_neumann_compatibility_3d(const double* rhs, double* xlo, double* xhi, double* ylo, double* yhi,
+                                         double* zlo, double* zhi, int nx, int ny, int nz, double dx, double dy,
+                                         double dz, double* correction, double* imbalance) {
+  return guarded([&] {
+    double* hf[6] = {xlo, xhi, ylo, yhi, zlo, zhi};
+    neumann_compat_host(rhs, hf, &dx, &dy, &dz, nx, ny, nz, 1, correction, imbalance);
+  });
+}
+
+int fpm_enforce_neumann_compatibility_nonuniform_3d(const double* rhs, double* xlo, double* xhi, double* ylo,
+                                                    double* yhi, double* zlo, double* zhi, const double* dx,
+                                                    const double* dy, const double* dz, int nx, int ny, int nz,
+                                                    double* correction, double* imbalance) {
+  return guarded([&] {
+    double* hf[6] = {xlo, xhi, ylo, yhi, zlo, zhi};
+    neumann_compat_host(rhs, hf, dx, dy, dz, nx, ny, nz, 0, correction, imbalance);
+  });
+}
+
+int fpm_solve_neumann_poisson_3d(double* phi, const double* rhs, const double* xlo, const double* xhi,
+                                 const double* ylo, const double* yhi, const double* zlo, const double* zhi, int nx,
+                                 int ny, int nz, double dx, double dy, double dz, double tolerance, int max_iterations,
+                                 int check_interval, int* iterations, double* final_residual) {
+  return guarded([&] {
+    if (!phi || !rhs || !xlo || !xhi || !ylo || !yhi || !zlo || !zhi || !iterations || !final_residual)
+      throw Error{FPM_E_ARG, "null argument"};
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = 0;
+    const Dims d{nx, ny, nz};
+    Scratch A(st);
+    Common cm = make_common(A, d, st);
+    const size_t nfull = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+    double* dphi = A.upload(phi, nfull);
+    const double* drhs = A.upload(rhs, d.ncell());
+    size_t nf[6];
+    face_sizes(nx, ny, nz, nf);
+    const double* hf[6] = {xlo, xhi, ylo, yhi, zlo, zhi};
+    double* f[6];
+    for (int m = 0; m < 6; m++) f[m] = A.upload(hf[m], nf[m]);
+    double* a = A.get<double>(d.ncell());
+    double* b = A.get<double>(d.ncell());
+    int rc = neumann_uniform_iterate(nx, ny, nz, dphi, drhs, Faces{f[0], f[1], f[2], f[3], f[4], f[5]}, dx, dy, dz,
+                                     tolerance, max_iterations, check_interval, a, b, cm.S, cm.rb, st, read_res_cb,
+                                     iterations, final_residual);
+    if (rc) throw Error{FPM_E_CUDA, cudaGetErrorString((cudaError_t)rc)};
+    download(phi, dphi, nfull * sizeof(double), st);
+    CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+int fpm_solve_neumann_poisson_nonuniform_3d(double* phi, const double* rhs, const double* xlo, const double* xhi,
+                                            const double* ylo, const double* yhi, const double* zlo,
+                                            const double* zhi, const double* xc, const double* yc, const double* zc,
+                                            const double* dx, const double* dy, const double* dz, int nx, int ny,
+                                            int nz, double tolerance, int max_iterations, int check_interval,
+                                            int* iterations, double* final_residual) {
+  return guarded([&] {
+    if (!phi || !rhs || !xlo || !xhi || !ylo || !yhi || !zlo || !zhi || !xc || !yc || !zc || !dx || !dy || !dz ||
+        !iterations || !final_residual)
+      throw Error{FPM_E_ARG, "null argument"};
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = 0;
+    const Dims d{nx, ny, nz};
+    Scratch A(st);
+    Common cm = make_common(A, d, st);
+    double* dphi = A.upload(phi, d.ncell());
+    const double* drhs = A.upload(rhs, d.ncell());
+    size_t nf[6];
+    face_sizes(nx, ny, nz, nf);
+    const double* hf[6] = {xlo, xhi, ylo, yhi, zlo, zhi};
+    double* f[6];
+    for (int m = 0; m < 6; m++) f[m] = A.upload(hf[m], nf[m]);
+    Axes ax{A.upload(xc, nx), A.upload(yc, ny), A.upload(zc, nz), A.upload(dx, nx), A.upload(dy, ny), A.upload(dz, nz)};
+    double* b = A.get<double>(d.ncell());
+    double* coef = A.get<double>(2 * (size_t)(nx + ny + nz));
+    int rc = neumann_nonuniform_iterate(nx, ny, nz, dphi, drhs, Faces{f[0], f[1], f[2], f[3], f[4], f[5]}, ax,
+                                        tolerance, max_iterations, check_interval, b, coef, cm.S, cm.rb, st,
+                                        read_res_cb, iterations, final_residual);
+    if (rc) throw Error{FPM_E_CUDA, cudaGetErrorString((cudaError_t)rc)};
+    download(phi, dphi, d.ncell() * sizeof(double), st);
+    CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+int fpm_compute_fpm_terms_uniform_3d(const double* phi, const double* u, const double* v, const double* w,
+                                     const double* ox, const double* oy, const double* oz, const double* ax,
+                                     const double* ay, const double* az, const int32_t* fluid, double* gx, double* gy,
+                                     double* gz, double* vortex, double* advection, double* totals, int nx, int ny,
+                                     int nz, double dx, double dy, double dz) {
+  return guarded([&] {
+    const double* in[9] = {u, v, w, ox, oy, oz, ax, ay, az};
+    double* hout[5] = {gx, gy, gz, vortex, advection};
+    if (!phi || !fluid || !totals) throw Error{FPM_E_ARG, "null argument"};
+    for (int m = 0; m < 9; m++)
+      if (!in[m]) throw Error{FPM_E_ARG, "null flow field"};
+    for (int m = 0; m < 5; m++)
+      if (!hout[m]) throw Error{FPM_E_ARG, "null output"};
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = 0;
+    const Dims d{nx, ny, nz};
+    const size_t nc = d.ncell();
+    Scratch A(st);
+    Common cm = make_common(A, d, st);
+    const double* din[9];
+    for (int m = 0; m < 9; m++) din[m] = A.upload(in[m], nc);
+    double* out[5];
+    for (int m = 0; m < 5; m++) out[m] = A.get<double>(nc);
+    const double* dphi = A.upload(phi, (size_t)(nx + 2) * (ny + 2) * (nz + 2));
+    Flow fl{din[0], din[1], din[2], din[3], din[4], din[5], din[6], din[7], din[8]};
+    CUDA_TRY(launch_terms_uniform(nx, ny, nz, dphi, fl, A.upload(fluid, nc), dx, dy, dz,
+                                  TermsOut{out[0], out[1], out[2], out[3], out[4]}, cm.S, cm.rb, st));
+    const SolveScalars& h = read_scalars(cm.S, st);
+    totals[0] = h.red[0];
+    totals[1] = h.red[1];
+    for (int m = 0; m < 5; m++) download(hout[m], out[m], nc * sizeof(double), st);
+    CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+int fpm_compute_fpm_terms_nonuniform_3d(const double* phi, const double* u, const double* v, const double* w,
+                                        const double* ox, const double* oy, const double* oz, const double* ax,
+                                        const double* ay, const double* az, const int32_t* fluid, const double* xc,
+                                        const double* yc, const double* zc, const double* dx, const double* dy,
+                                        const double* dz, const double* xlo, const double* xhi, const double* ylo,
+                                        const double* yhi, const double* zlo, const double* zhi,
+                                        const double* bounds, double* gx, double* gy, double* gz, double* vortex,
+                                        double* advection, double* totals, int nx, int ny, int nz) {
+  return guarded([&] {
+    const double* in[9] = {u, v, w, ox, oy, oz, ax, ay, az};
+    double* hout[5] = {gx, gy, gz, vortex, advection};
+    const double* hf[6] = {xlo, xhi, ylo, yhi, zlo, zhi};
+    if (!phi || !fluid || !totals || !bounds || !xc || !yc || !zc || !dx || !dy || !dz)
+      throw Error{FPM_E_ARG, "null argument"};
+    for (int m = 0; m < 9; m++)
+      if (!in[m]) throw Error{FPM_E_ARG, "null flow field"};
+    for (int m = 0; m < 5; m++)
+      if (!hout[m]) throw Error{FPM_E_ARG, "null output"};
+    for (int m = 0; m < 6; m++)
+      if (!hf[m]) throw Error{FPM_E_ARG, "null face array"};
+    if (nx < 2 || ny < 2 || nz < 2)
+      throw Error{FPM_E_SIZE, "nonuniform 3-D FPM kernel requires at least two cells per direction"};
+    require_device();
+    cudaStream_t st = 0;
+    const Dims d{nx, ny, nz};
+    const size_t nc = d.ncell();
+    Scratch A(st);
+    Common cm = make_common(A, d, st);
+    const double* din[9];
+    for (int m = 0; m < 9; m++) din[m] = A.upload(in[m], nc);
+    double* out[5];
+    for (int m = 0; m < 5; m++) out[m] = A.get<double>(nc);
+    size_t nf[6];
+    face_sizes(nx, ny, nz, nf);
+    double* f[6];
+    for (int m = 0; m < 6; m++) f[m] = A.upload(hf[m], nf[m]);
+    Axes axes{A.upload(xc, nx), A.upload(yc, ny), A.upload(zc, nz), A.upload(dx, nx), A.upload(dy, ny),
+              A.upload(dz, nz)};
+    Flow fl{din[0], din[1], din[2], din[3], din[4], din[5], din[6], din[7], din[8]};
+    CUDA_TRY(launch_terms_nonuniform(nx, ny, nz, A.upload(phi, nc), fl, A.upload(fluid, nc), axes,
+                                     Faces{f[0], f[1], f[2], f[3], f[4], f[5]}, bounds,
+                                     TermsOut{out[0], out[1], out[2], out[3], out[4]}, cm.S, cm.rb, st));
+    const SolveScalars& h = read_scalars(cm.S, st);
+    totals[0] = h.red[0];
+    totals[1] = h.red[1];
+    for (int m = 0; m < 5; m++) download(hout[m], out[m], nc * sizeof(double), st);
+    CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+int fpm_partition_terms_2d(const double* phi, const double* g, const double* u, const double* v,
+                           const uint8_t* solid, const double* xf, const double* yf, const double* kin,
+                           const double* ring, double dt, double nu, int nx, int ny, double* terms,
+                           double* vif_density, double* omega, int slip_body) {
+  return guarded([&] {
+    if (!phi || !g || !u || !v || !solid || !xf || !yf || !kin || !ring || !terms || !vif_density || !omega)
+      throw Error{FPM_E_ARG, "null argument"};
+    if (nx < 1 || ny < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = 0;
+    Scratch A(st);
+    const size_t n2 = (size_t)nx * ny, L = 2 * (size_t)nx + 2 * (size_t)ny;
+    Common cm;
+    cm.S = A.get<SolveScalars>(1);
+    CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
+    const int nb = ((nx + 31) / 32) * ((ny + 7) / 8);
+    cm.rb.max_blocks = nb;
+    cm.rb.partials = A.get<double>((size_t)4 * nb);
+    cm.rb.ticket = A.get<unsigned int>(1);
+    CUDA_TRY(cudaMemsetAsync(cm.rb.ticket, 0, sizeof(unsigned int), st));
+    Part2D p;
+    p.phi = A.upload(phi, n2);
+    p.u = A.upload(u, n2);
+    p.v = A.upload(v, n2);
+    p.xf = A.upload(xf, (size_t)nx + 1);
+    p.yf = A.upload(yf, (size_t)ny + 1);
+    p.ring = A.upload(ring, 4 * L);
+    p.solid = A.upload(solid, n2);
+    p.g0 = g[0];
+    p.g1 = g[1];
+    p.k1 = kin[0];
+    p.k2 = kin[1];
+    p.k3 = kin[2];
+    p.k4 = kin[3];
+    p.k5 = kin[4];
+    p.k6 = kin[5];
+    p.dt = dt;
+    p.nu = nu;
+    p.nx = nx;
+    p.ny = ny;
+    p.slip = slip_body ? 1 : 0;
+    double* scratch[4];
+    for (int m = 0; m < 4; m++) scratch[m] = A.get<double>(n2);
+    double* dvif = A.get<double>(n2);
+    double* domega = A.get<double>(n2);
+    CUDA_TRY(launch_partition_2d(p, scratch[0], scratch[1], scratch[2], scratch[3], dvif, domega, cm.S, cm.rb, st));
+    const SolveScalars& h = read_scalars(cm.S, st);
+    for (int m = 0; m < 4; m++) terms[m] = h.red[m];
+    download(vif_density, dvif, n2 * sizeof(double), st);
+    download(omega, domega, n2 * sizeof(double), st);
+    CUDA_TRY(cudaStreamSynchronize(st));
   });
 }
 

@@ -1,5 +1,6 @@
 // Internal host-side declarations shared by the kernel files and the C ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -13,7 +14,7 @@ namespace fpm {
 // these directly, so a PCG chunk runs without any host round trip.
 struct SolveScalars {
   double rz, pq, alpha, beta, rz_new;  // PCG recurrences
-  double red[4];                       // generic reduction outputs
+  double red[6];                       // generic reduction outputs
   double res;                          // max-norm residual of L(phi)-f
   double mean;                         // gauge mean
   double corr;                         // compatibility correction
@@ -82,11 +83,62 @@ cudaError_t launch_terms(const Dims& d, const double* phi, const Flow& fl, const
                          const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o, SolveScalars* S,
                          const RedBuf& rb, cudaStream_t st);
 
-// Double-float fast Jacobi (fpm_stairstep_df.cu).
+// FP64 -> double-float conversion (fpm_stairstep_df.cu).
 cudaError_t launch_to_df(const double* x, float2* y, long long n, cudaStream_t st);
-cudaError_t launch_from_df_interior(const Dims& d, const float2* x, double* y, cudaStream_t st);
-cudaError_t launch_jacobi_df(const Dims& d, const float2* a, float2* b, const float2* src, const float2* rdiag,
-                             const float2* coef_df, cudaStream_t st);
+
+// TMA-streamed double-float Jacobi (fpm_jacobi_tma.cu).
+struct JacobiDfPlan {
+  int nx, ny, nz;
+  long long px;      // x pitch (elements) of the internal phi layout, even
+  int kchunk;        // planes per CTA along z
+  int shape;         // index into the tile-shape table
+  float2 *a, *b;     // internal phi buffers, px * (ny+2) * nz
+  float4* sr;        // (src, rdiag) as double-float, nx * ny * nz
+  float2* coef;      // cw, ce, cs, cn, cb, ct as double-float
+  int* err;          // set to 1 if a pipeline wait timed out
+  CUtensorMap tm_a, tm_b, tm_sr;
+};
+int jacobi_df_num_shapes();
+cudaError_t jacobi_df_pack(JacobiDfPlan& pl, const double* phi, const double* src, const double* rdiag,
+                           const double* coef64, cudaStream_t st);
+cudaError_t jacobi_df_encode(JacobiDfPlan& pl);
+void jacobi_df_shape(int shape, int* tx, int* ty);
+cudaError_t jacobi_df_sweep(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st);
+cudaError_t jacobi_df_unpack(const JacobiDfPlan& pl, const float2* cur, double* phi, cudaStream_t st);
+
+// ---- no-body Neumann solvers and densities (fpm_laplace.cu) --------------
+cudaError_t launch_neumann_compat(int nx, int ny, int nz, const double* rhs, Faces f, const double* dx,
+                                  const double* dy, const double* dz, int uniform, double area_uniform,
+                                  SolveScalars* S, const RedBuf& rb, cudaStream_t st);
+typedef double (*ReadRes)(SolveScalars*, cudaStream_t, int);
+int neumann_uniform_iterate(int nx, int ny, int nz, double* phi, const double* rhs, Faces f, double dx, double dy,
+                            double dz, double tol, int max_it, int ci, double* a, double* b, SolveScalars* S,
+                            const RedBuf& rb, cudaStream_t st, ReadRes read_res, int* iterations,
+                            double* final_residual);
+int neumann_nonuniform_iterate(int nx, int ny, int nz, double* phi, const double* rhs, Faces f, const Axes& ax,
+                               double tol, int max_it, int ci, double* b, double* coef, SolveScalars* S,
+                               const RedBuf& rb, cudaStream_t st, ReadRes read_res, int* iterations,
+                               double* final_residual);
+cudaError_t launch_terms_uniform(int nx, int ny, int nz, const double* phi, const Flow& fl, const int32_t* fluid,
+                                 double dx, double dy, double dz, const TermsOut& o, SolveScalars* S,
+                                 const RedBuf& rb, cudaStream_t st);
+cudaError_t launch_terms_nonuniform(int nx, int ny, int nz, const double* phi, const Flow& fl, const int32_t* fluid,
+                                    const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o,
+                                    SolveScalars* S, const RedBuf& rb, cudaStream_t st);
+
+// ---- 2-D force partition (fpm_partition2d.cu) ------------------------------
+struct Part2D {
+  const double *phi, *u, *v, *xf, *yf, *ring;
+  const uint8_t* solid;
+  double g0, g1, k1, k2, k3, k4, k5, k6, dt, nu;
+  int nx, ny, slip;
+};
+cudaError_t launch_partition_2d(const Part2D& p, double* nxf, double* nyf, double* gpx, double* gpy,
+                                double* vif_density, double* omega, SolveScalars* S, const RedBuf& rb,
+                                cudaStream_t st);
+
+// Host-side count of kernel launches made by this library (fpm_capi.cu).
+void note_launch();
 
 // ---- error reporting (fpm_capi.cu) ----------------------------------------
 void set_error(const std::string& msg);

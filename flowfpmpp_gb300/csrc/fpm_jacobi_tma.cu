@@ -1,0 +1,385 @@
+// Weighted-Jacobi sweep (src/fpm_stairstep_mpi_3d.f90:384-399) in
+// double-float arithmetic, streamed through shared memory by TMA.
+//
+// Each CTA owns a TX x TY column of interior cells and marches k through a
+// chunk of planes.  One elected thread keeps a 4-deep ring of phi planes
+// (tile plus one-cell x-y halo) and a 3-deep ring of (src, rdiag) planes in
+// flight with cp.async.bulk.tensor, completion tracked by mbarriers; every
+// thread reads its seven phi values and its src/rdiag from shared memory, so
+// global memory sees each field once per sweep (the x-y halo re-reads hit L2)
+// and the DRAM stream never waits on a dependent load.
+//
+// Internal layout (owned by this module, not the caller's):
+//   phi   float2 (hi, lo), padded (0:nx+1, 0:ny+1, 1:nz) with x pitch PX even
+//   sr    (src_hi, src_lo, rdiag_hi, rdiag_lo) per interior cell, x fastest
+// The pitch keeps every TMA row start on a 16-byte boundary: the phi box
+// starts at x = TX*bx (TX even) and spans TX+2 elements of 8 bytes.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "fpm_internal.h"
+
+namespace fpm {
+
+namespace {
+
+constexpr int kPhiStages = 4;
+constexpr int kSrStages = 3;
+constexpr unsigned kSpinLimit = 1u << 20;  // x ~1 us suspend hint: about a second
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Bounded wait: false if the phase did not complete within the spin limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (unsigned it = 0; it < kSpinLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(1000u)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+}  // namespace
+
+// 0.2 as hi + lo.
+#define DF_POINT2 make_float2(0.2f, -2.9802322831784522e-09f)
+
+// Unnormalised double-float accumulator: value = s + e.  Adding an exact
+// product c*a costs 12 FP32 operations (TwoProd with FMA, TwoSum into s, the
+// two error terms into e); normalisation is deferred to the end of the sum.
+struct DfAcc {
+  float s, e;
+};
+__device__ __forceinline__ void acc_prod(DfAcc& A, float2 c, float2 a) {
+  const float p = c.x * a.x;
+  float pe = fmaf(c.x, a.x, -p);
+  pe = fmaf(c.x, a.y, pe);
+  pe = fmaf(c.y, a.x, pe);
+  const float s = A.s + p;
+  const float bb = s - A.s;
+  const float t = (A.s - (s - bb)) + (p - bb);
+  A.s = s;
+  A.e += t + pe;
+}
+__device__ __forceinline__ float2 acc_norm(const DfAcc& A) {
+  const float h = A.s + A.e;
+  return make_float2(h, A.e - (h - A.s));
+}
+// b = 0.2 a + rdiag * s for double-float a, rdiag, s.
+__device__ __forceinline__ float2 df_jacobi_finish(float2 a, float2 rd, float2 s) {
+  const float2 P2 = DF_POINT2;
+  const float p = P2.x * a.x;
+  float pe = fmaf(P2.x, a.x, -p);
+  pe = fmaf(P2.x, a.y, pe);
+  pe = fmaf(P2.y, a.x, pe);
+  const float q = rd.x * s.x;
+  float qe = fmaf(rd.x, s.x, -q);
+  qe = fmaf(rd.x, s.y, qe);
+  qe = fmaf(rd.y, s.x, qe);
+  const float u = p + q;
+  const float bb = u - p;
+  const float t = (p - (u - bb)) + (q - bb);
+  const float e = t + (pe + qe);
+  const float h = u + e;
+  return make_float2(h, e - (h - u));
+}
+
+// One CTA: TX x (TYB*CY) interior cells; thread (tx, tyb) owns rows
+// tyb + r*TYB (r < CY) of its column, so a warp reads contiguous rows of the
+// shared-memory plane.
+template <int TX, int TYB, int CY>
+__global__ void __launch_bounds__(TX* TYB, 2) k_jacobi_df_tma(const __grid_constant__ CUtensorMap tm_phi,
+                                                             const __grid_constant__ CUtensorMap tm_sr,
+                                                             float2* __restrict__ out,
+                                                             const float2* __restrict__ coef, int nx, int ny, int nz,
+                                                             long long px, int kchunk, int* err) {
+  constexpr int TY = TYB * CY, PW = TX + 2, PH = TY + 2;
+  constexpr uint32_t kPhiBytes = PW * PH * 8, kSrBytes = TX * TY * 16;
+  constexpr uint32_t kPhiStage = (kPhiBytes + 127) / 128 * 128;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float4* sr_s = reinterpret_cast<float4*>(smem + kPhiStages * kPhiStage);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(sr_s) + kSrStages * kSrBytes);
+  const uint32_t phi_base = smem_u32(smem), sr_base = smem_u32(sr_s), bar_base = smem_u32(bars);
+
+  const int tid = threadIdx.x, tx = tid % TX, tyb = tid / TX;
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int k0 = blockIdx.z * kchunk + 1;
+  const int k1 = min(nz, k0 + kchunk - 1);
+  const int i = TX * bx + tx + 1;
+  const int jbase = TY * by + tyb + 1;
+
+  if (tid == 0) {
+    for (int s = 0; s < kPhiStages + kSrStages; s++) mbar_init(bar_base + 8 * s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // Plane p of phi goes to ring slot (p - (k0-1)) % 4; its n-th use of the
+  // slot completes phase n.  (src, rdiag) plane p goes to slot (p - k0) % 3.
+  auto issue_phi = [&](int p) {
+    const int u = p - (k0 - 1), s = u % kPhiStages;
+    const uint32_t bar = bar_base + 8 * s;
+    mbar_expect_tx(bar, kPhiBytes);
+    tma_load_3d(phi_base + s * kPhiStage, &tm_phi, TX * bx, TY * by, p - 1, bar);
+  };
+  auto issue_sr = [&](int p) {
+    const int s = (p - k0) % kSrStages;
+    const uint32_t bar = bar_base + 8 * (kPhiStages + s);
+    mbar_expect_tx(bar, kSrBytes);
+    tma_load_3d(sr_base + s * kSrBytes, &tm_sr, 2 * TX * bx, TY * by, p - 1, bar);
+  };
+  auto phi_ready = [&](int p) {
+    const int u = p - (k0 - 1);
+    return mbar_wait(bar_base + 8 * (u % kPhiStages), (uint32_t)((u / kPhiStages) & 1));
+  };
+  auto sr_ready = [&](int p) {
+    const int u = p - k0;
+    return mbar_wait(bar_base + 8 * (kPhiStages + u % kSrStages), (uint32_t)((u / kSrStages) & 1));
+  };
+
+  int next_phi = k0 - 1, next_sr = k0;
+  if (tid == 0) {
+    for (; next_phi <= k0 + 2 && next_phi <= k1 + 1; next_phi++) issue_phi(next_phi);
+    for (; next_sr <= k0 + 2 && next_sr <= k1; next_sr++) issue_sr(next_sr);
+  }
+
+  const bool col = i <= nx;
+  float2 cwi = make_float2(0.f, 0.f), cei = cwi;
+  if (col) {
+    cwi = coef[i - 1];
+    cei = coef[nx + i - 1];
+  }
+  float2 csj[CY], cnj[CY];
+#pragma unroll
+  for (int r = 0; r < CY; r++) {
+    const int j = jbase + r * TYB;
+    csj[r] = j <= ny ? coef[2 * nx + j - 1] : make_float2(0.f, 0.f);
+    cnj[r] = j <= ny ? coef[2 * nx + ny + j - 1] : make_float2(0.f, 0.f);
+  }
+  const float2* cb = coef + 2 * nx + 2 * ny;
+  const float2* ct = cb + nz;
+  const long long plane = px * (long long)(ny + 2);
+  float2* outp = out + (long long)i + px * (long long)jbase + plane * (long long)(k0 - 1);
+
+  bool failed = false;
+  int kfail = k0;
+  bool ok = phi_ready(k0 - 1) && phi_ready(k0);
+  for (int k = k0; k <= k1; k++) {
+    ok = ok && phi_ready(k + 1) && sr_ready(k);
+    if (ok && col) {
+      const int um = k - 1 - (k0 - 1);
+      const float2* pm = reinterpret_cast<const float2*>(smem + (um % kPhiStages) * kPhiStage);
+      const float2* pc = reinterpret_cast<const float2*>(smem + ((um + 1) % kPhiStages) * kPhiStage);
+      const float2* pp = reinterpret_cast<const float2*>(smem + ((um + 2) % kPhiStages) * kPhiStage);
+      const float4* srp = sr_s + ((k - k0) % kSrStages) * (TX * TY);
+      // z neighbours clamp at the domain ends like a(i,j,max(k-1,1)); there
+      // cb(1) = ct(nz) = 0, so reading the zero-filled plane gives the same sum.
+      const float2 cbk = cb[k - 1], ctk = ct[k - 1];
+#pragma unroll
+      for (int r = 0; r < CY; r++) {
+        const int j = jbase + r * TYB;
+        if (j <= ny) {
+          const int c0 = (tx + 1) + PW * (tyb + r * TYB + 1);
+          const float4 sr = srp[tx + TX * (tyb + r * TYB)];
+          const float2 ac = pc[c0];
+          DfAcc A{sr.x, sr.y};
+          acc_prod(A, cwi, pc[c0 - 1]);
+          acc_prod(A, cei, pc[c0 + 1]);
+          acc_prod(A, csj[r], pc[c0 - PW]);
+          acc_prod(A, cnj[r], pc[c0 + PW]);
+          acc_prod(A, cbk, pm[c0]);
+          acc_prod(A, ctk, pp[c0]);
+          outp[px * (r * TYB)] = df_jacobi_finish(ac, make_float2(sr.z, sr.w), acc_norm(A));
+        }
+      }
+    }
+    outp += plane;
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      kfail = k;
+      break;
+    }
+    if (tid == 0) {
+      if (next_phi <= k1 + 1) issue_phi(next_phi++);
+      if (next_sr <= k1) issue_sr(next_sr++);
+    }
+  }
+  if (failed && tid == 0) {
+    atomicExch(err, 1);
+    // Drain the copies still in flight (bounded) before the CTA exits:
+    // phases already complete return at once.
+    for (int p = kfail - 1; p < next_phi; p++) phi_ready(p);
+    for (int p = kfail; p < next_sr; p++) sr_ready(p);
+  }
+}
+
+// ---------------------------------------------------------------- packing
+__global__ void k_pack_phi_df(Dims d, const double* __restrict__ phi, float2* __restrict__ out, long long px) {
+  const long long n = d.npad();
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n; m += (long long)gridDim.x * blockDim.x) {
+    const long long i = m % (d.nx + 2), r = m / (d.nx + 2);  // r = j + (ny+2)(k-1)
+    out[i + px * r] = df_from_double(phi[m]);
+  }
+}
+__global__ void k_unpack_phi_df(Dims d, const float2* __restrict__ in, double* __restrict__ phi, long long px) {
+  const int i = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  if (i > d.nx || j > d.ny) return;
+  for (int k = blockIdx.z + 1; k <= d.nz; k += gridDim.z)
+    phi[d.ph(i, j, k)] = df_to_double(in[(long long)i + px * ((long long)j + (long long)(d.ny + 2) * (k - 1))]);
+}
+__global__ void k_pack_sr(long long n, const double* __restrict__ src, const double* __restrict__ rdiag,
+                          float4* __restrict__ out) {
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n; m += (long long)gridDim.x * blockDim.x) {
+    const float2 s = df_from_double(src[m]), r = df_from_double(rdiag[m]);
+    out[m] = make_float4(s.x, s.y, r.x, r.y);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+static bool encode_3d(CUtensorMap* map, void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t stride1_bytes,
+                      uint64_t stride2_bytes, uint32_t b0, uint32_t b1) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {d0, d1, d2};
+  cuuint64_t strides[2] = {stride1_bytes, stride2_bytes};
+  cuuint32_t box[3] = {b0, b1, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+struct TileShape {
+  int tx, tyb, cy;  // tile = tx x (tyb*cy); threads = tx*tyb
+};
+static const TileShape kShapes[] = {{64, 4, 2}, {32, 8, 2}, {64, 2, 4}, {32, 4, 4}, {128, 2, 2},
+                                    {64, 4, 1}, {32, 8, 1}, {64, 8, 1}};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+
+template <int TX, int TYB, int CY>
+static size_t shape_smem() {
+  constexpr size_t ty = TYB * CY;
+  constexpr size_t phi = ((TX + 2) * (ty + 2) * 8 + 127) / 128 * 128;
+  return kPhiStages * phi + kSrStages * (size_t)TX * ty * 16 + (kPhiStages + kSrStages) * 8;
+}
+
+template <int TX, int TYB, int CY>
+static cudaError_t launch_shape(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st) {
+  const CUtensorMap& tm = (src_phi == pl.a) ? pl.tm_a : pl.tm_b;
+  const size_t smem = shape_smem<TX, TYB, CY>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_jacobi_df_tma<TX, TYB, CY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  constexpr int TY = TYB * CY;
+  dim3 grid((pl.nx + TX - 1) / TX, (pl.ny + TY - 1) / TY, (pl.nz + pl.kchunk - 1) / pl.kchunk);
+  k_jacobi_df_tma<TX, TYB, CY><<<grid, TX * TYB, smem, st>>>(tm, pl.tm_sr, dst_phi, pl.coef, pl.nx, pl.ny, pl.nz,
+                                                             pl.px, pl.kchunk, pl.err); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t jacobi_df_sweep(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st) {
+  switch (pl.shape) {
+    case 0: return launch_shape<64, 4, 2>(pl, src_phi, dst_phi, st);
+    case 1: return launch_shape<32, 8, 2>(pl, src_phi, dst_phi, st);
+    case 2: return launch_shape<64, 2, 4>(pl, src_phi, dst_phi, st);
+    case 3: return launch_shape<32, 4, 4>(pl, src_phi, dst_phi, st);
+    case 4: return launch_shape<128, 2, 2>(pl, src_phi, dst_phi, st);
+    case 5: return launch_shape<64, 4, 1>(pl, src_phi, dst_phi, st);
+    case 6: return launch_shape<32, 8, 1>(pl, src_phi, dst_phi, st);
+    default: return launch_shape<64, 8, 1>(pl, src_phi, dst_phi, st);
+  }
+}
+
+int jacobi_df_num_shapes() { return kNumShapes; }
+
+// Packs FP64 phi / src / rdiag / coefficients into the internal double-float
+// arrays.  a/b/sr/coef/err are allocated by the caller: a and b hold
+// px*(ny+2)*nz float2, sr nx*ny*nz float4, coef 2(nx+ny+nz) float2.
+cudaError_t jacobi_df_pack(JacobiDfPlan& pl, const double* phi, const double* src, const double* rdiag,
+                           const double* coef64, cudaStream_t st) {
+  const Dims d{pl.nx, pl.ny, pl.nz};
+  const size_t nphi = sizeof(float2) * pl.px * (pl.ny + 2) * (size_t)pl.nz;
+  long long nb = (d.npad() + 255) / 256;
+  if (nb > 152LL * 32) nb = 152LL * 32;
+  cudaError_t e = cudaMemsetAsync(pl.a, 0, nphi, st);
+  if (e != cudaSuccess) return e;
+  k_pack_phi_df<<<(unsigned)nb, 256, 0, st>>>(d, phi, pl.a, pl.px); note_launch();
+  e = cudaMemcpyAsync(pl.b, pl.a, nphi, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  const long long nc = d.ncell();
+  long long nb2 = (nc + 255) / 256;
+  if (nb2 > 152LL * 32) nb2 = 152LL * 32;
+  k_pack_sr<<<(unsigned)nb2, 256, 0, st>>>(nc, src, rdiag, pl.sr); note_launch();
+  e = launch_to_df(coef64, pl.coef, 2LL * (pl.nx + pl.ny + pl.nz), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(pl.err, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// Tensor maps for the plan's current tile shape.
+cudaError_t jacobi_df_encode(JacobiDfPlan& pl) {
+  const TileShape sh = kShapes[(pl.shape >= 0 && pl.shape < kNumShapes) ? pl.shape : 0];
+  const uint64_t pitch1 = (uint64_t)pl.px * 8, pitch2 = pitch1 * (uint64_t)(pl.ny + 2);
+  const int ty = sh.tyb * sh.cy;
+  if (!encode_3d(&pl.tm_a, pl.a, pl.nx + 2, pl.ny + 2, pl.nz, pitch1, pitch2, sh.tx + 2, ty + 2) ||
+      !encode_3d(&pl.tm_b, pl.b, pl.nx + 2, pl.ny + 2, pl.nz, pitch1, pitch2, sh.tx + 2, ty + 2) ||
+      !encode_3d(&pl.tm_sr, pl.sr, 2ULL * pl.nx, pl.ny, pl.nz, 16ULL * pl.nx, 16ULL * pl.nx * pl.ny, 2 * sh.tx, ty))
+    return cudaErrorInvalidValue;
+  return cudaSuccess;
+}
+
+void jacobi_df_shape(int shape, int* tx, int* ty) {
+  const TileShape sh = kShapes[(shape >= 0 && shape < kNumShapes) ? shape : 0];
+  *tx = sh.tx;
+  *ty = sh.tyb * sh.cy;
+}
+
+cudaError_t jacobi_df_unpack(const JacobiDfPlan& pl, const float2* cur, double* phi, cudaStream_t st) {
+  const Dims d{pl.nx, pl.ny, pl.nz};
+  Launch L = cells_launch(d);
+  k_unpack_phi_df<<<L.grid, L.block, 0, st>>>(d, cur, phi, pl.px); note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace fpm

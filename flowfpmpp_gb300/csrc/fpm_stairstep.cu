@@ -46,7 +46,7 @@ __global__ void k_axis_coefs(Axes ax, int nx, int ny, int nz, double* coef) {
 cudaError_t launch_axis_coefs(const Axes& ax, int nx, int ny, int nz, double* coef, cudaStream_t st) {
   int n = nx > ny ? nx : ny;
   if (nz > n) n = nz;
-  k_axis_coefs<<<(n + 255) / 256, 256, 0, st>>>(ax, nx, ny, nz, coef);
+  k_axis_coefs<<<(n + 255) / 256, 256, 0, st>>>(ax, nx, ny, nz, coef); note_launch();
   return cudaGetLastError();
 }
 
@@ -111,7 +111,7 @@ cudaError_t launch_build_operator(const Dims& d, const double* rhs, const int32_
                                   double* diag, double* rdiag, SolveScalars* S, cudaStream_t st) {
   Launch L = cells_launch(d);
   k_build_operator<<<L.grid, L.block, 0, st>>>(d, rhs, solid, Bg{bg[0], bg[1], bg[2]}, f, c, ax, for_pcg, src, diag,
-                                               rdiag, S);
+                                               rdiag, S); note_launch();
   return cudaGetLastError();
 }
 
@@ -134,7 +134,7 @@ __global__ void k_init_fields(Dims d, const int32_t* __restrict__ solid, double*
 }
 cudaError_t launch_init_fields(const Dims& d, const int32_t* solid, double* phi, double* next, cudaStream_t st) {
   Launch L = cells_launch(d, 1);
-  k_init_fields<<<L.grid, L.block, 0, st>>>(d, solid, phi, next);
+  k_init_fields<<<L.grid, L.block, 0, st>>>(d, solid, phi, next); note_launch();
   return cudaGetLastError();
 }
 
@@ -157,7 +157,7 @@ __global__ void k_jacobi_f64(Dims d, const double* __restrict__ a, double* __res
 cudaError_t launch_jacobi_f64(const Dims& d, const double* a, double* b, const double* src, const double* rdiag,
                               const Coefs& c, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_jacobi_f64<<<L.grid, L.block, 0, st>>>(d, a, b, src, rdiag, c);
+  k_jacobi_f64<<<L.grid, L.block, 0, st>>>(d, a, b, src, rdiag, c); note_launch();
   return cudaGetLastError();
 }
 
@@ -169,7 +169,7 @@ __global__ void k_copy_interior(Dims d, const double* __restrict__ from, double*
 }
 cudaError_t launch_copy_interior(const Dims& d, const double* from, double* to, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_copy_interior<<<L.grid, L.block, 0, st>>>(d, from, to);
+  k_copy_interior<<<L.grid, L.block, 0, st>>>(d, from, to); note_launch();
   return cudaGetLastError();
 }
 
@@ -205,7 +205,7 @@ __global__ void k_operator_residual(Dims d, const double* __restrict__ phi, cons
 cudaError_t launch_operator_residual(const Dims& d, const double* phi, const double* src, const double* diag,
                                      const Coefs& c, SolveScalars* S, const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_operator_residual<<<L.grid, L.block, 0, st>>>(d, phi, src, diag, c, S, rb);
+  k_operator_residual<<<L.grid, L.block, 0, st>>>(d, phi, src, diag, c, S, rb); note_launch();
   return cudaGetLastError();
 }
 
@@ -267,8 +267,8 @@ cudaError_t launch_true_residual(const Dims& d, const double* phi, const double*
                                  const double* rdiag, double* r, double* p, const Coefs& c, const Axes& ax, int reset,
                                  SolveScalars* S, const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_true_residual_a<<<L.grid, L.block, 0, st>>>(d, phi, src, diag, r, c, ax, S, rb);
-  k_true_residual_b<<<L.grid, L.block, 0, st>>>(d, r, diag, rdiag, p, reset, S, rb);
+  k_true_residual_a<<<L.grid, L.block, 0, st>>>(d, phi, src, diag, r, c, ax, S, rb); note_launch();
+  k_true_residual_b<<<L.grid, L.block, 0, st>>>(d, r, diag, rdiag, p, reset, S, rb); note_launch();
   return cudaGetLastError();
 }
 
@@ -349,9 +349,9 @@ cudaError_t launch_pcg_iteration(const Dims& d, double* phi, double* p, double* 
                                  const double* rdiag, const Coefs& c, const Axes& ax, SolveScalars* S,
                                  const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_pcg_spmv<<<L.grid, L.block, 0, st>>>(d, p, q, diag, c, ax, S, rb);
-  k_pcg_update<<<L.grid, L.block, 0, st>>>(d, phi, p, q, r, rdiag, S, rb);
-  k_pcg_direction<<<L.grid, L.block, 0, st>>>(d, p, r, rdiag, S);
+  k_pcg_spmv<<<L.grid, L.block, 0, st>>>(d, p, q, diag, c, ax, S, rb); note_launch();
+  k_pcg_update<<<L.grid, L.block, 0, st>>>(d, phi, p, q, r, rdiag, S, rb); note_launch();
+  k_pcg_direction<<<L.grid, L.block, 0, st>>>(d, p, r, rdiag, S); note_launch();
   return cudaGetLastError();
 }
 
@@ -382,8 +382,8 @@ __global__ void k_gauge_sub(Dims d, const int32_t* __restrict__ solid, double* _
 cudaError_t launch_gauge(const Dims& d, const int32_t* solid, double* phi, const Axes& ax, SolveScalars* S,
                          const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_gauge_sum<<<L.grid, L.block, 0, st>>>(d, solid, phi, ax, S, rb);
-  k_gauge_sub<<<L.grid, L.block, 0, st>>>(d, solid, phi, S);
+  k_gauge_sum<<<L.grid, L.block, 0, st>>>(d, solid, phi, ax, S, rb); note_launch();
+  k_gauge_sub<<<L.grid, L.block, 0, st>>>(d, solid, phi, S); note_launch();
   return cudaGetLastError();
 }
 
@@ -441,12 +441,12 @@ cudaError_t launch_compat(const Dims& d, const double* rhs, const int32_t* solid
                           const Axes& ax, SolveScalars* S, const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
   Bg b{bg[0], bg[1], bg[2]};
-  k_compat_sums<<<L.grid, L.block, 0, st>>>(d, rhs, solid, b, f, ax, 0, S, rb);
+  k_compat_sums<<<L.grid, L.block, 0, st>>>(d, rhs, solid, b, f, ax, 0, S, rb); note_launch();
   long long nmax = (long long)d.ny * d.nz;
   if ((long long)d.nx * d.nz > nmax) nmax = (long long)d.nx * d.nz;
   if ((long long)d.nx * d.ny > nmax) nmax = (long long)d.nx * d.ny;
-  k_shift_faces<<<(unsigned)((nmax + 255) / 256), 256, 0, st>>>(d, f, S);
-  k_compat_sums<<<L.grid, L.block, 0, st>>>(d, rhs, solid, b, f, ax, 1, S, rb);
+  k_shift_faces<<<(unsigned)((nmax + 255) / 256), 256, 0, st>>>(d, f, S); note_launch();
+  k_compat_sums<<<L.grid, L.block, 0, st>>>(d, rhs, solid, b, f, ax, 1, S, rb); note_launch();
   return cudaGetLastError();
 }
 
@@ -501,7 +501,7 @@ cudaError_t launch_face_residual(const Dims& d, const double* phi, const double*
                                  const double bg[3], const Faces& f, const Axes& ax, SolveScalars* S,
                                  const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
-  k_face_residual<<<L.grid, L.block, 0, st>>>(d, phi, rhs, solid, Bg{bg[0], bg[1], bg[2]}, f, ax, S, rb);
+  k_face_residual<<<L.grid, L.block, 0, st>>>(d, phi, rhs, solid, Bg{bg[0], bg[1], bg[2]}, f, ax, S, rb); note_launch();
   return cudaGetLastError();
 }
 
@@ -552,7 +552,7 @@ cudaError_t launch_terms(const Dims& d, const double* phi, const Flow& fl, const
                          const RedBuf& rb, cudaStream_t st) {
   Launch L = cells_launch(d);
   k_terms<<<L.grid, L.block, 0, st>>>(d, phi, fl, solid, Bg{bg[0], bg[1], bg[2]}, ax, f, bounds[0], bounds[1],
-                                      bounds[2], bounds[3], bounds[4], bounds[5], o, S, rb);
+                                      bounds[2], bounds[3], bounds[4], bounds[5], o, S, rb); note_launch();
   return cudaGetLastError();
 }
 

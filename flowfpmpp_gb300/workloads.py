@@ -1,0 +1,158 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Every generator returns plain numpy arrays in the reference's Fortran layout
+(order='F'), ready for the stair-step API: axes with mirrored halo centres
+(xc(0:nx+1)), a padded int32 solid flag with a zero physical halo, zero
+outer-face data, rhs = 0 and body_grad = e_axis (the FPM influence problem).
+
+Configurations (sizes in cells):
+  c1  64x64x32 on [-4,4]^2 x [-2,2], geometric ratio 1.03 away from the
+      centre planes, sphere r=0.5 at the origin; flow = U=1 + 8 Gaussian
+      z-tubes (core 0.2, circulation N(0,1)), acceleration = 6 Fourier modes.
+  c2  256^3, ratio 1.01, four seeded axis-aligned boxes of 8-40 cells per
+      side, one touching the outer boundary; phi_x right-hand side.
+  c3  384x384x192, ratio 1.02, union of 3 random ellipsoids (semi-axes
+      0.3-1.0, random orientation).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def geometric_axis(n: int, lo: float, hi: float, ratio: float):
+    """n cells on [lo, hi], widths growing by `ratio` per cell away from the
+    centre plane (symmetric).  Returns (faces(0:n), centres(0:n+1) with
+    mirrored halo centres, widths(1:n))."""
+    half = n // 2
+    if n % 2 == 0:
+        side = ratio ** np.arange(half)
+        w = np.concatenate([side[::-1], side])
+    else:
+        side = ratio ** np.arange(1, half + 1)
+        w = np.concatenate([side[::-1], [1.0], side])
+    w = w * (hi - lo) / w.sum()
+    faces = lo + np.concatenate([[0.0], np.cumsum(w)])
+    faces[-1] = hi
+    c = 0.5 * (faces[:-1] + faces[1:])
+    centres = np.concatenate([[c[0] - w[0]], c, [c[-1] + w[-1]]])
+    return faces, centres, w
+
+
+def _empty_faces(nx, ny, nz):
+    z = lambda a, b: np.zeros((a, b), order="F")
+    return [z(ny, nz), z(ny, nz), z(nx, nz), z(nx, nz), z(nx, ny), z(nx, ny)]
+
+
+def _frame(nx, ny, nz, ax, ay, az, solid_interior, axis):
+    solid = np.zeros((nx + 2, ny + 2, nz), dtype=np.int32, order="F")
+    solid[1:nx + 1, 1:ny + 1, :] = solid_interior
+    body = np.zeros(3)
+    body[axis] = 1.0
+    return dict(nx=nx, ny=ny, nz=nz, xf=ax[0], yf=ay[0], zf=az[0], xc=ax[1], yc=ay[1], zc=az[1][1:nz + 1].copy(),
+                dx=ax[2], dy=ay[2], dz=az[2], solid=solid, rhs=np.zeros((nx, ny, nz), order="F"),
+                phi=np.zeros((nx + 2, ny + 2, nz), order="F"), body=body, faces=_empty_faces(nx, ny, nz))
+
+
+def boxes_c2(n=256, seed=2025, ratio=1.01, half=4.0, nboxes=4):
+    """Config 2: n^3 grid, four axis-aligned boxes of 8-40 cells per side at
+    seeded positions, the first one touching the outer boundary (x = -half)."""
+    rng = np.random.default_rng(seed)
+    ax = geometric_axis(n, -half, half, ratio)
+    solid = np.zeros((n, n, n), dtype=np.int32)
+    for b in range(nboxes):
+        size = rng.integers(8, 41, size=3)
+        lo = np.array([rng.integers(0, n - s + 1) for s in size])
+        if b == 0:
+            lo[0] = 0  # touches the west boundary
+        else:
+            lo = np.clip(lo, 1, n - 1 - size)
+        solid[lo[0]:lo[0] + size[0], lo[1]:lo[1] + size[1], lo[2]:lo[2] + size[2]] = 1
+    return _frame(n, n, n, ax, ax, ax, solid, 0)
+
+
+def sphere_c1(nx=64, ny=64, nz=32, ratio=1.03, radius=0.5, axis=0):
+    """Config 1: stretched grid on [-4,4]^2 x [-2,2], sphere at the origin."""
+    ax = geometric_axis(nx, -4.0, 4.0, ratio)
+    ay = geometric_axis(ny, -4.0, 4.0, ratio)
+    az = geometric_axis(nz, -2.0, 2.0, ratio)
+    X = ax[1][1:nx + 1][:, None, None]
+    Y = ay[1][1:ny + 1][None, :, None]
+    Z = az[1][1:nz + 1][None, None, :]
+    solid = ((X ** 2 + Y ** 2 + Z ** 2) < radius ** 2).astype(np.int32)
+    return _frame(nx, ny, nz, ax, ay, az, solid, axis)
+
+
+def _rotation(rng):
+    q = rng.standard_normal(4)
+    q /= np.linalg.norm(q)
+    a, b, c, d = q
+    return np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                     [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                     [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+
+
+def ellipsoids_c3(nx=384, ny=384, nz=192, ratio=1.02, seed=3, count=3, axis=0):
+    """Config 3: union of `count` random ellipsoids (semi-axes 0.3-1.0, random
+    orientation, centres within 1.0 of the origin) on [-4,4]^2 x [-2,2]."""
+    rng = np.random.default_rng(seed)
+    ax = geometric_axis(nx, -4.0, 4.0, ratio)
+    ay = geometric_axis(ny, -4.0, 4.0, ratio)
+    az = geometric_axis(nz, -2.0, 2.0, ratio)
+    X = ax[1][1:nx + 1][:, None, None]
+    Y = ay[1][1:ny + 1][None, :, None]
+    Z = az[1][1:nz + 1][None, None, :]
+    solid = np.zeros((nx, ny, nz), dtype=bool)
+    for _ in range(count):
+        semi = rng.uniform(0.3, 1.0, 3)
+        cen = rng.uniform(-1.0, 1.0, 3) * np.array([1.0, 1.0, 0.5])
+        R = _rotation(rng)
+        dX, dY, dZ = X - cen[0], Y - cen[1], Z - cen[2]
+        q = 0.0
+        for r in range(3):
+            comp = R[0, r] * dX + R[1, r] * dY + R[2, r] * dZ
+            q = q + (comp / semi[r]) ** 2
+        solid |= q < 1.0
+    return _frame(nx, ny, nz, ax, ay, az, solid.astype(np.int32), axis)
+
+
+def flow_c1(frame, seed=11, ntubes=8, core=0.2, nmodes=6):
+    """Velocity U=1 plus `ntubes` z-aligned Gaussian (Lamb-Oseen) vortex tubes
+    with centres uniform in the fluid and circulation N(0,1), analytic
+    vorticity; acceleration = sum of `nmodes` Fourier modes with wavenumbers
+    1-3 and amplitudes N(0, 0.1)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = frame["nx"], frame["ny"], frame["nz"]
+    X = frame["xc"][1:nx + 1][:, None, None] * np.ones((nx, ny, nz))
+    Y = frame["yc"][1:ny + 1][None, :, None] * np.ones((nx, ny, nz))
+    Z = frame["zc"][None, None, :] * np.ones((nx, ny, nz))
+    fluid = frame["solid"][1:nx + 1, 1:ny + 1, :] == 0
+    u = np.ones((nx, ny, nz))
+    v = np.zeros((nx, ny, nz))
+    w = np.zeros((nx, ny, nz))
+    oz = np.zeros((nx, ny, nz))
+    fx, fy = X[fluid], Y[fluid]
+    for _ in range(ntubes):
+        m = rng.integers(0, fx.size)
+        x0, y0 = fx[m], fy[m]
+        gam = rng.standard_normal()
+        r2 = (X - x0) ** 2 + (Y - y0) ** 2
+        r2s = np.where(r2 > 0, r2, 1.0)
+        vt = gam / (2 * math.pi) * (1 - np.exp(-r2 / core ** 2)) / r2s
+        vt = np.where(r2 > 0, vt, 0.0)
+        u += -vt * (Y - y0)
+        v += vt * (X - x0)
+        oz += gam / (math.pi * core ** 2) * np.exp(-r2 / core ** 2)
+    ox = np.zeros((nx, ny, nz))
+    oy = np.zeros((nx, ny, nz))
+    acc = [np.zeros((nx, ny, nz)) for _ in range(3)]
+    for _ in range(nmodes):
+        k = rng.integers(1, 4, size=3) * rng.choice([-1, 1], size=3)
+        ph = rng.uniform(0, 2 * math.pi)
+        amp = rng.normal(0, 0.1, size=3)
+        arg = np.sin(k[0] * X + k[1] * Y + k[2] * Z + ph)
+        for c in range(3):
+            acc[c] += amp[c] * arg
+    F = lambda a: np.asfortranarray(a)
+    return dict(u=F(u), v=F(v), w=F(w), ox=F(ox), oy=F(oy), oz=F(oz), ax=F(acc[0]), ay=F(acc[1]), az=F(acc[2]))

@@ -50,6 +50,7 @@ extern "C" {
 #define FPM_E_CUDA 6          /* CUDA runtime error (message has the CUDA error string) */
 #define FPM_E_NO_DEVICE 7     /* no CUDA device visible */
 #define FPM_E_LIMIT 8         /* a size exceeds a documented limit */
+#define FPM_E_TIMEOUT 9       /* a bounded device-side wait gave up (no GPU hang: the kernel returned) */
 
 /* ---- solver methods (the reference's method='pcg' | 'jacobi') ---------- */
 #define FPM_METHOD_PCG 0        /* diagonal PCG, FP64 throughout (reference 'pcg') */
@@ -62,6 +63,21 @@ extern "C" {
 const char* fpm_last_error(void);
 /* Library version as 10000*major + 100*minor + patch. */
 int fpm_version(void);
+/* CUDA-event timing of the hot loops on the stream they run on (off by
+ * default).  fpm_timing_read resolves the recorded events and returns, for
+ * kernel `which` (FPM_TIMER_*), the number of launches and their total
+ * device time; reset != 0 clears that counter afterwards. */
+#define FPM_TIMER_JACOBI_DF 0   /* double-float Jacobi sweep (TMA-streamed) */
+#define FPM_TIMER_JACOBI_F64 1  /* FP64 Jacobi sweep */
+#define FPM_TIMER_PCG_ITER 2    /* one FP64 PCG iteration (three kernels) */
+#define FPM_TIMER_COUNT 4
+int fpm_timing_enable(int on);
+/* Number of kernels this library has launched in this process. */
+long long fpm_kernel_launches(void);
+int fpm_timing_read(int which, long long* launches, double* total_ms, int reset);
+/* Tile shape (x, y) and planes per CTA the double-float Jacobi autotuner chose
+ * for an nx*ny*nz grid (after a double-float run at that size). */
+int fpm_jacobi_df_config(int nx, int ny, int nz, int* tile_x, int* tile_y, int* kchunk);
 /* Pinned (page-locked) host memory for fast transfers; NULL on failure. */
 void* fpm_host_alloc(size_t bytes);
 void fpm_host_free(void* p);
@@ -131,6 +147,61 @@ int fpm_compute_stairstep_fpm_terms_3d_dev(const double* phi, const double* u, c
                                            const double* bounds, double* gx, double* gy, double* gz, double* vortex,
                                            double* advection, double* totals, int nx, int ny, int nz, void* stream);
 
+
+/* ---- fpm_laplace_3d (no body; src/fpm_laplace_3d.f90) -------------------
+ * enforce_neumann_compatibility_3d (:9-53): uniform spacing dx, dy, dz. */
+int fpm_enforce_neumann_compatibility_3d(const double* rhs, double* xlo, double* xhi, double* ylo, double* yhi,
+                                         double* zlo, double* zhi, int nx, int ny, int nz, double dx, double dy,
+                                         double dz, double* correction, double* imbalance);
+/* solve_neumann_poisson_3d (:55-107): undamped Jacobi with clamped neighbours,
+ * mean removal and ghost fill; phi is (0:nx+1, 0:ny+1, 0:nz+1). */
+int fpm_solve_neumann_poisson_3d(double* phi, const double* rhs, const double* xlo, const double* xhi,
+                                 const double* ylo, const double* yhi, const double* zlo, const double* zhi, int nx,
+                                 int ny, int nz, double dx, double dy, double dz, double tolerance, int max_iterations,
+                                 int check_interval, int* iterations, double* final_residual);
+/* enforce_neumann_compatibility_nonuniform_3d (:150-217). */
+int fpm_enforce_neumann_compatibility_nonuniform_3d(const double* rhs, double* xlo, double* xhi, double* ylo,
+                                                    double* yhi, double* zlo, double* zhi, const double* dx,
+                                                    const double* dy, const double* dz, int nx, int ny, int nz,
+                                                    double* correction, double* imbalance);
+/* solve_neumann_poisson_nonuniform_3d (:219-293): weighted 0.2/0.8 Jacobi,
+ * volume-weighted gauge; phi is (nx, ny, nz), xc(nx), yc(ny), zc(nz). */
+int fpm_solve_neumann_poisson_nonuniform_3d(double* phi, const double* rhs, const double* xlo, const double* xhi,
+                                            const double* ylo, const double* yhi, const double* zlo,
+                                            const double* zhi, const double* xc, const double* yc, const double* zc,
+                                            const double* dx, const double* dy, const double* dz, int nx, int ny,
+                                            int nz, double tolerance, int max_iterations, int check_interval,
+                                            int* iterations, double* final_residual);
+
+/* ---- fpm_terms_3d (no body; src/fpm_terms_3d.f90) -----------------------
+ * compute_fpm_terms_uniform_3d (:8-37): central differences on phi
+ * (0:nx+1, 0:ny+1, 0:nz+1); fluid is int32 (nx,ny,nz), 1 fluid / 0 masked. */
+int fpm_compute_fpm_terms_uniform_3d(const double* phi, const double* u, const double* v, const double* w,
+                                     const double* ox, const double* oy, const double* oz, const double* ax,
+                                     const double* ay, const double* az, const int32_t* fluid, double* gx, double* gy,
+                                     double* gz, double* vortex, double* advection, double* totals, int nx, int ny,
+                                     int nz, double dx, double dy, double dz);
+/* compute_fpm_terms_nonuniform_3d (:39-88): face-gradient averages with the
+ * outer-face data, integrals over cells strictly inside bounds(6);
+ * phi (nx,ny,nz), xc(nx), yc(ny), zc(nz).  Needs >= 2 cells per direction. */
+int fpm_compute_fpm_terms_nonuniform_3d(const double* phi, const double* u, const double* v, const double* w,
+                                        const double* ox, const double* oy, const double* oz, const double* ax,
+                                        const double* ay, const double* az, const int32_t* fluid, const double* xc,
+                                        const double* yc, const double* zc, const double* dx, const double* dy,
+                                        const double* dz, const double* xlo, const double* xhi, const double* ylo,
+                                        const double* yhi, const double* zlo, const double* zhi,
+                                        const double* bounds, double* gx, double* gy, double* gz, double* vortex,
+                                        double* advection, double* totals, int nx, int ny, int nz);
+
+/* ---- fpm_partition_2d (src/fpm_partition_2d.f90:35-154) -----------------
+ * fpm_partition_terms_2d: terms[4] = [F_KINE, F_VIF, F_VIS, F_BOUND],
+ * vif_density and omega (nx,ny).  phi, u, v (nx,ny); g[2]; solid (nx,ny)
+ * uint8, nonzero = solid (the reference's logical); xf(0:nx), yf(0:ny);
+ * kin[6]; ring(2nx+2ny, 2, 2); slip_body 0/1. */
+int fpm_partition_terms_2d(const double* phi, const double* g, const double* u, const double* v,
+                           const uint8_t* solid, const double* xf, const double* yf, const double* kin,
+                           const double* ring, double dt, double nu, int nx, int ny, double* terms,
+                           double* vif_density, double* omega, int slip_body);
 
 /* ---- operator-level entry points (device arrays) ------------------------
  * The private building blocks of solve_stairstep_poisson_3d, exposed so a
