@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["jacobi256", "pcg_c1", "pcg_c3"], default="jacobi256",
+                    help="jacobi256: the headline bandwidth benchmark; pcg_c1 / pcg_c3: three-potential PCG "
+                         "time to 1e-10 (plain FP64 vs mixed precision)")
     return ap.parse_args()
 
 
@@ -191,6 +194,82 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- PCG time to solution
+def run_pcg(args):
+    """Three influence potentials (phi_x, phi_y, phi_z) to a 1e-10 max-norm
+    residual: plain FP64 PCG (one after the other, the reference's method) and
+    FP32 PCG in FP64 refinement batched over the three right-hand sides."""
+    import torch
+    from flowfpmpp_gb300 import build as fbuild
+    fbuild.build()
+    import flowfpmpp_gb300
+    from flowfpmpp_gb300 import stairstep as ss
+    from flowfpmpp_gb300 import workloads
+    lib = flowfpmpp_gb300.lib()
+    if args.workload == "pcg_c1":
+        f = workloads.sphere_c1()
+        name = "C1 64x64x32 sphere, ratio 1.03"
+    else:
+        f = workloads.ellipsoids_c3()
+        name = "C3 384x384x192, 3 ellipsoids, ratio 1.02"
+    nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    faces_dev, bgs, rhss = [], [], []
+    for axis in range(3):
+        body = np.zeros(3)
+        body[axis] = 1.0
+        faces = [x.copy(order="F") for x in f["faces"]]
+        ss.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], body, *faces, f["dx"], f["dy"], f["dz"])
+        faces_dev += [dev(x) for x in faces]
+        bgs.append(body)
+        rhss.append(dev(f["rhs"]))
+    phis = [dev(f["phi"]) for _ in range(3)]
+    dsolid = dev(f["solid"])
+    dax = [dev(f[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    VP = ctypes.c_void_p
+    bg = np.ascontiguousarray(np.concatenate(bgs))
+    stream = torch.cuda.current_stream()
+
+    def solve(method):
+        for t in phis:
+            t.zero_()
+        sweeps = (ctypes.c_int * 3)()
+        res = (ctypes.c_double * 3)()
+        rc = lib.fpm_solve_stairstep_multi_dev(
+            3, (VP * 3)(*[t.data_ptr() for t in phis]), (VP * 3)(*[t.data_ptr() for t in rhss]),
+            VP(dsolid.data_ptr()), bg.ctypes.data_as(VP), (VP * 18)(*[t.data_ptr() for t in faces_dev]),
+            *[VP(t.data_ptr()) for t in dax], nx, ny, nz, ctypes.c_double(1e-10), 2000000, 50, method, sweeps, res,
+            VP(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+        return list(sweeps), list(res)
+
+    out = {}
+    for method, label in ((0, "fp64"), (3, "mixed")):
+        for _ in range(args.warmup):
+            solve(method)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            sw, res = solve(method)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[label] = {"seconds": e0.elapsed_time(e1) / args.steps / 1e3, "iterations": sw, "residual": res,
+                      "phi": [t.cpu().numpy().copy() for t in phis]}
+    err = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+              for a, b in zip(out["mixed"]["phi"], out["fp64"]["phi"]))
+    line = {"metric": "PCG solve time to 1e-10 max-norm residual, three potentials (mixed vs plain FP64)",
+            "value": out["mixed"]["seconds"], "unit": "s", "higher_is_better": False, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded)",
+            "config": {"workload": name, "grid": [nx, ny, nz], "rhs": 3, "tolerance": 1e-10, "check_interval": 50},
+            "fp64": {k: v for k, v in out["fp64"].items() if k != "phi"},
+            "mixed": {k: v for k, v in out["mixed"].items() if k != "phi"},
+            "speedup_vs_fp64": out["fp64"]["seconds"] / out["mixed"]["seconds"],
+            "mixed_vs_fp64_rel_linf": err}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
 def main():
     args = parse()
@@ -204,6 +283,10 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if args.workload != "jacobi256":
+        if rank == 0:
+            run_pcg(args)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

@@ -145,7 +145,7 @@ struct TimedRun {
       std::lock_guard<std::mutex> g(g_timer.mu);
       on = g_timer.on;
     }
-    if (on && n > 0) {
+    if (on) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
       cudaEventRecord(a, st);
@@ -153,6 +153,11 @@ struct TimedRun {
   }
   ~TimedRun() {
     if (!a) return;
+    if (n <= 0) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return;
+    }
     cudaEventRecord(b, st);
     std::lock_guard<std::mutex> g(g_timer.mu);
     g_timer.pending.push_back({id, n, a, b});
@@ -390,40 +395,176 @@ static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src,
   *sweeps = sw;
 }
 
-// solve_stairstep_poisson_3d (src/fpm_stairstep_mpi_3d.f90:106-330), device arrays.
-static void solve_dev(const SolveArgs& a, int* sweeps, double* residual, cudaStream_t st) {
-  if (a.method != FPM_METHOD_PCG && a.method != FPM_METHOD_JACOBI && a.method != FPM_METHOD_JACOBI_DF)
-    throw Error{FPM_E_METHOD, "stair-step method must be pcg or jacobi"};
-  check_dims(a.nx, a.ny, a.nz);
+// Mixed-precision PCG for 1..4 right-hand sides sharing the operator:
+// outer FP64 true residual and max-norm test, inner FP32 PCG batched over the
+// right-hand sides (see fpm_pcg_mixed.cu).  Every inner solve reduces the
+// preconditioned residual norm by kInnerDrop; the outer loop stops when every
+// max-norm residual is <= tol, when max_sweeps inner iterations have run, or
+// after three outer steps in a row without halving any residual.
+constexpr double kInnerDrop = 1e-4;
+constexpr int kInnerCap = 20000;
+
+static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
+                        const double* rdiag, const double* coef64, const Axes& ax, const Coefs& c, double tol,
+                        int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st) {
+  const long long nc = d.ncell(), np = d.npad(), ncoef = 2LL * (d.nx + d.ny + d.nz);
+  MixedVecs v;
+  std::memset(&v, 0, sizeof(v));
+  v.nrhs = nrhs;
+  float* diag32 = A.get<float>(nc);
+  float* rdiag32 = A.get<float>(nc);
+  float* coef32 = A.get<float>(ncoef);
+  float* dx32 = A.get<float>(d.nx);
+  float* dy32 = A.get<float>(d.ny);
+  float* dz32 = A.get<float>(d.nz);
+  CUDA_TRY(launch_mx_convert(diag, diag32, nc, st));
+  CUDA_TRY(launch_mx_convert(rdiag, rdiag32, nc, st));
+  CUDA_TRY(launch_mx_convert(coef64, coef32, ncoef, st));
+  CUDA_TRY(launch_mx_convert(ax.dx, dx32, d.nx, st));
+  CUDA_TRY(launch_mx_convert(ax.dy, dy32, d.ny, st));
+  CUDA_TRY(launch_mx_convert(ax.dz, dz32, d.nz, st));
+  v.diag = diag32;
+  v.rdiag = rdiag32;
+  v.coef = coef32;
+  v.dx = dx32;
+  v.dy = dy32;
+  v.dz = dz32;
+  DPtr4 r64{}, phis{};
+  SolveScalars* S64[kMaxRhs] = {};
+  for (int m = 0; m < nrhs; m++) {
+    v.p[m] = A.get<float>(np);
+    CUDA_TRY(cudaMemsetAsync(v.p[m], 0, np * sizeof(float), st));
+    v.q[m] = A.get<float>(nc);
+    v.r[m] = A.get<float>(nc);
+    v.e[m] = A.get<float>(nc);
+    r64.p[m] = A.get<double>(nc);
+    phis.p[m] = phi[m];
+    S64[m] = A.get<SolveScalars>(1);
+    CUDA_TRY(cudaMemsetAsync(S64[m], 0, sizeof(SolveScalars), st));
+  }
+  MixedScalars* MS = A.get<MixedScalars>(1);
+  {
+    MixedScalars h;
+    std::memset(&h, 0, sizeof(h));
+    for (int m = 0; m < kMaxRhs; m++) h.tol2[m] = kInnerDrop * kInnerDrop;
+    CUDA_TRY(cudaMemcpyAsync(MS, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  }
+  auto true_res = [&](int m) {
+    CUDA_TRY(launch_true_residual(d, phi[m], src[m], diag, rdiag, r64.p[m], nullptr, c, ax, 0, S64[m], cm.rb, st));
+    return read_scalars(S64[m], st).res;
+  };
+  double res[kMaxRhs];
+  for (int m = 0; m < nrhs; m++) res[m] = true_res(m);
+  MixedScalars* hms = nullptr;
+  CUDA_TRY(cudaMallocHost(&hms, sizeof(MixedScalars)));
+  struct HostFree {
+    void* p;
+    ~HostFree() { cudaFreeHost(p); }
+  } hf{hms};
+  const int chunk_len = ci < 1 ? 1 : ci;
+  int total = 0, stall = 0;
+  for (int outer = 0; outer < 100; outer++) {
+    MixedScale sc;
+    std::memset(&sc, 0, sizeof(sc));
+    bool any = false;
+    for (int m = 0; m < nrhs; m++) {
+      sc.in_set[m] = res[m] > tol && res[m] == res[m];
+      sc.scale[m] = res[m] > 0 ? 1.0 / res[m] : 1.0;
+      any = any || sc.in_set[m];
+    }
+    if (!any || total >= max_sweeps) break;
+    CUDA_TRY(launch_mx_start(d, v, r64, sc, MS, cm.rb, st));
+    int inner = 0;
+    {
+      TimedRun t(FPM_TIMER_PCG_MIXED_ITER, 0, st);
+      while (total + inner < max_sweeps && inner < kInnerCap) {
+        int chunk = chunk_len;
+        if (chunk > max_sweeps - total - inner) chunk = max_sweeps - total - inner;
+        for (int n = 0; n < chunk; n++) CUDA_TRY(launch_mx_iteration(d, v, MS, cm.rb, st));
+        CUDA_TRY(cudaMemcpyAsync(hms, MS, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        inner = hms->iters;
+        bool act = false;
+        for (int m = 0; m < nrhs; m++) act = act || hms->active[m];
+        if (!act) break;
+      }
+      t.n = inner;
+    }
+    total += inner;
+    CUDA_TRY(launch_mx_apply(d, v, phis, sc, st));
+    bool improved = false;
+    for (int m = 0; m < nrhs; m++) {
+      if (!sc.in_set[m]) continue;
+      const double r = true_res(m);
+      improved = improved || r < 0.5 * res[m];
+      res[m] = r;
+    }
+    stall = improved ? 0 : stall + 1;
+    if (stall >= 3) break;
+  }
+  for (int m = 0; m < nrhs; m++) sweeps_out[m] = total;
+}
+
+// solve_stairstep_poisson_3d (src/fpm_stairstep_mpi_3d.f90:106-330), device
+// arrays, for nrhs right-hand sides that share solid and axes.  FP64 methods
+// solve them one after the other; FPM_METHOD_PCG_MIXED solves them together.
+static bool valid_method(int m) {
+  return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED;
+}
+
+static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double* residual, cudaStream_t st) {
+  const SolveArgs& a0 = args[0];
+  if (!valid_method(a0.method)) throw Error{FPM_E_METHOD, "stair-step method must be pcg or jacobi"};
+  if (nrhs < 1 || nrhs > kMaxRhs) throw Error{FPM_E_LIMIT, "between 1 and 4 right-hand sides per call"};
+  check_dims(a0.nx, a0.ny, a0.nz);
   require_device();
-  const Dims d{a.nx, a.ny, a.nz};
+  const Dims d{a0.nx, a0.ny, a0.nz};
   Scratch A(st);
   Common cm = make_common(A, d, st);
   Trace t0("stair-step setup");
-  double* coef = A.get<double>(2 * (size_t)(a.nx + a.ny + a.nz));
-  CUDA_TRY(launch_axis_coefs(a.ax, a.nx, a.ny, a.nz, coef, st));
-  Coefs c{coef, coef + a.nx, coef + 2 * a.nx, coef + 2 * a.nx + a.ny, coef + 2 * a.nx + 2 * a.ny,
-          coef + 2 * a.nx + 2 * a.ny + a.nz};
+  double* coef = A.get<double>(2 * (size_t)(a0.nx + a0.ny + a0.nz));
+  CUDA_TRY(launch_axis_coefs(a0.ax, a0.nx, a0.ny, a0.nz, coef, st));
+  Coefs c{coef, coef + a0.nx, coef + 2 * a0.nx, coef + 2 * a0.nx + a0.ny, coef + 2 * a0.nx + 2 * a0.ny,
+          coef + 2 * a0.nx + 2 * a0.ny + a0.nz};
   double* next = A.get<double>(d.npad());
-  double* src = A.get<double>(d.ncell());
   double* diag = A.get<double>(d.ncell());
   double* rdiag = A.get<double>(d.ncell());
-  const bool use_pcg = a.method == FPM_METHOD_PCG;
-  CUDA_TRY(launch_build_operator(d, a.rhs, a.solid, a.bg, a.f, c, a.ax, use_pcg, src, diag, rdiag, cm.S, st));
+  const bool for_pcg = a0.method == FPM_METHOD_PCG || a0.method == FPM_METHOD_PCG_MIXED;
+  double* src[kMaxRhs] = {};
+  for (int m = 0; m < nrhs; m++) {
+    src[m] = A.get<double>(d.ncell());
+    CUDA_TRY(launch_build_operator(d, args[m].rhs, args[m].solid, args[m].bg, args[m].f, c, args[m].ax, for_pcg,
+                                   src[m], diag, rdiag, cm.S, st));
+  }
   if (read_scalars(cm.S, st).isolated > 0) throw Error{FPM_E_ISOLATED, "stair-step fluid cell has no fluid neighbour"};
-  CUDA_TRY(launch_init_fields(d, a.solid, a.phi, next, st));
-  int sw = 0;
+  for (int m = 0; m < nrhs; m++) CUDA_TRY(launch_init_fields(d, args[m].solid, args[m].phi, next, st));
   {
     Trace t1("stair-step iterations");
-    if (use_pcg) pcg_loop(a, d, next, src, diag, rdiag, c, A, cm, &sw, st);
-    else if (a.method == FPM_METHOD_JACOBI) jacobi_loop_f64(a, d, next, src, diag, rdiag, c, cm, &sw, st);
-    else jacobi_loop_df(a, d, src, diag, rdiag, coef, c, A, cm, &sw, st);
+    if (a0.method == FPM_METHOD_PCG_MIXED) {
+      double* phis[kMaxRhs] = {};
+      for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
+      mixed_solve(d, nrhs, phis, src, diag, rdiag, coef, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps, st);
+    } else {
+      for (int m = 0; m < nrhs; m++) {
+        const SolveArgs& a = args[m];
+        if (m > 0) CUDA_TRY(launch_init_fields(d, a.solid, a.phi, next, st));
+        CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
+        if (a.method == FPM_METHOD_PCG) pcg_loop(a, d, next, src[m], diag, rdiag, c, A, cm, &sweeps[m], st);
+        else if (a.method == FPM_METHOD_JACOBI) jacobi_loop_f64(a, d, next, src[m], diag, rdiag, c, cm, &sweeps[m], st);
+        else jacobi_loop_df(a, d, src[m], diag, rdiag, coef, c, A, cm, &sweeps[m], st);
+      }
+    }
   }
   Trace t2("stair-step gauge");
-  CUDA_TRY(launch_gauge(d, a.solid, a.phi, a.ax, cm.S, cm.rb, st));
-  CUDA_TRY(launch_operator_residual(d, a.phi, src, diag, c, cm.S, cm.rb, st));
-  *residual = read_scalars(cm.S, st).res;
-  *sweeps = sw;
+  for (int m = 0; m < nrhs; m++) {
+    CUDA_TRY(launch_gauge(d, args[m].solid, args[m].phi, args[m].ax, cm.S, cm.rb, st));
+    CUDA_TRY(launch_operator_residual(d, args[m].phi, src[m], diag, c, cm.S, cm.rb, st));
+    residual[m] = read_scalars(cm.S, st).res;
+  }
+}
+
+static void solve_dev(const SolveArgs& a, int* sweeps, double* residual, cudaStream_t st) {
+  solve_multi_dev(1, &a, sweeps, residual, st);
 }
 
 static size_t nface_x(int ny, int nz) { return (size_t)ny * nz; }
@@ -621,8 +762,7 @@ int fpm_solve_stairstep_poisson_3d(double* phi, const double* rhs, const int32_t
     if (!phi || !rhs || !solid || !body_grad || !xlo || !xhi || !ylo || !yhi || !zlo || !zhi || !xc || !yc || !zc ||
         !dx || !dy || !dz || !sweeps || !residual)
       throw Error{FPM_E_ARG, "null argument"};
-    if (method != FPM_METHOD_PCG && method != FPM_METHOD_JACOBI && method != FPM_METHOD_JACOBI_DF)
-      throw Error{FPM_E_METHOD, "stair-step method must be pcg or jacobi"};
+    if (!valid_method(method)) throw Error{FPM_E_METHOD, "stair-step method must be pcg or jacobi"};
     check_dims(nx, ny, nz);
     require_device();
     cudaStream_t st = 0;
@@ -648,6 +788,44 @@ int fpm_solve_stairstep_poisson_3d(double* phi, const double* rhs, const int32_t
     if (rc != FPM_OK) throw Error{rc, g_last_error};
     download(phi, dphi, d.npad() * sizeof(double), st);
     CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+int fpm_solve_stairstep_multi_dev(int nrhs, double* const* phi, const double* const* rhs, const int32_t* solid,
+                                  const double* body_grads, const double* const* faces, const double* xc,
+                                  const double* yc, const double* zc, const double* dx, const double* dy,
+                                  const double* dz, int nx, int ny, int nz, double tolerance, int max_sweeps,
+                                  int check_interval, int method, int* sweeps, double* residual, void* stream) {
+  return guarded([&] {
+    if (!phi || !rhs || !solid || !body_grads || !faces || !xc || !yc || !zc || !dx || !dy || !dz || !sweeps ||
+        !residual)
+      throw Error{FPM_E_ARG, "null argument"};
+    if (nrhs < 1 || nrhs > kMaxRhs) throw Error{FPM_E_LIMIT, "between 1 and 4 right-hand sides per call"};
+    SolveArgs args[kMaxRhs];
+    for (int m = 0; m < nrhs; m++) {
+      SolveArgs& a = args[m];
+      if (!phi[m] || !rhs[m]) throw Error{FPM_E_ARG, "null phi or rhs"};
+      for (int f = 0; f < 6; f++)
+        if (!faces[6 * m + f]) throw Error{FPM_E_ARG, "null face array"};
+      a.phi = phi[m];
+      a.rhs = rhs[m];
+      a.solid = solid;
+      for (int q = 0; q < 3; q++) a.bg[q] = body_grads[3 * m + q];
+      a.f = Faces{const_cast<double*>(faces[6 * m]), const_cast<double*>(faces[6 * m + 1]),
+                  const_cast<double*>(faces[6 * m + 2]), const_cast<double*>(faces[6 * m + 3]),
+                  const_cast<double*>(faces[6 * m + 4]), const_cast<double*>(faces[6 * m + 5])};
+      a.ax = Axes{xc, yc, zc, dx, dy, dz};
+      a.nx = nx;
+      a.ny = ny;
+      a.nz = nz;
+      a.tol = tolerance;
+      a.max_sweeps = max_sweeps;
+      a.ci = check_interval;
+      a.method = method;
+      sweeps[m] = 0;
+      residual[m] = HUGE_VAL;
+    }
+    solve_multi_dev(nrhs, args, sweeps, residual, (cudaStream_t)stream);
   });
 }
 
@@ -1120,6 +1298,222 @@ int fpm_partition_terms_2d(const double* phi, const double* g, const double* u, 
     download(vif_density, dvif, n2 * sizeof(double), st);
     download(omega, domega, n2 * sizeof(double), st);
     CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
+// ---------------------------------------------------------------- batched 2-D frames
+// examples/flapping_foil_fpm.f90:61-81 for every frame of a batch at once:
+// phi_x, phi_y (nz = 2, dz = 0.5, zero outer data, compatibility, mixed PCG
+// to the tolerance, gauge), then fpm_partition_terms_2d for both directions.
+int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const double* const* xf,
+                            const double* const* yf, const double* const* u, const double* const* v,
+                            const uint8_t* const* solid, const double* const* ring, const double* kin,
+                            const double* dt, double nu, double tolerance, int max_sweeps, int check_interval,
+                            double* terms, int* sweeps, double* residual, double* const* phi_out) {
+  return guarded([&] {
+    if (nframes < 1) throw Error{FPM_E_SIZE, "no frames"};
+    if (!nx || !ny || !xf || !yf || !u || !v || !solid || !ring || !kin || !dt || !terms || !sweeps || !residual)
+      throw Error{FPM_E_ARG, "null argument"};
+    require_device();
+    cudaStream_t st = 0;
+    std::vector<Frame2> fr(nframes);
+    std::vector<int> tile_frame;
+    long long npx = 0, npy = 0, npad = 0, nint = 0, n2 = 0, nring = 0;
+    for (int f = 0; f < nframes; f++) {
+      if (nx[f] < 1 || ny[f] < 1) throw Error{FPM_E_SIZE, "frame with no cells"};
+      if (!xf[f] || !yf[f] || !u[f] || !v[f] || !solid[f] || !ring[f]) throw Error{FPM_E_ARG, "null frame array"};
+      Frame2& F = fr[f];
+      F.nx = nx[f];
+      F.ny = ny[f];
+      F.tiles_x = (F.nx + 31) / 32;
+      F.tile0 = (int)tile_frame.size();
+      F.ntiles = F.tiles_x * ((F.ny + 7) / 8);
+      for (int t = 0; t < F.ntiles; t++) tile_frame.push_back(f);
+      F.ox = (int)npx;
+      F.oy = (int)npy;
+      F.opad = npad;
+      F.oint = nint;
+      F.o2 = n2;
+      F.oring = nring;
+      npx += F.nx + 2;
+      npy += F.ny + 2;
+      npad += (long long)(F.nx + 2) * (F.ny + 2) * 2;
+      nint += (long long)F.nx * F.ny * 2;
+      n2 += (long long)F.nx * F.ny;
+      nring += 4LL * (2LL * F.nx + 2LL * F.ny);
+    }
+    const int ntiles = (int)tile_frame.size();
+    // Host staging of the pools (axes as in examples/flapping_foil_fpm.f90:211-213).
+    std::vector<double> hxc(npx), hdx(npx), hxf(npx), hyc(npy), hdy(npy), hyf(npy);
+    std::vector<int32_t> hs3(npad, 0);
+    std::vector<uint8_t> hs2(n2);
+    std::vector<double> hu(n2), hv(n2), hring(nring);
+    for (int f = 0; f < nframes; f++) {
+      const Frame2& F = fr[f];
+      for (int i = 0; i <= F.nx; i++) hxf[F.ox + i] = xf[f][i];
+      for (int i = 1; i <= F.nx; i++) {
+        hdx[F.ox + i - 1] = xf[f][i] - xf[f][i - 1];
+        hxc[F.ox + i] = 0.5 * (xf[f][i - 1] + xf[f][i]);
+      }
+      hxc[F.ox] = hxc[F.ox + 1] - hdx[F.ox];
+      hxc[F.ox + F.nx + 1] = hxc[F.ox + F.nx] + hdx[F.ox + F.nx - 1];
+      for (int j = 0; j <= F.ny; j++) hyf[F.oy + j] = yf[f][j];
+      for (int j = 1; j <= F.ny; j++) {
+        hdy[F.oy + j - 1] = yf[f][j] - yf[f][j - 1];
+        hyc[F.oy + j] = 0.5 * (yf[f][j - 1] + yf[f][j]);
+      }
+      hyc[F.oy] = hyc[F.oy + 1] - hdy[F.oy];
+      hyc[F.oy + F.ny + 1] = hyc[F.oy + F.ny] + hdy[F.oy + F.ny - 1];
+      const long long cells = (long long)F.nx * F.ny;
+      for (long long m = 0; m < cells; m++) {
+        const int i = (int)(m % F.nx) + 1, j = (int)(m / F.nx) + 1;
+        const uint8_t sv = solid[f][m] ? 1 : 0;
+        hs2[F.o2 + m] = sv;
+        for (int k = 1; k <= 2; k++) hs3[F.opad + i + (long long)(F.nx + 2) * (j + (long long)(F.ny + 2) * (k - 1))] = sv;
+      }
+      std::memcpy(&hu[F.o2], u[f], cells * sizeof(double));
+      std::memcpy(&hv[F.o2], v[f], cells * sizeof(double));
+      std::memcpy(&hring[F.oring], ring[f], 4 * (2LL * F.nx + 2LL * F.ny) * sizeof(double));
+    }
+    Scratch A(st);
+    Frame2* dfr = A.upload(fr.data(), fr.size());
+    int* dtf = A.upload(tile_frame.data(), tile_frame.size());
+    Batch2 b;
+    std::memset(&b, 0, sizeof(b));
+    b.xc = A.upload(hxc.data(), hxc.size());
+    b.dx = A.upload(hdx.data(), hdx.size());
+    b.xf = A.upload(hxf.data(), hxf.size());
+    b.yc = A.upload(hyc.data(), hyc.size());
+    b.dy = A.upload(hdy.data(), hdy.size());
+    b.yf = A.upload(hyf.data(), hyf.size());
+    b.solid3 = A.upload(hs3.data(), hs3.size());
+    b.solid2 = A.upload(hs2.data(), hs2.size());
+    b.u = A.upload(hu.data(), hu.size());
+    b.v = A.upload(hv.data(), hv.size());
+    b.ring = A.upload(hring.data(), hring.size());
+    b.kin = A.upload(kin, 6 * (size_t)nframes);
+    b.dt = A.upload(dt, (size_t)nframes);
+    b.nu = nu;
+    for (int r = 0; r < 2; r++) {
+      b.src[r] = A.get<double>(nint);
+      b.phi[r] = A.get<double>(npad);
+      CUDA_TRY(cudaMemsetAsync(b.phi[r], 0, npad * sizeof(double), st));
+      b.r64[r] = A.get<double>(nint);
+      b.r32[r] = A.get<float>(nint);
+      b.p32[r] = A.get<float>(npad);
+      CUDA_TRY(cudaMemsetAsync(b.p32[r], 0, npad * sizeof(float), st));
+      b.q32[r] = A.get<float>(nint);
+      b.e32[r] = A.get<float>(nint);
+      b.gpx[r] = A.get<double>(n2);
+      b.gpy[r] = A.get<double>(n2);
+      b.vif[r] = A.get<double>(n2);
+    }
+    b.diag = A.get<double>(nint);
+    b.rdiag = A.get<double>(nint);
+    b.diag32 = A.get<float>(nint);
+    b.rdiag32 = A.get<float>(nint);
+    b.nxf = A.get<double>(n2);
+    b.nyf = A.get<double>(n2);
+    b.omega = A.get<double>(n2);
+    const size_t nq = 2 * (size_t)nframes;
+    b.terms = A.get<double>(8 * (size_t)nframes);
+    b.corr = A.get<double>(nq);
+    b.res = A.get<double>(nq);
+    b.rmean = A.get<double>(nq);
+    b.scale = A.get<double>(nq);
+    b.rz = A.get<double>(nq);
+    b.rz0 = A.get<double>(nq);
+    b.alpha = A.get<double>(nq);
+    b.beta = A.get<double>(nq);
+    b.in_set = A.get<int>(nq);
+    b.active = A.get<int>(nq);
+    b.iters = A.get<int>(nq);
+    CUDA_TRY(cudaMemsetAsync(b.iters, 0, nq * sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(b.active, 0, nq * sizeof(int), st));
+    b.tol2 = kInnerDrop * kInnerDrop;
+    b.partials = A.get<double>(8 * (size_t)ntiles);
+    b.tickets = A.get<unsigned int>(nframes);
+    CUDA_TRY(cudaMemsetAsync(b.tickets, 0, nframes * sizeof(unsigned int), st));
+    b.err = A.get<int>(1);
+    CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(int), st));
+
+    Trace tr("frames: compatibility and operator");
+    CUDA_TRY(launch_k_b2_compat(dfr, dtf, ntiles, b, st));
+    CUDA_TRY(launch_k_b2_build(dfr, dtf, ntiles, b, st));
+    std::vector<int> set(nq, 1), stall(nq, 0), act(nq);
+    std::vector<double> res(nq), scale(nq);
+    auto push_set = [&] {
+      CUDA_TRY(cudaMemcpyAsync(b.in_set, set.data(), nq * sizeof(int), cudaMemcpyHostToDevice, st));
+    };
+    auto pull = [&](void* h, const void* d, size_t bytes) {
+      CUDA_TRY(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+    };
+    push_set();
+    CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
+    pull(res.data(), b.res, nq * sizeof(double));
+    int err = 0;
+    pull(&err, b.err, sizeof(int));
+    if (err == 2) throw Error{FPM_E_NO_OUTER_FACE, "stair-step compatibility needs at least one fluid outer face"};
+    const int chunk_len = check_interval < 1 ? 1 : check_interval;
+    long long total = 0;
+    for (int outer = 0; outer < 100; outer++) {
+      bool any = false;
+      for (size_t q = 0; q < nq; q++) {
+        set[q] = res[q] > tolerance && res[q] == res[q] && stall[q] < 3;
+        scale[q] = res[q] > 0 ? 1.0 / res[q] : 1.0;
+        any = any || set[q];
+      }
+      if (!any || total >= max_sweeps) break;
+      push_set();
+      CUDA_TRY(cudaMemcpyAsync(b.scale, scale.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(launch_k_b2_start(dfr, dtf, ntiles, b, st));
+      int inner = 0;
+      {
+        TimedRun t(FPM_TIMER_FRAMES_ITER, 0, st);
+        while (total + inner < max_sweeps && inner < kInnerCap) {
+          int chunk = chunk_len;
+          if (chunk > max_sweeps - total - inner) chunk = (int)(max_sweeps - total - inner);
+          for (int n = 0; n < chunk; n++) CUDA_TRY(launch_b2_iteration(dfr, dtf, ntiles, b, st));
+          inner += chunk;
+          pull(act.data(), b.active, nq * sizeof(int));
+          bool live = false;
+          for (size_t q = 0; q < nq; q++) live = live || act[q];
+          if (!live) break;
+        }
+        t.n = inner;
+      }
+      total += inner;
+      CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
+      std::vector<double> old = res;
+      CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
+      pull(res.data(), b.res, nq * sizeof(double));
+      for (size_t q = 0; q < nq; q++)
+        if (set[q]) stall[q] = res[q] < 0.5 * old[q] ? 0 : stall[q] + 1;
+    }
+    Trace tg("frames: gauge and partition");
+    CUDA_TRY(launch_k_b2_gauge_sum(dfr, dtf, ntiles, b, st));
+    CUDA_TRY(launch_k_b2_gauge_sub(dfr, dtf, ntiles, b, st));
+    std::fill(set.begin(), set.end(), 1);
+    push_set();
+    CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
+    CUDA_TRY(launch_k_b2_part1(dfr, dtf, ntiles, b, st));
+    CUDA_TRY(launch_k_b2_part2(dfr, dtf, ntiles, b, st));
+    pull(residual, b.res, nq * sizeof(double));
+    pull(sweeps, b.iters, nq * sizeof(int));
+    pull(terms, b.terms, 8 * (size_t)nframes * sizeof(double));
+    if (phi_out) {
+      for (int f = 0; f < nframes; f++) {
+        if (!phi_out[f]) continue;
+        const Frame2& F = fr[f];
+        // layer k = 1 of each direction, (nx, ny) column-major, direction-major
+        for (int r = 0; r < 2; r++)
+          CUDA_TRY(cudaMemcpy2DAsync(phi_out[f] + (size_t)r * F.nx * F.ny, F.nx * sizeof(double),
+                                     b.phi[r] + F.opad + 1 + (F.nx + 2), (F.nx + 2) * sizeof(double),
+                                     F.nx * sizeof(double), F.ny, cudaMemcpyDeviceToHost, st));
+      }
+      CUDA_TRY(cudaStreamSynchronize(st));
+    }
   });
 }
 

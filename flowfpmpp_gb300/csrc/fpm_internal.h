@@ -106,6 +106,78 @@ void jacobi_df_shape(int shape, int* tx, int* ty);
 cudaError_t jacobi_df_sweep(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st);
 cudaError_t jacobi_df_unpack(const JacobiDfPlan& pl, const float2* cur, double* phi, cudaStream_t st);
 
+// Mixed-precision multi-right-hand-side PCG (fpm_pcg_mixed.cu).
+constexpr int kMaxRhs = 4;
+struct MixedVecs {
+  int nrhs;
+  const float *diag, *rdiag, *coef, *dx, *dy, *dz;  // FP32 copies of the operator
+  float *p[kMaxRhs], *q[kMaxRhs], *r[kMaxRhs], *e[kMaxRhs];
+};
+struct MixedScale {
+  double scale[kMaxRhs];
+  int in_set[kMaxRhs];
+};
+struct MixedScalars {
+  double rz[kMaxRhs], rz0[kMaxRhs], pq[kMaxRhs], alpha[kMaxRhs], beta[kMaxRhs], tol2[kMaxRhs];
+  int active[kMaxRhs];
+  int iters;
+  int pad[3];
+};
+struct DPtr4 {
+  double* p[kMaxRhs];
+};
+cudaError_t launch_mx_convert(const double* a, float* b, long long n, cudaStream_t st);
+cudaError_t launch_mx_start(const Dims& d, const MixedVecs& v, const DPtr4& rv64, const MixedScale& sc,
+                            MixedScalars* S, const RedBuf& rb, cudaStream_t st);
+cudaError_t launch_mx_iteration(const Dims& d, const MixedVecs& v, MixedScalars* S, const RedBuf& rb,
+                                cudaStream_t st);
+cudaError_t launch_mx_apply(const Dims& d, const MixedVecs& v, const DPtr4& phi, const MixedScale& sc,
+                            cudaStream_t st);
+
+// Batched uneven 2-D frames (fpm_frames2d.cu).
+struct Frame2 {
+  int nx, ny;           // cells; nz = 2 (dz = 0.5)
+  int tile0, ntiles;    // range in the tile list (32 x 8 columns)
+  int tiles_x;          // tiles along x
+  int ox, oy;           // offsets into the x / y axis pools (stride >= n+2 per frame)
+  long long opad;       // offset of padded 3-D fields, (nx+2)(ny+2)*2 per frame
+  long long oint;       // offset of interior 3-D fields, nx*ny*2 per frame
+  long long o2;         // offset of 2-D fields, nx*ny per frame
+  long long oring;      // offset of the outer ring, (2nx+2ny)*4 per frame
+};
+struct Batch2 {
+  // inputs
+  const double *xc, *yc, *dx, *dy, *xf, *yf;  // axis pools: xc(0:nx+1), dx(1:nx), xf(0:nx) at ox
+  const int32_t* solid3;                      // padded, both layers
+  const uint8_t* solid2;                      // (nx, ny)
+  const double *u, *v, *ring, *kin, *dt;
+  double nu;
+  // operator and solution (two directions)
+  double *src[2], *diag, *rdiag, *phi[2], *r64[2];
+  float *diag32, *rdiag32, *r32[2], *p32[2], *q32[2], *e32[2];
+  // partition
+  double *nxf, *nyf, *omega, *gpx[2], *gpy[2], *vif[2], *terms;
+  // per (frame, direction) scalars, index 2*f + r
+  double *corr, *res, *rmean, *scale, *rz, *rz0, *alpha, *beta;
+  int *in_set, *active, *iters;
+  double tol2;
+  double* partials;       // ntiles * 8
+  unsigned int* tickets;  // one per frame
+  int* err;
+};
+#define B2_DECL(kern) \
+  cudaError_t launch_##kern(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, cudaStream_t st);
+B2_DECL(k_b2_compat)
+B2_DECL(k_b2_build)
+B2_DECL(k_b2_tres)
+B2_DECL(k_b2_start)
+B2_DECL(k_b2_apply)
+B2_DECL(k_b2_gauge_sum)
+B2_DECL(k_b2_gauge_sub)
+B2_DECL(k_b2_part1)
+B2_DECL(k_b2_part2)
+cudaError_t launch_b2_iteration(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, cudaStream_t st);
+
 // ---- no-body Neumann solvers and densities (fpm_laplace.cu) --------------
 cudaError_t launch_neumann_compat(int nx, int ny, int nz, const double* rhs, Faces f, const double* dx,
                                   const double* dy, const double* dz, int uniform, double area_uniform,

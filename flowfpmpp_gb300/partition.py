@@ -38,3 +38,48 @@ def fpm_partition_terms_2d(phi, g, u, v, solid, xf, yf, kin, ring, dt, nu, nx=No
                                        _ptr(kk), _ptr(ring), _D(dt), _D(nu), _I(nx), _I(ny), _ptr(terms),
                                        _ptr(vif), _ptr(omega), _I(int(bool(slip_body)))))
     return terms, vif, omega
+
+
+def partition_frames_2d(frames, tolerance=1e-10, max_sweeps=2000000, check_interval=50, return_phi=False):
+    """Batched uneven 2-D frames: for each frame (dict with nx, ny, xf, yf, u,
+    v, solid, ring, kin, dt and a shared nu) the reference foil example's
+    phi_x, phi_y solve (examples/flapping_foil_fpm.f90:61-81) and
+    fpm_partition_terms_2d for both directions, all frames together on the GPU.
+    Returns (terms (nframes, 2, 4), sweeps (nframes, 2), residual (nframes, 2)
+    [, phi list of (2, nx, ny) arrays])."""
+    nf = len(frames)
+    VP = ctypes.c_void_p
+    keep = []
+
+    def arr(a, dtype):
+        a = np.asfortranarray(a, dtype=dtype)
+        keep.append(a)
+        return a.ctypes.data
+
+    nx = np.array([f["nx"] for f in frames], dtype=np.int32)
+    ny = np.array([f["ny"] for f in frames], dtype=np.int32)
+    xf = (VP * nf)(*[arr(f["xf"], np.float64) for f in frames])
+    yf = (VP * nf)(*[arr(f["yf"], np.float64) for f in frames])
+    u = (VP * nf)(*[arr(f["u"], np.float64) for f in frames])
+    v = (VP * nf)(*[arr(f["v"], np.float64) for f in frames])
+    solid = (VP * nf)(*[arr(np.asarray(f["solid"]) != 0, np.uint8) for f in frames])
+    ring = (VP * nf)(*[arr(f["ring"], np.float64) for f in frames])
+    kin = np.ascontiguousarray(np.concatenate([np.asarray(f["kin"], dtype=np.float64) for f in frames]))
+    dt = np.ascontiguousarray([float(f["dt"]) for f in frames])
+    nu = float(frames[0]["nu"])
+    terms = np.zeros((nf, 2, 4))
+    sweeps = np.zeros((nf, 2), dtype=np.int32)
+    res = np.zeros((nf, 2))
+    phis = None
+    phi_ptrs = None
+    if return_phi:
+        phis = [np.zeros((2, f["ny"], f["nx"])) for f in frames]
+        phi_ptrs = (VP * nf)(*[p.ctypes.data for p in phis])
+    check(lib().fpm_partition_frames_2d(_I(nf), _ptr(nx), _ptr(ny), xf, yf, u, v, solid, ring, _ptr(kin), _ptr(dt),
+                                        _D(nu), _D(tolerance), _I(max_sweeps), _I(check_interval), _ptr(terms),
+                                        _ptr(sweeps), _ptr(res), phi_ptrs))
+    if return_phi:
+        # (2, ny, nx) C-order buffers hold (nx, ny) Fortran-order planes
+        phis = [np.stack([np.asfortranarray(p[r].T) for r in range(2)]) for p in phis]
+        return terms, sweeps, res, phis
+    return terms, sweeps, res

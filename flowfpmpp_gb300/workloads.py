@@ -156,3 +156,64 @@ def flow_c1(frame, seed=11, ntubes=8, core=0.2, nmodes=6):
             acc[c] += amp[c] * arg
     F = lambda a: np.asfortranarray(a)
     return dict(u=F(u), v=F(v), w=F(w), ox=F(ox), oy=F(oy), oz=F(oz), ax=F(acc[0]), ay=F(acc[1]), az=F(acc[2]))
+
+
+def foil_frames_c4(nframes=256, seed=4, nmin=96, nmax=512, ratio=1.02, half_x=4.0, half_y=4.0, nvort=12,
+                   dt=0.4, nu=1e-4):
+    """Config 4: uneven 2-D frames in the fpm_partition_2d form.  Each frame:
+    nx, ny ~ U[nmin, nmax], geometric stretching `ratio` away from the centre
+    lines; an elliptic foil (chord 1, thickness 0.12) at pitch U[-30, 30]
+    degrees and heave U[-0.5, 0.5], blocked by cell centre; rigid-body
+    kinematics kin ~ N(0,1); velocity U=1 plus `nvort` Lamb-Oseen vortices
+    (circulation N(0,1), core U[0.05, 0.2]); the outer ring at t -/+ dt is
+    the frame's ring perturbed by N(0, 0.01 dt)."""
+    rng = np.random.default_rng(seed)
+    frames = []
+    for _ in range(nframes):
+        nx, ny = (int(v) for v in rng.integers(nmin, nmax + 1, size=2))
+        xf, xc, dx = geometric_axis(nx, -half_x, half_x, ratio)
+        yf, yc, dy = geometric_axis(ny, -half_y, half_y, ratio)
+        X = xc[1:nx + 1][:, None] * np.ones((nx, ny))
+        Y = yc[1:ny + 1][None, :] * np.ones((nx, ny))
+        pitch = math.radians(rng.uniform(-30, 30))
+        heave = rng.uniform(-0.5, 0.5)
+        cp, sp = math.cos(pitch), math.sin(pitch)
+        xr = cp * X + sp * (Y - heave)
+        yr = -sp * X + cp * (Y - heave)
+        solid = ((xr / 0.5) ** 2 + (yr / 0.06) ** 2 < 1.0).astype(np.uint8)
+        if solid.sum() == 0:  # keep at least one blocked cell at the foil centre
+            solid[np.argmin(np.abs(xc[1:nx + 1])), np.argmin(np.abs(yc[1:ny + 1] - heave))] = 1
+        u = np.ones((nx, ny))
+        v = np.zeros((nx, ny))
+        for _ in range(nvort):
+            x0, y0 = rng.uniform(-half_x, half_x), rng.uniform(-half_y, half_y)
+            gam, rc = rng.standard_normal(), rng.uniform(0.05, 0.2)
+            r2 = (X - x0) ** 2 + (Y - y0) ** 2
+            fac = np.where(r2 > 0, gam / (2 * math.pi) * (1 - np.exp(-r2 / rc ** 2)) / np.where(r2 > 0, r2, 1.0), 0.0)
+            u -= fac * (Y - y0)
+            v += fac * (X - x0)
+        fluid = solid == 0
+        u *= fluid
+        v *= fluid
+        ring = np.zeros((2 * nx + 2 * ny, 2, 2), order="F")
+        base_u = np.concatenate([u[0, :], u[nx - 1, :], u[:, 0], u[:, ny - 1]])
+        base_v = np.concatenate([v[0, :], v[nx - 1, :], v[:, 0], v[:, ny - 1]])
+        for t, sgn in ((0, -1.0), (1, 1.0)):
+            ring[:, 0, t] = base_u + sgn * rng.normal(0, 0.01 * dt, base_u.size)
+            ring[:, 1, t] = base_v + sgn * rng.normal(0, 0.01 * dt, base_v.size)
+        frames.append(dict(nx=nx, ny=ny, xf=xf, yf=yf, xc=xc, yc=yc, dx=dx, dy=dy,
+                           solid=np.asfortranarray(solid), u=np.asfortranarray(u), v=np.asfortranarray(v),
+                           ring=ring, kin=rng.standard_normal(6), dt=dt, nu=nu))
+    return frames
+
+
+def frame_as_stairstep(fr):
+    """The reference's 2-D use of the 3-D solver (examples/flapping_foil_fpm.f90:
+    nz = 2, dz = 0.5, zero z-face data): padded solid, axes and zero faces."""
+    nx, ny, nz = fr["nx"], fr["ny"], 2
+    solid = np.zeros((nx + 2, ny + 2, nz), dtype=np.int32, order="F")
+    for k in range(nz):
+        solid[1:nx + 1, 1:ny + 1, k] = fr["solid"]
+    return dict(nx=nx, ny=ny, nz=nz, xc=fr["xc"], yc=fr["yc"], zc=np.array([0.25, 0.75]), dx=fr["dx"], dy=fr["dy"],
+                dz=np.array([0.5, 0.5]), solid=solid, rhs=np.zeros((nx, ny, nz), order="F"),
+                phi=np.zeros((nx + 2, ny + 2, nz), order="F"), faces=_empty_faces(nx, ny, nz))

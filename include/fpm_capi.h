@@ -58,6 +58,8 @@ extern "C" {
                                    -ffp-contract=off evaluation (reference 'jacobi') */
 #define FPM_METHOD_JACOBI_DF 2  /* weighted Jacobi in double-float (f32 pair, 48-bit significand)
                                    arithmetic with FP64 residual checks: same iteration, HBM-bound on GB300 */
+#define FPM_METHOD_PCG_MIXED 3  /* FP64 iterative refinement (true residual, max-norm test, phi update in FP64)
+                                   around FP32 diagonal PCG; max_sweeps caps the FP32 iterations */
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char* fpm_last_error(void);
@@ -70,7 +72,9 @@ int fpm_version(void);
 #define FPM_TIMER_JACOBI_DF 0   /* double-float Jacobi sweep (TMA-streamed) */
 #define FPM_TIMER_JACOBI_F64 1  /* FP64 Jacobi sweep */
 #define FPM_TIMER_PCG_ITER 2    /* one FP64 PCG iteration (three kernels) */
-#define FPM_TIMER_COUNT 4
+#define FPM_TIMER_PCG_MIXED_ITER 3 /* one FP32 inner PCG iteration over all right-hand sides */
+#define FPM_TIMER_FRAMES_ITER 4 /* one batched FP32 PCG iteration over every frame of a 2-D batch */
+#define FPM_TIMER_COUNT 5
 int fpm_timing_enable(int on);
 /* Number of kernels this library has launched in this process. */
 long long fpm_kernel_launches(void);
@@ -117,6 +121,19 @@ int fpm_solve_stairstep_poisson_3d_dev(double* phi, const double* rhs, const int
                                        const double* zc, const double* dx, const double* dy, const double* dz, int nx,
                                        int ny, int nz, double tolerance, int max_sweeps, int check_interval,
                                        int method, int* sweeps, double* residual, void* stream);
+
+/* Several right-hand sides (1..4; e.g. the phi_x, phi_y, phi_z influence
+ * fields) on one grid: solve_stairstep_poisson_3d for each, in one call.
+ * phi[m], rhs[m] are device pointers; faces[6*m + f] the six face arrays of
+ * right-hand side m (xlo, xhi, ylo, yhi, zlo, zhi); body_grads[3*m + q] is host
+ * memory; solid and the axes are shared.  FPM_METHOD_PCG_MIXED iterates all
+ * right-hand sides together (shared operator reads); the FP64 methods solve
+ * them one after the other.  sweeps[m], residual[m] per right-hand side. */
+int fpm_solve_stairstep_multi_dev(int nrhs, double* const* phi, const double* const* rhs, const int32_t* solid,
+                                  const double* body_grads, const double* const* faces, const double* xc,
+                                  const double* yc, const double* zc, const double* dx, const double* dy,
+                                  const double* dz, int nx, int ny, int nz, double tolerance, int max_sweeps,
+                                  int check_interval, int method, int* sweeps, double* residual, void* stream);
 
 /* stairstep_residual_3d (src/fpm_stairstep_mpi_3d.f90:403-419): independent
  * max-norm residual of L(phi)-f from face gradients. */
@@ -202,6 +219,24 @@ int fpm_partition_terms_2d(const double* phi, const double* g, const double* u, 
                            const uint8_t* solid, const double* xf, const double* yf, const double* kin,
                            const double* ring, double dt, double nu, int nx, int ny, double* terms,
                            double* vif_density, double* omega, int slip_body);
+
+/* ---- batched 2-D frames (examples/flapping_foil_fpm.f90:61-81 per frame) ---
+ * For each of nframes independent 2-D frames (cells nx[f] x ny[f], faces
+ * xf[f](0:nx), yf[f](0:ny), velocity u[f], v[f] (nx,ny), solid[f] (nx,ny)
+ * uint8, ring[f](2nx+2ny,2,2), kin[6f..6f+5], dt[f]): the influence
+ * potentials phi_x and phi_y as the reference's foil example computes them
+ * (nz = 2, dz = 0.5, zero outer data, compatibility, solve to `tolerance`),
+ * then fpm_partition_terms_2d (src/fpm_partition_2d.f90:35-154) for each.
+ * All frames are solved together (mixed-precision PCG, FP64 refinement and
+ * max-norm test per frame and direction).  Outputs, host memory:
+ * terms[8f + 4r + t] (r = 0 x, 1 y; t = KINE, VIF, VIS, BOUND), sweeps[2f + r]
+ * (FP32 iterations), residual[2f + r] (final max-norm), and, when phi_out and
+ * phi_out[f] are non-NULL, layer 1 of phi_x then phi_y as 2 x (nx,ny). */
+int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const double* const* xf,
+                            const double* const* yf, const double* const* u, const double* const* v,
+                            const uint8_t* const* solid, const double* const* ring, const double* kin,
+                            const double* dt, double nu, double tolerance, int max_sweeps, int check_interval,
+                            double* terms, int* sweeps, double* residual, double* const* phi_out);
 
 /* ---- operator-level entry points (device arrays) ------------------------
  * The private building blocks of solve_stairstep_poisson_3d, exposed so a
