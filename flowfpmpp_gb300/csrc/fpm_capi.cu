@@ -1517,4 +1517,20 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
   });
 }
 
+int fpm_stairstep_operator_residual_noalloc_dev(const double* phi, const double* src, const double* diag,
+                                                const double* xc, const double* yc, const double* zc,
+                                                const double* dx, const double* dy, const double* dz, int nx, int ny,
+                                                int nz, double* value, void* stream) {
+  return guarded([&] {
+    if (!phi || !src || !diag || !xc || !yc || !zc || !dx || !dy || !dz || !value)
+      throw Error{FPM_E_ARG, "null argument"};
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    std::string msg;
+    const int rc = operator_residual_noalloc(phi, src, diag, Axes{xc, yc, zc, dx, dy, dz}, nx, ny, nz, value,
+                                             (cudaStream_t)stream, &msg);
+    if (rc != FPM_OK) throw Error{rc, msg};
+  });
+}
+
 }  // extern "C"

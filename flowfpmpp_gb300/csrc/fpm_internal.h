@@ -209,6 +209,11 @@ cudaError_t launch_partition_2d(const Part2D& p, double* nxf, double* nyf, doubl
                                 double* vif_density, double* omega, SolveScalars* S, const RedBuf& rb,
                                 cudaStream_t st);
 
+// Allocation-free max-norm operator residual (fpm_noalloc.cu); returns a
+// status code and fills *msg on failure.
+int operator_residual_noalloc(const double* phi, const double* src, const double* diag, const Axes& ax, int nx, int ny,
+                              int nz, double* value, cudaStream_t st, std::string* msg);
+
 // Host-side count of kernel launches made by this library (fpm_capi.cu).
 void note_launch();
 

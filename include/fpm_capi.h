@@ -265,6 +265,23 @@ int fpm_stairstep_operator_residual_dev(const double* phi, const double* src, co
                                         const double* yc, const double* zc, const double* dx, const double* dy,
                                         const double* dz, int nx, int ny, int nz, double* value, void* stream);
 
+/* Allocation-free form of fpm_stairstep_operator_residual_dev.  No counterpart
+ * in the reference: it exists for callers that cannot allocate GPU memory
+ * while they run (a fixed memory pool, an allocator policy that forbids
+ * cudaMalloc, or a hard cap on the process's GPU footprint).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine: its scratch is a fixed
+ * file-scope device array (about 200 KB, held on every GPU that loads the
+ * library until the process exits).  Limit: nx + ny + nz <= 12288, else
+ * FPM_E_LIMIT.  The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array, so calls whose GPU
+ * work overlaps (different streams or host threads) race: serialise them.
+ * Same arguments and result as fpm_stairstep_operator_residual_dev. */
+int fpm_stairstep_operator_residual_noalloc_dev(const double* phi, const double* src, const double* diag,
+                                                const double* xc, const double* yc, const double* zc,
+                                                const double* dx, const double* dy, const double* dz, int nx, int ny,
+                                                int nz, double* value, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
