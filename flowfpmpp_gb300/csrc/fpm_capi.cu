@@ -164,6 +164,24 @@ struct TimedRun {
   }
 };
 
+// ---------------------------------------------------------------- options
+// FPM_VERBOSE=1 prints one line per convergence check of every solver loop
+// to stderr.  FPM_PCG_STALL_CHECKS overrides the number of checks without a
+// 1% improvement after which PCG stops (50, src/fpm_stairstep_mpi_3d.f90:288).
+static bool verbose() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("FPM_VERBOSE");
+    v = (e && e[0] && e[0] != '0') ? 1 : 0;
+  }
+  return v == 1;
+}
+static int stall_checks() {
+  const char* e = std::getenv("FPM_PCG_STALL_CHECKS");
+  const int n = e ? std::atoi(e) : 50;
+  return n > 0 ? n : 50;
+}
+
 // ---------------------------------------------------------------- solve
 struct SolveArgs {
   double* phi;
@@ -190,6 +208,7 @@ static double pcg_loop(const SolveArgs& a, const Dims& d, double* p, const doubl
   CUDA_TRY(launch_true_residual(d, a.phi, src, diag, rdiag, r, p, c, a.ax, 1, cm.S, cm.rb, st));
   double res = read_scalars(cm.S, st).res;
   const int ci = a.ci < 1 ? 1 : a.ci;
+  const int max_stalled = stall_checks();
   int it = 0, restarts = 0, stalled = 0;
   double best = res;
   int sw = 0;
@@ -217,13 +236,14 @@ static double pcg_loop(const SolveArgs& a, const Dims& d, double* p, const doubl
     if (halt == 2) break;
     CUDA_TRY(launch_true_residual(d, a.phi, src, diag, rdiag, r, p, c, a.ax, 0, cm.S, cm.rb, st));
     res = read_scalars(cm.S, st).res;
+    if (verbose()) std::fprintf(stderr, "fpm pcg: iterations %d residual %.3e\n", sw, res);
     if (res < 0.99 * best) {
       best = res;
       stalled = 0;
     } else {
       stalled++;
     }
-    if (stalled >= 50 || !(res == res)) break;
+    if (stalled >= max_stalled || !(res == res)) break;
   }
   *sweeps = sw;
   return res;
@@ -395,14 +415,23 @@ static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src,
   *sweeps = sw;
 }
 
-// Mixed-precision PCG for 1..4 right-hand sides sharing the operator:
-// outer FP64 true residual and max-norm test, inner FP32 PCG batched over the
-// right-hand sides (see fpm_pcg_mixed.cu).  Every inner solve reduces the
-// preconditioned residual norm by kInnerDrop; the outer loop stops when every
-// max-norm residual is <= tol, when max_sweeps inner iterations have run, or
-// after three outer steps in a row without halving any residual.
-constexpr double kInnerDrop = 1e-4;
-constexpr int kInnerCap = 20000;
+// Mixed-precision PCG for 1..4 right-hand sides sharing the operator.
+// One FP32 diagonal PCG per right-hand side (batched in the same kernels)
+// whose residual is periodically replaced by the FP64 true residual -- the
+// reference's true-residual replacement (src/fpm_stairstep_mpi_3d.f90:285-290)
+// done as a reliable update: the FP32 correction is added to phi in FP64, the
+// projected FP64 residual r = b - A phi becomes the new FP32 residual
+// (rescaled to unit max-norm) and the search direction is kept, rescaled, so
+// the Krylov process continues instead of restarting.  An update happens
+// when the FP32 preconditioned residual norm has dropped by kUpdateDrop since
+// the last one, after kUpdateMax iterations, or on a breakdown (then p
+// restarts from rdiag r).  Convergence is decided on the FP64 max-norm
+// residual at each update, exactly the reference's test; a right-hand side
+// also stops after kStallUpdates updates without a 1% improvement (the
+// reference's roundoff-floor rule, counted in updates).
+constexpr double kUpdateDrop = 1e-3;
+constexpr int kUpdateMax = 1000;
+constexpr int kStallUpdates = 4;
 
 static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
                         const double* rdiag, const double* coef64, const Axes& ax, const Coefs& c, double tol,
@@ -437,71 +466,114 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
     v.q[m] = A.get<float>(nc);
     v.r[m] = A.get<float>(nc);
     v.e[m] = A.get<float>(nc);
+    CUDA_TRY(cudaMemsetAsync(v.e[m], 0, nc * sizeof(float), st));
     r64.p[m] = A.get<double>(nc);
     phis.p[m] = phi[m];
     S64[m] = A.get<SolveScalars>(1);
     CUDA_TRY(cudaMemsetAsync(S64[m], 0, sizeof(SolveScalars), st));
   }
   MixedScalars* MS = A.get<MixedScalars>(1);
-  {
-    MixedScalars h;
-    std::memset(&h, 0, sizeof(h));
-    for (int m = 0; m < kMaxRhs; m++) h.tol2[m] = kInnerDrop * kInnerDrop;
-    CUDA_TRY(cudaMemcpyAsync(MS, &h, sizeof(h), cudaMemcpyHostToDevice, st));
-  }
+  CUDA_TRY(cudaMemsetAsync(MS, 0, sizeof(MixedScalars), st));  // tol2 = 0: the host decides the updates
   auto true_res = [&](int m) {
     CUDA_TRY(launch_true_residual(d, phi[m], src[m], diag, rdiag, r64.p[m], nullptr, c, ax, 0, S64[m], cm.rb, st));
     return read_scalars(S64[m], st).res;
   };
-  double res[kMaxRhs];
-  for (int m = 0; m < nrhs; m++) res[m] = true_res(m);
   MixedScalars* hms = nullptr;
   CUDA_TRY(cudaMallocHost(&hms, sizeof(MixedScalars)));
   struct HostFree {
     void* p;
     ~HostFree() { cudaFreeHost(p); }
   } hf{hms};
-  const int chunk_len = ci < 1 ? 1 : ci;
-  int total = 0, stall = 0;
-  for (int outer = 0; outer < 100; outer++) {
-    MixedScale sc;
-    std::memset(&sc, 0, sizeof(sc));
-    bool any = false;
-    for (int m = 0; m < nrhs; m++) {
-      sc.in_set[m] = res[m] > tol && res[m] == res[m];
-      sc.scale[m] = res[m] > 0 ? 1.0 / res[m] : 1.0;
-      any = any || sc.in_set[m];
-    }
-    if (!any || total >= max_sweeps) break;
-    CUDA_TRY(launch_mx_start(d, v, r64, sc, MS, cm.rb, st));
-    int inner = 0;
-    {
-      TimedRun t(FPM_TIMER_PCG_MIXED_ITER, 0, st);
-      while (total + inner < max_sweeps && inner < kInnerCap) {
-        int chunk = chunk_len;
-        if (chunk > max_sweeps - total - inner) chunk = max_sweeps - total - inner;
-        for (int n = 0; n < chunk; n++) CUDA_TRY(launch_mx_iteration(d, v, MS, cm.rb, st));
-        CUDA_TRY(cudaMemcpyAsync(hms, MS, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        inner = hms->iters;
-        bool act = false;
-        for (int m = 0; m < nrhs; m++) act = act || hms->active[m];
-        if (!act) break;
-      }
-      t.n = inner;
-    }
-    total += inner;
-    CUDA_TRY(launch_mx_apply(d, v, phis, sc, st));
-    bool improved = false;
-    for (int m = 0; m < nrhs; m++) {
-      if (!sc.in_set[m]) continue;
-      const double r = true_res(m);
-      improved = improved || r < 0.5 * res[m];
-      res[m] = r;
-    }
-    stall = improved ? 0 : stall + 1;
-    if (stall >= 3) break;
+
+  double res[kMaxRhs], best[kMaxRhs], scale[kMaxRhs];
+  int stall[kMaxRhs] = {}, since[kMaxRhs] = {};
+  bool live[kMaxRhs] = {};
+  MixedScale sc;
+  std::memset(&sc, 0, sizeof(sc));
+  bool any = false;
+  for (int m = 0; m < nrhs; m++) {
+    res[m] = best[m] = true_res(m);
+    live[m] = res[m] > tol && res[m] == res[m];
+    scale[m] = res[m] > 0 ? 1.0 / res[m] : 1.0;
+    sc.in_set[m] = live[m];
+    sc.scale[m] = scale[m];
+    sc.pmul[m] = 0.0;
+    any = any || live[m];
   }
+  if (any) CUDA_TRY(launch_mx_start(d, v, r64, sc, MS, cm.rb, st));
+  const int chunk_len = ci < 1 ? 1 : ci;
+  int total = 0;
+  while (any && total < max_sweeps) {
+    int chunk = chunk_len;
+    if (chunk > max_sweeps - total) chunk = max_sweeps - total;
+    CUDA_TRY(cudaMemsetAsync(&MS->iters, 0, sizeof(int), st));
+    {
+      TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
+      for (int n = 0; n < chunk; n++) CUDA_TRY(launch_mx_iteration(d, v, MS, cm.rb, st));
+    }
+    CUDA_TRY(cudaMemcpyAsync(hms, MS, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    total += chunk;
+    // Which right-hand sides need a reliable update now?
+    std::memset(&sc, 0, sizeof(sc));
+    bool upd = false;
+    for (int m = 0; m < nrhs; m++) {
+      if (!live[m]) continue;
+      since[m] += chunk;
+      const bool broke = !hms->active[m];
+      if (broke || hms->rz[m] < kUpdateDrop * kUpdateDrop * hms->rz0[m] || since[m] >= kUpdateMax ||
+          total >= max_sweeps) {
+        sc.in_set[m] = 1;
+        sc.scale[m] = scale[m];          // the scale the correction was computed in
+        sc.pmul[m] = broke ? 0.0 : 1.0;  // rescaled below
+        upd = true;
+      }
+    }
+    if (!upd) continue;
+    CUDA_TRY(launch_mx_apply(d, v, phis, sc, st));
+    any = false;
+    for (int m = 0; m < nrhs; m++) {
+      if (sc.in_set[m]) {
+        since[m] = 0;
+        res[m] = true_res(m);
+        if (res[m] < 0.99 * best[m]) {
+          best[m] = res[m];
+          stall[m] = 0;
+        } else {
+          stall[m]++;
+        }
+        if (!(res[m] > tol) || !(res[m] == res[m]) || stall[m] >= kStallUpdates) {
+          live[m] = false;
+          sc.in_set[m] = 0;
+          // park it: no further iterations for this right-hand side
+          const int zero = 0;
+          CUDA_TRY(cudaMemcpyAsync(&MS->active[m], &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+        } else {
+          const double ns = res[m] > 0 ? 1.0 / res[m] : 1.0;
+          if (sc.pmul[m] != 0.0) sc.pmul[m] = ns / scale[m];
+          scale[m] = ns;
+          sc.scale[m] = ns;
+        }
+      }
+      any = any || live[m];
+    }
+    if (verbose())
+      std::fprintf(stderr, "fpm pcg_mixed: iterations %d residual %.3e %.3e %.3e\n", total, res[0],
+                   nrhs > 1 ? res[1] : 0.0, nrhs > 2 ? res[2] : 0.0);
+    bool refresh = false;
+    for (int m = 0; m < nrhs; m++) refresh = refresh || sc.in_set[m];
+    if (refresh) CUDA_TRY(launch_mx_start(d, v, r64, sc, MS, cm.rb, st));
+  }
+  // Fold in any correction still pending (right-hand sides stopped by the cap).
+  std::memset(&sc, 0, sizeof(sc));
+  bool pend = false;
+  for (int m = 0; m < nrhs; m++)
+    if (live[m]) {
+      sc.in_set[m] = 1;
+      sc.scale[m] = scale[m];
+      pend = true;
+    }
+  if (pend) CUDA_TRY(launch_mx_apply(d, v, phis, sc, st));
   for (int m = 0; m < nrhs; m++) sweeps_out[m] = total;
 }
 
@@ -1430,7 +1502,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     b.iters = A.get<int>(nq);
     CUDA_TRY(cudaMemsetAsync(b.iters, 0, nq * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(b.active, 0, nq * sizeof(int), st));
-    b.tol2 = kInnerDrop * kInnerDrop;
+    b.tol2 = 0.0;  // the host decides the residual replacements
+    b.pmul = A.get<double>(nq);
     b.partials = A.get<double>(8 * (size_t)ntiles);
     b.tickets = A.get<unsigned int>(nframes);
     CUDA_TRY(cudaMemsetAsync(b.tickets, 0, nframes * sizeof(unsigned int), st));
@@ -1455,41 +1528,98 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     int err = 0;
     pull(&err, b.err, sizeof(int));
     if (err == 2) throw Error{FPM_E_NO_OUTER_FACE, "stair-step compatibility needs at least one fluid outer face"};
+    // Reliable updates per (frame, direction), as in mixed_solve.
     const int chunk_len = check_interval < 1 ? 1 : check_interval;
     long long total = 0;
-    for (int outer = 0; outer < 100; outer++) {
-      bool any = false;
-      for (size_t q = 0; q < nq; q++) {
-        set[q] = res[q] > tolerance && res[q] == res[q] && stall[q] < 3;
-        scale[q] = res[q] > 0 ? 1.0 / res[q] : 1.0;
-        any = any || set[q];
-      }
-      if (!any || total >= max_sweeps) break;
+    std::vector<double> best(res), pmul(nq, 0.0), rz(nq), rz0(nq);
+    std::vector<int> live(nq), since(nq, 0);
+    bool any = false;
+    for (size_t q = 0; q < nq; q++) {
+      live[q] = res[q] > tolerance && res[q] == res[q];
+      set[q] = live[q];
+      scale[q] = res[q] > 0 ? 1.0 / res[q] : 1.0;
+      any = any || live[q];
+    }
+    auto push_start = [&] {
       push_set();
       CUDA_TRY(cudaMemcpyAsync(b.scale, scale.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(b.pmul, pmul.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
       CUDA_TRY(launch_k_b2_start(dfr, dtf, ntiles, b, st));
-      int inner = 0;
+    };
+    if (any) push_start();
+    while (any && total < max_sweeps) {
+      int chunk = chunk_len;
+      if (chunk > max_sweeps - total) chunk = (int)(max_sweeps - total);
       {
-        TimedRun t(FPM_TIMER_FRAMES_ITER, 0, st);
-        while (total + inner < max_sweeps && inner < kInnerCap) {
-          int chunk = chunk_len;
-          if (chunk > max_sweeps - total - inner) chunk = (int)(max_sweeps - total - inner);
-          for (int n = 0; n < chunk; n++) CUDA_TRY(launch_b2_iteration(dfr, dtf, ntiles, b, st));
-          inner += chunk;
-          pull(act.data(), b.active, nq * sizeof(int));
-          bool live = false;
-          for (size_t q = 0; q < nq; q++) live = live || act[q];
-          if (!live) break;
-        }
-        t.n = inner;
+        TimedRun t(FPM_TIMER_FRAMES_ITER, chunk, st);
+        for (int n = 0; n < chunk; n++) CUDA_TRY(launch_b2_iteration(dfr, dtf, ntiles, b, st));
       }
-      total += inner;
+      total += chunk;
+      pull(act.data(), b.active, nq * sizeof(int));
+      pull(rz.data(), b.rz, nq * sizeof(double));
+      pull(rz0.data(), b.rz0, nq * sizeof(double));
+      bool upd = false;
+      for (size_t q = 0; q < nq; q++) {
+        set[q] = 0;
+        if (!live[q]) continue;
+        since[q] += chunk;
+        const bool broke = !act[q];
+        if (broke || rz[q] < kUpdateDrop * kUpdateDrop * rz0[q] || since[q] >= kUpdateMax || total >= max_sweeps) {
+          set[q] = 1;
+          pmul[q] = broke ? 0.0 : 1.0;
+          upd = true;
+        }
+      }
+      if (!upd) continue;
+      push_set();  // apply with the scales the corrections were computed in
       CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
-      std::vector<double> old = res;
       CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
       pull(res.data(), b.res, nq * sizeof(double));
-      for (size_t q = 0; q < nq; q++)
-        if (set[q]) stall[q] = res[q] < 0.5 * old[q] ? 0 : stall[q] + 1;
+      any = false;
+      for (size_t q = 0; q < nq; q++) {
+        if (set[q]) {
+          since[q] = 0;
+          if (res[q] < 0.99 * best[q]) {
+            best[q] = res[q];
+            stall[q] = 0;
+          } else {
+            stall[q]++;
+          }
+          if (!(res[q] > tolerance) || !(res[q] == res[q]) || stall[q] >= kStallUpdates) {
+            live[q] = 0;
+            set[q] = 0;
+            act[q] = 0;
+          } else {
+            const double ns = res[q] > 0 ? 1.0 / res[q] : 1.0;
+            if (pmul[q] != 0.0) pmul[q] = ns / scale[q];
+            scale[q] = ns;
+          }
+        }
+        any = any || live[q];
+      }
+      CUDA_TRY(cudaMemcpyAsync(b.active, act.data(), nq * sizeof(int), cudaMemcpyHostToDevice, st));
+      bool refresh = false;
+      for (size_t q = 0; q < nq; q++) refresh = refresh || set[q];
+      if (refresh) push_start();
+      if (verbose()) {
+        int nlive = 0;
+        double worst = 0;
+        for (size_t q = 0; q < nq; q++) {
+          nlive += live[q];
+          if (live[q] && res[q] > worst) worst = res[q];
+        }
+        std::fprintf(stderr, "fpm frames: iterations %lld live %d worst live residual %.3e\n", total, nlive, worst);
+      }
+    }
+    // fold in corrections still pending (stopped by the iteration cap)
+    bool pend = false;
+    for (size_t q = 0; q < nq; q++) {
+      set[q] = live[q];
+      pend = pend || live[q];
+    }
+    if (pend) {
+      push_set();
+      CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
     }
     Trace tg("frames: gauge and partition");
     CUDA_TRY(launch_k_b2_gauge_sum(dfr, dtf, ntiles, b, st));
@@ -1530,6 +1660,57 @@ int fpm_stairstep_operator_residual_noalloc_dev(const double* phi, const double*
     const int rc = operator_residual_noalloc(phi, src, diag, Axes{xc, yc, zc, dx, dy, dz}, nx, ny, nz, value,
                                              (cudaStream_t)stream, &msg);
     if (rc != FPM_OK) throw Error{rc, msg};
+  });
+}
+
+int fpm_partition_terms_3d(const double* phi, const double* g, const double* u, const double* v, const double* w,
+                           const uint8_t* solid, const double* xf, const double* yf, const double* zf,
+                           const double* kin, const double* shell, double dt, double nu, int nx, int ny, int nz,
+                           double* terms, double* vif_density, double* omega, int slip_body) {
+  return guarded([&] {
+    if (!phi || !g || !u || !v || !w || !solid || !xf || !yf || !zf || !kin || !terms || !vif_density)
+      throw Error{FPM_E_ARG, "null argument"};
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = 0;
+    Scratch A(st);
+    const size_t n3 = (size_t)nx * ny * nz;
+    const size_t L = 2 * (size_t)ny * nz + 2 * (size_t)nx * nz + 2 * (size_t)nx * ny;
+    Common cm;
+    cm.S = A.get<SolveScalars>(1);
+    CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
+    const int nb = ((nx + 31) / 32) * ((ny + 7) / 8) * nz;
+    cm.rb.max_blocks = nb;
+    cm.rb.partials = A.get<double>((size_t)4 * nb);
+    cm.rb.ticket = A.get<unsigned int>(1);
+    CUDA_TRY(cudaMemsetAsync(cm.rb.ticket, 0, sizeof(unsigned int), st));
+    Part3D p;
+    p.phi = A.upload(phi, n3);
+    p.u = A.upload(u, n3);
+    p.v = A.upload(v, n3);
+    p.w = A.upload(w, n3);
+    p.solid = A.upload(solid, n3);
+    p.xf = A.upload(xf, (size_t)nx + 1);
+    p.yf = A.upload(yf, (size_t)ny + 1);
+    p.zf = A.upload(zf, (size_t)nz + 1);
+    p.kin = A.upload(kin, 12);
+    p.shell = shell ? A.upload(shell, 6 * L) : nullptr;
+    for (int a = 0; a < 3; a++) p.g[a] = g[a];
+    p.dt = dt;
+    p.nu = nu;
+    p.nx = nx;
+    p.ny = ny;
+    p.nz = nz;
+    p.slip = slip_body ? 1 : 0;
+    double* scratch = A.get<double>(6 * n3);
+    double* dvif = A.get<double>(n3);
+    double* domega = omega ? A.get<double>(3 * n3) : nullptr;
+    CUDA_TRY(launch_partition_3d(p, scratch, dvif, domega, cm.S, cm.rb, st));
+    const SolveScalars& h = read_scalars(cm.S, st);
+    for (int m = 0; m < 4; m++) terms[m] = h.red[m];
+    download(vif_density, dvif, n3 * sizeof(double), st);
+    if (omega) download(omega, domega, 3 * n3 * sizeof(double), st);
+    CUDA_TRY(cudaStreamSynchronize(st));
   });
 }
 

@@ -266,6 +266,8 @@ __global__ void k_b2_tres(const Frame2* __restrict__ fr, const int* __restrict__
 }
 
 // ---------------------------------------------------------------- FP32 inner PCG
+// Residual replacement (reliable update) for the (frame, direction) pairs in
+// the set: r = scale (rV - mean), e = 0, p = rdiag r (pmul == 0) or p *= pmul.
 __global__ void k_b2_start(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
   const TileRef t = tile_ref(fr, tile_frame);
   const Frame2& F = fr[t.f];
@@ -284,8 +286,9 @@ __global__ void k_b2_start(const Frame2* __restrict__ fr, const int* __restrict_
         const double rv = fl ? b.r64[r][c] - b.rmean[t.f * kR + r] : 0.0;
         const float rr = (float)(rv * b.scale[t.f * kR + r]);
         const float z = rd * rr;
+        const float pm = (float)b.pmul[t.f * kR + r];
         b.r32[r][c] = rr;
-        b.p32[r][p] = z;
+        b.p32[r][p] = pm == 0.f ? z : b.p32[r][p] * pm;
         b.e32[r][c] = 0.f;
         acc[r].add_prod(z, rr);
       }

@@ -115,6 +115,7 @@ struct MixedVecs {
 };
 struct MixedScale {
   double scale[kMaxRhs];
+  double pmul[kMaxRhs];  // 0: restart p from rdiag r; else rescale p by pmul
   int in_set[kMaxRhs];
 };
 struct MixedScalars {
@@ -158,7 +159,7 @@ struct Batch2 {
   // partition
   double *nxf, *nyf, *omega, *gpx[2], *gpy[2], *vif[2], *terms;
   // per (frame, direction) scalars, index 2*f + r
-  double *corr, *res, *rmean, *scale, *rz, *rz0, *alpha, *beta;
+  double *corr, *res, *rmean, *scale, *pmul, *rz, *rz0, *alpha, *beta;
   int *in_set, *active, *iters;
   double tol2;
   double* partials;       // ntiles * 8
@@ -216,6 +217,16 @@ int operator_residual_noalloc(const double* phi, const double* src, const double
 
 // Host-side count of kernel launches made by this library (fpm_capi.cu).
 void note_launch();
+
+// ---- 3-D four-term partition (fpm_partition3d.cu) --------------------------
+struct Part3D {
+  const double *phi, *u, *v, *w, *xf, *yf, *zf, *kin, *shell;
+  const uint8_t* solid;
+  double g[3], dt, nu;
+  int nx, ny, nz, slip;
+};
+cudaError_t launch_partition_3d(const Part3D& p, double* scratch, double* vif, double* omega, SolveScalars* S,
+                                const RedBuf& rb, cudaStream_t st);
 
 // ---- error reporting (fpm_capi.cu) ----------------------------------------
 void set_error(const std::string& msg);

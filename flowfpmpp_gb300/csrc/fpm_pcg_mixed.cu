@@ -44,7 +44,10 @@ __global__ void k_mx_convert(long long n, const double* __restrict__ a, float* _
     b[m] = (float)a[m];
 }
 
-// r = scale * rV (FP64 -> FP32), p = z = rdiag r, e = 0, rz = r.z.
+// Residual replacement for the right-hand sides in the set: r = scale * rV
+// (the projected FP64 true residual), e = 0, and either a restart from the
+// steepest-descent direction p = rdiag r (pmul == 0) or the current direction
+// rescaled to the new residual scale (p *= pmul); rz = r.(rdiag r).
 __global__ void k_mx_start(Dims d, MixedVecs v, DPtr4 rv64, MixedScale sc,
                            MixedScalars* S, RedBuf rb) {
   double s[kMaxRhs] = {0.0, 0.0, 0.0, 0.0}, mm[1] = {0.0};
@@ -58,7 +61,8 @@ __global__ void k_mx_start(Dims d, MixedVecs v, DPtr4 rv64, MixedScale sc,
       const float r = (float)(rv64.p[m][c] * sc.scale[m]);
       const float z = rd * r;
       v.r[m][c] = r;
-      v.p[m][p] = z;
+      const float pm = (float)sc.pmul[m];
+      v.p[m][p] = pm == 0.f ? z : v.p[m][p] * pm;
       v.e[m][c] = 0.f;
       acc[m].add_prod(z, r);
     }
@@ -70,14 +74,11 @@ __global__ void k_mx_start(Dims d, MixedVecs v, DPtr4 rv64, MixedScale sc,
   if (grid_reduce<kMaxRhs, 0>(s, mm, rb.partials, rb.ticket, out)) {
     if (lin_tid() == 0) {
       for (int m = 0; m < kMaxRhs; m++) {
-        const bool on = m < v.nrhs && sc.in_set[m] && out[m] > 0;
+        if (!(m < v.nrhs && sc.in_set[m])) continue;
         S->rz[m] = out[m];
         S->rz0[m] = out[m];
-        S->active[m] = on ? 1 : 0;
-        S->alpha[m] = 0;
-        S->beta[m] = 0;
+        S->active[m] = out[m] > 0 ? 1 : 0;
       }
-      S->iters = 0;
     }
   }
 }

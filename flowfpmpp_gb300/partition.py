@@ -83,3 +83,26 @@ def partition_frames_2d(frames, tolerance=1e-10, max_sweeps=2000000, check_inter
         phis = [np.stack([np.asfortranarray(p[r].T) for r in range(2)]) for p in phis]
         return terms, sweeps, res, phis
     return terms, sweeps, res
+
+
+def fpm_partition_terms_3d(phi, g, u, v, w, solid, xf, yf, zf, kin, shell=None, dt=1.0, nu=0.0, slip_body=False):
+    """3-D four-term partition (the 2-D scheme of src/fpm_partition_2d.f90 on
+    six faces).  Returns (terms[4], vif_density (nx,ny,nz), omega (3,nx,ny,nz))."""
+    nx, ny, nz = np.asarray(u).shape
+    f64 = np.float64
+    arrs = [_need(a, (nx, ny, nz), f64, n) for a, n in ((phi, "phi"), (u, "u"), (v, "v"), (w, "w"))]
+    s8 = np.asfortranarray(np.asarray(solid) != 0, dtype=np.uint8)
+    faces = [np.ascontiguousarray(a, dtype=f64) for a in (xf, yf, zf)]
+    gg = np.ascontiguousarray(g, dtype=f64)
+    kk = np.ascontiguousarray(kin, dtype=f64)
+    if gg.shape != (3,) or kk.shape != (12,):
+        raise ValueError("g has 3 entries and kin 12")
+    sh = None if shell is None else np.asfortranarray(shell, dtype=f64)
+    terms = np.zeros(4)
+    vif = np.empty((nx, ny, nz), order="F")
+    om = np.empty(3 * nx * ny * nz)
+    check(lib().fpm_partition_terms_3d(*[_ptr(a) for a in (arrs[0], gg, arrs[1], arrs[2], arrs[3], s8, *faces, kk)],
+                                       _ptr(sh) if sh is not None else None, _D(dt), _D(nu), _I(nx), _I(ny), _I(nz),
+                                       _ptr(terms), _ptr(vif), _ptr(om), _I(int(bool(slip_body)))))
+    omega = np.stack([om[a * nx * ny * nz:(a + 1) * nx * ny * nz].reshape((nx, ny, nz), order="F") for a in range(3)])
+    return terms, vif, omega

@@ -220,6 +220,24 @@ int fpm_partition_terms_2d(const double* phi, const double* g, const double* u, 
                            const double* ring, double dt, double nu, int nx, int ny, double* terms,
                            double* vif_density, double* omega, int slip_body);
 
+/* ---- 3-D four-term partition ---------------------------------------------
+ * The divergence-form force partition of fpm_partition_terms_2d
+ * (src/fpm_partition_2d.f90:35-154) on the six faces of every cell of a 3-D
+ * stair-step grid (the reference provides it in 2-D only).  phi, u, v, w and
+ * solid (uint8, nonzero = solid) are (nx,ny,nz); xf(0:nx), yf(0:ny), zf(0:nz)
+ * cell faces; g[3] the body face gradient of phi; kin[12] = rigid body motion
+ * about the origin: velocity V(3), angular velocity W(3), acceleration A(3),
+ * angular acceleration Al(3) (U_B = V + W x r, a_B = A + Al x r + W x (W x r));
+ * shell (L,3,2), L = 2 ny nz + 2 nx nz + 2 nx ny: the velocity of the outer
+ * cells (west face (j,k), east, south (i,k), north, bottom (i,j), top) at
+ * t - dt and t + dt for Du/Dt on the outer boundary, or NULL for zero.
+ * Outputs terms[4] = [F_KINE, F_VIF, F_VIS, F_BOUND], vif_density (nx,ny,nz)
+ * and, unless NULL, omega (nx,ny,nz,3). */
+int fpm_partition_terms_3d(const double* phi, const double* g, const double* u, const double* v, const double* w,
+                           const uint8_t* solid, const double* xf, const double* yf, const double* zf,
+                           const double* kin, const double* shell, double dt, double nu, int nx, int ny, int nz,
+                           double* terms, double* vif_density, double* omega, int slip_body);
+
 /* ---- batched 2-D frames (examples/flapping_foil_fpm.f90:61-81 per frame) ---
  * For each of nframes independent 2-D frames (cells nx[f] x ny[f], faces
  * xf[f](0:nx), yf[f](0:ny), velocity u[f], v[f] (nx,ny), solid[f] (nx,ny)

@@ -258,3 +258,22 @@ def local_axis(gn, gcenter, gwidth, offset, n):
     center, width = np.zeros(n + 2), np.zeros(n)
     lib().orc_local_axis(I(gn), _p(_f64(gcenter)), _p(_f64(gwidth)), I(offset), I(n), _p(center), _p(width))
     return center, width
+
+
+def fpm_partition_terms_3d(phi, g, u, v, w, solid, xf, yf, zf, kin, shell, dt, nu, slip_body=False):
+    """3-D four-term partition; returns (terms[4], vif_density, omega (3,nx,ny,nz))."""
+    nx, ny, nz = u.shape
+    terms = np.zeros(4)
+    vif = np.zeros((nx, ny, nz), order="F")
+    omega = np.zeros((3, nx, ny, nz))
+    om = np.zeros(3 * nx * ny * nz)
+    s8 = np.asfortranarray(solid, dtype=np.uint8)
+    gg, kk = _f64(g), _f64(kin)
+    sh = None if shell is None else _f64(shell)
+    _check(lib().orc_fpm_partition_terms_3d(_p(phi), _p(gg), _p(u), _p(v), _p(w), _p(s8), _p(_f64(xf)), _p(_f64(yf)),
+                                            _p(_f64(zf)), _p(kk), _p(sh) if sh is not None else None, D(dt), D(nu),
+                                            I(nx), I(ny), I(nz), _p(terms), _p(vif),
+                                            om.ctypes.data_as(ctypes.c_void_p), I(int(bool(slip_body)))))
+    for a in range(3):
+        omega[a] = om[a * nx * ny * nz:(a + 1) * nx * ny * nz].reshape((nx, ny, nz), order="F")
+    return terms, vif, omega

@@ -1046,3 +1046,131 @@ void orc_local_axis(int gn, const double *gcenter, const double *gwidth, int off
     }
     for (int m = 1; m <= n; m++) width[m - 1] = gwidth[offset + m - 1];
 }
+
+/* ---------------- 3-D four-term partition ----------------
+ * The 3-D counterpart of fpm_partition_terms_2d (src/fpm_partition_2d.f90:35-154),
+ * which the reference provides in 2-D only: the same face-flux discretisation
+ * on the six faces of every fluid cell.  Rigid body motion about the origin:
+ * U_B = V + W x r, a_B = A + Al x r + W x (W x r), (U_B.grad)U_B = W x U_B,
+ * kin = [V(3), W(3), A(3), Al(3)].  Outer faces: the cell's own u and
+ * (u.grad)u, zero viscous flux, Du/Dt from shell(t+dt) - shell(t-dt) over 2 dt
+ * plus (u.grad)u.  shell(L,3,2), L = 2 ny nz + 2 nx nz + 2 nx ny, lists the
+ * outer cells of the west face (j,k), east, south (i,k), north, bottom (i,j),
+ * top; NULL means Du/Dt = 0 there.  Faces f = 1..6: east, west, north, south,
+ * top, bottom (outward sign +, -, +, -, +, -).  terms = [KINE, VIF, VIS, BOUND]. */
+int orc_fpm_partition_terms_3d(const double *phi, const double *g, const double *u, const double *v,
+                               const double *w, const uint8_t *solid, const double *xf, const double *yf,
+                               const double *zf, const double *kin, const double *shell, double dt, double nu,
+                               int nx, int ny, int nz, double *terms, double *vif_density, double *omega, int slip) {
+#define C3(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * (size_t)((k) - 1)))
+    size_t n3 = (size_t)nx * ny * nz;
+    size_t L = 2 * (size_t)ny * nz + 2 * (size_t)nx * nz + 2 * (size_t)nx * ny;
+    double *N[3], *gp[3];
+    for (int a = 0; a < 3; a++) {
+        N[a] = (double *)calloc(n3, sizeof(double));
+        gp[a] = (double *)calloc(n3, sizeof(double));
+        if (!N[a] || !gp[a]) return ORC_E_ALLOC;
+    }
+    const double *vel[3] = {u, v, w};
+    terms[0] = terms[1] = terms[2] = terms[3] = 0;
+    for (size_t m = 0; m < n3; m++) {
+        vif_density[m] = 0;
+        if (omega) omega[m] = omega[n3 + m] = omega[2 * n3 + m] = 0;
+    }
+    const double V0 = kin[0], V1 = kin[1], V2 = kin[2], W0 = kin[3], W1 = kin[4], W2 = kin[5];
+    const double A0 = kin[6], A1 = kin[7], A2 = kin[8], B0 = kin[9], B1 = kin[10], B2 = kin[11];
+    for (int pass = 1; pass <= 2; pass++)
+        for (int k = 1; k <= nz; k++)
+            for (int j = 1; j <= ny; j++)
+                for (int i = 1; i <= nx; i++) {
+                    size_t c = C3(i, j, k);
+                    if (solid[c]) continue;
+                    double dxi = xf[i] - xf[i - 1], dyj = yf[j] - yf[j - 1], dzk = zf[k] - zf[k - 1];
+                    double xc = 0.5 * (xf[i - 1] + xf[i]), yc = 0.5 * (yf[j - 1] + yf[j]), zc = 0.5 * (zf[k - 1] + zf[k]);
+                    double fvel[3][6], fp[6], div = 0, lap[3] = {0, 0, 0};
+                    for (int f = 1; f <= 6; f++) {
+                        int ii = i, jj = j, kk = k, axis;
+                        double sgn = (f % 2 == 1) ? 1.0 : -1.0, hw, area, d, fx = xc, fy = yc, fz = zc;
+                        if (f <= 2) {
+                            axis = 0; ii = i + (int)sgn; hw = 0.5 * dxi; area = dyj * dzk; fx = xc + sgn * hw; d = hw;
+                            if (ii >= 1 && ii <= nx) d = fabs(0.5 * (xf[ii - 1] + xf[ii]) - xc);
+                        } else if (f <= 4) {
+                            axis = 1; jj = j + (int)sgn; hw = 0.5 * dyj; area = dxi * dzk; fy = yc + sgn * hw; d = hw;
+                            if (jj >= 1 && jj <= ny) d = fabs(0.5 * (yf[jj - 1] + yf[jj]) - yc);
+                        } else {
+                            axis = 2; kk = k + (int)sgn; hw = 0.5 * dzk; area = dxi * dyj; fz = zc + sgn * hw; d = hw;
+                            if (kk >= 1 && kk <= nz) d = fabs(0.5 * (zf[kk - 1] + zf[kk]) - zc);
+                        }
+                        int outer = ii < 1 || ii > nx || jj < 1 || jj > ny || kk < 1 || kk > nz;
+                        size_t c2 = outer ? c : C3(ii, jj, kk);
+                        /* rigid body velocity and acceleration at the face centre */
+                        double ub[3] = {V0 + (W1 * fz - W2 * fy), V1 + (W2 * fx - W0 * fz), V2 + (W0 * fy - W1 * fx)};
+                        if (pass == 1) {
+                            if (outer) {
+                                for (int a = 0; a < 3; a++) fvel[a][f - 1] = vel[a][c];
+                                fp[f - 1] = 0;
+                            } else if (solid[c2]) {
+                                for (int a = 0; a < 3; a++) fvel[a][f - 1] = slip ? vel[a][c] : ub[a];
+                                fp[f - 1] = g[axis];
+                            } else {
+                                for (int a = 0; a < 3; a++) fvel[a][f - 1] = vel[a][c] + (vel[a][c2] - vel[a][c]) * hw / d;
+                                fp[f - 1] = sgn * (phi[c2] - phi[c]) / d;
+                            }
+                        } else {
+                            if (outer) {
+                                div = div + sgn * N[axis][c] * area;
+                                double dudt = 0;
+                                if (shell) {
+                                    size_t m;
+                                    if (f == 2) m = (size_t)(j - 1) + (size_t)ny * (k - 1);
+                                    else if (f == 1) m = (size_t)ny * nz + (size_t)(j - 1) + (size_t)ny * (k - 1);
+                                    else if (f == 4) m = 2 * (size_t)ny * nz + (size_t)(i - 1) + (size_t)nx * (k - 1);
+                                    else if (f == 3) m = 2 * (size_t)ny * nz + (size_t)nx * nz + (size_t)(i - 1) + (size_t)nx * (k - 1);
+                                    else if (f == 6) m = 2 * (size_t)ny * nz + 2 * (size_t)nx * nz + (size_t)(i - 1) + (size_t)nx * (j - 1);
+                                    else m = 2 * (size_t)ny * nz + 2 * (size_t)nx * nz + (size_t)nx * ny + (size_t)(i - 1) + (size_t)nx * (j - 1);
+                                    dudt = (shell[m + L * ((size_t)axis + 3)] - shell[m + L * (size_t)axis]) / (2 * dt);
+                                }
+                                terms[3] = terms[3] - sgn * (dudt + N[axis][c]) * phi[c] * area;
+                            } else if (solid[c2]) {
+                                double rx = fx, ry = fy, rz = fz;
+                                double wr[3] = {W1 * rz - W2 * ry, W2 * rx - W0 * rz, W0 * ry - W1 * rx};
+                                double ab[3] = {A0 + (B1 * rz - B2 * ry) + (W1 * wr[2] - W2 * wr[1]),
+                                                A1 + (B2 * rx - B0 * rz) + (W2 * wr[0] - W0 * wr[2]),
+                                                A2 + (B0 * ry - B1 * rx) + (W0 * wr[1] - W1 * wr[0])};
+                                double phif = phi[c] + sgn * hw * g[axis];
+                                terms[0] = terms[0] - sgn * ab[axis] * phif * area;
+                                if (slip) {
+                                    div = div + sgn * N[axis][c] * area;
+                                } else {
+                                    double cb[3] = {W1 * ub[2] - W2 * ub[1], W2 * ub[0] - W0 * ub[2], W0 * ub[1] - W1 * ub[0]};
+                                    div = div + sgn * cb[axis] * area;
+                                    for (int a = 0; a < 3; a++) lap[a] = lap[a] + (ub[a] - vel[a][c]) / hw * area;
+                                }
+                            } else {
+                                div = div + sgn * (N[axis][c] + (N[axis][c2] - N[axis][c]) * hw / d) * area;
+                                for (int a = 0; a < 3; a++) lap[a] = lap[a] + (vel[a][c2] - vel[a][c]) / d * area;
+                            }
+                        }
+                    }
+                    if (pass == 1) {
+                        for (int a = 0; a < 3; a++)
+                            N[a][c] = u[c] * (fvel[a][0] - fvel[a][1]) / dxi + v[c] * (fvel[a][2] - fvel[a][3]) / dyj +
+                                      w[c] * (fvel[a][4] - fvel[a][5]) / dzk;
+                        if (omega) {
+                            omega[c] = (fvel[2][2] - fvel[2][3]) / dyj - (fvel[1][4] - fvel[1][5]) / dzk;
+                            omega[n3 + c] = (fvel[0][4] - fvel[0][5]) / dzk - (fvel[2][0] - fvel[2][1]) / dxi;
+                            omega[2 * n3 + c] = (fvel[1][0] - fvel[1][1]) / dxi - (fvel[0][2] - fvel[0][3]) / dyj;
+                        }
+                        gp[0][c] = 0.5 * (fp[0] + fp[1]);
+                        gp[1][c] = 0.5 * (fp[2] + fp[3]);
+                        gp[2][c] = 0.5 * (fp[4] + fp[5]);
+                    } else {
+                        vif_density[c] = phi[c] * div / (dxi * dyj * dzk);
+                        terms[1] = terms[1] + phi[c] * div;
+                        terms[2] = terms[2] + nu * (lap[0] * gp[0][c] + lap[1] * gp[1][c] + lap[2] * gp[2][c]);
+                    }
+                }
+    for (int a = 0; a < 3; a++) { free(N[a]); free(gp[a]); }
+    return ORC_OK;
+#undef C3
+}

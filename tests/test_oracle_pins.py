@@ -185,3 +185,43 @@ def test_partition_2d_known_answers():
     cm = -terms[0] / (math.pi * radius ** 2)
     assert abs(cm - 1) < 0.2 and np.all(terms[1:] == 0)
     assert f"{cm:.2f}" == "1.14"
+
+
+def test_partition_3d_known_answers():
+    """3-D four-term partition (the 2-D reference scheme on six faces):
+    solid-body rotation gives div[(u.grad)u] = -2 W^2 and omega_z = 2W inside,
+    uniform flow gives exactly zero, and an accelerating sphere's -F_KINE / V
+    equals the sphere test's added-mass coefficient (README.md:127-132,
+    0.639 at N = 48)."""
+    n, w0 = 24, 0.7
+    xf = np.linspace(-1.5, 1.5, n + 1)
+    c = 0.5 * (xf[:-1] + xf[1:])
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    solid = np.zeros((n, n, n), dtype=np.uint8, order="F")
+    kin = np.zeros(12)
+    zero = np.zeros((n, n, n), order="F")
+    u, v = np.asfortranarray(-w0 * Y), np.asfortranarray(w0 * X)
+    terms, dens, om = orc.fpm_partition_terms_3d(np.ones((n, n, n), order="F"), [1.0, 0, 0], u, v, zero, solid, xf,
+                                                 xf, xf, kin, None, 1.0, 1e-3)
+    inner = (slice(2, n - 2),) * 3
+    assert np.abs(dens[inner] + 2 * w0 ** 2).max() < 1e-10
+    assert np.abs(om[2][inner] - 2 * w0).max() < 1e-10 and np.abs(om[0][inner]).max() < 1e-12
+    ones = np.ones((n, n, n), order="F")
+    terms, _, _ = orc.fpm_partition_terms_3d(np.asfortranarray(X - Y + 0.3 * Z), [1.0, 0, 0], ones, zero, zero, solid,
+                                             xf, xf, xf, kin, None, 1.0, 1e-3)
+    assert np.all(terms == 0)
+    # accelerating sphere: the N = 48 sphere case of the convergence table
+    sc = sphere_case(48)
+    out = run_stairstep(sc, "pcg", 1e-10, 2000000, ci=100)
+    _, _, cm_ref = sphere_errors(sc, out["phi"])
+    m = 48
+    p3 = np.asfortranarray(out["phi"][1:m + 1, 1:m + 1, :])
+    s3 = np.asfortranarray((sc["solid"][1:m + 1, 1:m + 1, :] != 0).astype(np.uint8))
+    fz = np.linspace(-1.5, 1.5, m + 1)
+    z3 = np.zeros((m, m, m), order="F")
+    kin = np.zeros(12)
+    kin[6] = 1.0  # body acceleration (1, 0, 0)
+    terms, _, _ = orc.fpm_partition_terms_3d(p3, [1.0, 0, 0], z3, z3, z3, s3, fz, fz, fz, kin, None, 1.0, 1e-3)
+    cm = -terms[0] / (4 * math.pi * 0.5 ** 3 / 3)
+    assert abs(cm - cm_ref) < 1e-12 and round(cm, 3) == pytest.approx(0.639, abs=1e-12)
+    assert np.all(terms[1:] == 0)
