@@ -168,13 +168,17 @@ struct TimedRun {
 // FPM_VERBOSE=1 prints one line per convergence check of every solver loop
 // to stderr.  FPM_PCG_STALL_CHECKS overrides the number of checks without a
 // 1% improvement after which PCG stops (50, src/fpm_stairstep_mpi_3d.f90:288).
-static bool verbose() {
+static int verbose_level() {
   static int v = -1;
   if (v < 0) {
     const char* e = std::getenv("FPM_VERBOSE");
-    v = (e && e[0] && e[0] != '0') ? 1 : 0;
+    v = (e && e[0]) ? std::atoi(e) : 0;
+    if (v < 0) v = 0;
   }
-  return v == 1;
+  return v;
+}
+static bool verbose() {
+  return verbose_level() >= 1;
 }
 static int stall_checks() {
   const char* e = std::getenv("FPM_PCG_STALL_CHECKS");
@@ -429,51 +433,94 @@ static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src,
 // residual at each update, exactly the reference's test; a right-hand side
 // also stops after kStallUpdates updates without a 1% improvement (the
 // reference's roundoff-floor rule, counted in updates).
+// An update whose true residual is not below kUpdateGain times the previous
+// one restarts the direction (p = rdiag r) instead of keeping it, and every
+// right-hand side finishes on its best iterate.
 constexpr double kUpdateDrop = 1e-3;
+// Planes per thread in the FP32 kernels (FPM_MIXED_KCHUNK overrides).
+static int mixed_kchunk() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("FPM_MIXED_KCHUNK");
+    v = (e && std::atoi(e) > 0) ? std::atoi(e) : 8;
+  }
+  return v;
+}
+constexpr double kUpdateGain = 0.5;
+constexpr double kBlowup = 4.0;
 constexpr int kUpdateMax = 1000;
 constexpr int kStallUpdates = 4;
 
 static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
                         const double* rdiag, const double* coef64, const Axes& ax, const Coefs& c, double tol,
                         int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st) {
-  const long long nc = d.ncell(), np = d.npad(), ncoef = 2LL * (d.nx + d.ny + d.nz);
+  const long long np = d.npad();
+  const MixedGrid G = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk());
   MixedVecs v;
   std::memset(&v, 0, sizeof(v));
   v.nrhs = nrhs;
-  float* diag32 = A.get<float>(nc);
-  float* rdiag32 = A.get<float>(nc);
-  float* coef32 = A.get<float>(ncoef);
-  float* dx32 = A.get<float>(d.nx);
-  float* dy32 = A.get<float>(d.ny);
-  float* dz32 = A.get<float>(d.nz);
-  CUDA_TRY(launch_mx_convert(diag, diag32, nc, st));
-  CUDA_TRY(launch_mx_convert(rdiag, rdiag32, nc, st));
-  CUDA_TRY(launch_mx_convert(coef64, coef32, ncoef, st));
-  CUDA_TRY(launch_mx_convert(ax.dx, dx32, d.nx, st));
-  CUDA_TRY(launch_mx_convert(ax.dy, dy32, d.ny, st));
-  CUDA_TRY(launch_mx_convert(ax.dz, dz32, d.nz, st));
+  auto vec = [&]() {
+    float* x = A.get<float>(G.size);
+    CUDA_TRY(cudaMemsetAsync(x, 0, G.size * sizeof(float), st));
+    return x;
+  };
+  float* diag32 = vec();
+  float* rdiag32 = vec();
+  CUDA_TRY(launch_mx_layout(G, diag, diag32, st));
+  CUDA_TRY(launch_mx_layout(G, rdiag, rdiag32, st));
   v.diag = diag32;
   v.rdiag = rdiag32;
-  v.coef = coef32;
-  v.dx = dx32;
-  v.dy = dy32;
-  v.dz = dz32;
+  auto row = [&](const double* a) {
+    float* x = A.get<float>(G.px);
+    CUDA_TRY(launch_mx_row(d.nx, G.px, a, x, st));
+    return (const float*)x;
+  };
+  auto axis = [&](const double* a, int n) {
+    float* x = A.get<float>(n);
+    CUDA_TRY(launch_mx_convert(a, x, n, st));
+    return (const float*)x;
+  };
+  v.cw = row(c.cw);
+  v.ce = row(c.ce);
+  v.dx = row(ax.dx);
+  v.cs = axis(c.cs, d.ny);
+  v.cn = axis(c.cn, d.ny);
+  v.dy = axis(ax.dy, d.ny);
+  v.cb = axis(c.cb, d.nz);
+  v.ct = axis(c.ct, d.nz);
+  v.dz = axis(ax.dz, d.nz);
+  RedBuf rbm;
+  rbm.max_blocks = G.nblocks;
+  rbm.partials = A.get<double>((size_t)kMaxRhs * G.nblocks);
+  rbm.ticket = A.get<unsigned int>(1);
+  CUDA_TRY(cudaMemsetAsync(rbm.ticket, 0, sizeof(unsigned int), st));
   DPtr4 r64{}, phis{};
+  double* best_phi[kMaxRhs] = {};
   SolveScalars* S64[kMaxRhs] = {};
   for (int m = 0; m < nrhs; m++) {
-    v.p[m] = A.get<float>(np);
-    CUDA_TRY(cudaMemsetAsync(v.p[m], 0, np * sizeof(float), st));
-    v.q[m] = A.get<float>(nc);
-    v.r[m] = A.get<float>(nc);
-    v.e[m] = A.get<float>(nc);
-    CUDA_TRY(cudaMemsetAsync(v.e[m], 0, nc * sizeof(float), st));
-    r64.p[m] = A.get<double>(nc);
+    v.p[m] = vec();
+    v.q[m] = vec();
+    v.r[m] = vec();
+    v.e[m] = vec();
+    r64.p[m] = A.get<double>(d.ncell());
     phis.p[m] = phi[m];
+    best_phi[m] = A.get<double>(np);
+    CUDA_TRY(cudaMemcpyAsync(best_phi[m], phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
     S64[m] = A.get<SolveScalars>(1);
     CUDA_TRY(cudaMemsetAsync(S64[m], 0, sizeof(SolveScalars), st));
   }
   MixedScalars* MS = A.get<MixedScalars>(1);
-  CUDA_TRY(cudaMemsetAsync(MS, 0, sizeof(MixedScalars), st));  // tol2 = 0: the host decides the updates
+  {
+    // The FP32 iteration of a right-hand side stops itself once its
+    // preconditioned residual norm has dropped by kUpdateDrop (tol2 on the
+    // squared norm), so it never runs on into the FP32 rounding floor between
+    // two host checks.
+    MixedScalars h0;
+    std::memset(&h0, 0, sizeof(h0));
+    for (int m = 0; m < kMaxRhs; m++) h0.tol2[m] = kUpdateDrop * kUpdateDrop;
+    CUDA_TRY(cudaMemcpyAsync(MS, &h0, sizeof(MixedScalars), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
   auto true_res = [&](int m) {
     CUDA_TRY(launch_true_residual(d, phi[m], src[m], diag, rdiag, r64.p[m], nullptr, c, ax, 0, S64[m], cm.rb, st));
     return read_scalars(S64[m], st).res;
@@ -485,14 +532,14 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
     ~HostFree() { cudaFreeHost(p); }
   } hf{hms};
 
-  double res[kMaxRhs], best[kMaxRhs], scale[kMaxRhs];
+  double res[kMaxRhs], best[kMaxRhs], prev[kMaxRhs], scale[kMaxRhs];
   int stall[kMaxRhs] = {}, since[kMaxRhs] = {};
   bool live[kMaxRhs] = {};
   MixedScale sc;
   std::memset(&sc, 0, sizeof(sc));
   bool any = false;
   for (int m = 0; m < nrhs; m++) {
-    res[m] = best[m] = true_res(m);
+    res[m] = best[m] = prev[m] = true_res(m);
     live[m] = res[m] > tol && res[m] == res[m];
     scale[m] = res[m] > 0 ? 1.0 / res[m] : 1.0;
     sc.in_set[m] = live[m];
@@ -500,7 +547,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
     sc.pmul[m] = 0.0;
     any = any || live[m];
   }
-  if (any) CUDA_TRY(launch_mx_start(d, v, r64, sc, MS, cm.rb, st));
+  if (any) CUDA_TRY(launch_mx_start(G, v, r64, sc, MS, rbm, st));
   const int chunk_len = ci < 1 ? 1 : ci;
   int total = 0;
   while (any && total < max_sweeps) {
@@ -509,7 +556,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
     CUDA_TRY(cudaMemsetAsync(&MS->iters, 0, sizeof(int), st));
     {
       TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
-      for (int n = 0; n < chunk; n++) CUDA_TRY(launch_mx_iteration(d, v, MS, cm.rb, st));
+      for (int n = 0; n < chunk; n++) CUDA_TRY(launch_mx_iteration(G, v, MS, rbm, st));
     }
     CUDA_TRY(cudaMemcpyAsync(hms, MS, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
@@ -520,9 +567,9 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
     for (int m = 0; m < nrhs; m++) {
       if (!live[m]) continue;
       since[m] += chunk;
-      const bool broke = !hms->active[m];
-      if (broke || hms->rz[m] < kUpdateDrop * kUpdateDrop * hms->rz0[m] || since[m] >= kUpdateMax ||
-          total >= max_sweeps) {
+      const bool dropped = hms->rz[m] <= kUpdateDrop * kUpdateDrop * hms->rz0[m];
+      const bool broke = !hms->active[m] && !dropped;
+      if (broke || dropped || since[m] >= kUpdateMax || total >= max_sweeps) {
         sc.in_set[m] = 1;
         sc.scale[m] = scale[m];          // the scale the correction was computed in
         sc.pmul[m] = broke ? 0.0 : 1.0;  // rescaled below
@@ -530,27 +577,37 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
       }
     }
     if (!upd) continue;
-    CUDA_TRY(launch_mx_apply(d, v, phis, sc, st));
+    CUDA_TRY(launch_mx_apply(G, v, phis, sc, st));
     any = false;
     for (int m = 0; m < nrhs; m++) {
       if (sc.in_set[m]) {
         since[m] = 0;
         res[m] = true_res(m);
-        if (res[m] < 0.99 * best[m]) {
-          best[m] = res[m];
-          stall[m] = 0;
-        } else {
-          stall[m]++;
+        if (!(res[m] <= kBlowup * best[m])) {
+          // the FP32 correction made things much worse: back to the best
+          // iterate and restart the direction there
+          CUDA_TRY(cudaMemcpyAsync(phi[m], best_phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
+          res[m] = true_res(m);
+          sc.pmul[m] = 0.0;
         }
+        stall[m] = res[m] < 0.99 * best[m] ? 0 : stall[m] + 1;
+        if (res[m] < best[m]) {
+          best[m] = res[m];
+          CUDA_TRY(cudaMemcpyAsync(best_phi[m], phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
+        const bool restart = !(res[m] < kUpdateGain * prev[m]);
+        prev[m] = res[m];
         if (!(res[m] > tol) || !(res[m] == res[m]) || stall[m] >= kStallUpdates) {
           live[m] = false;
           sc.in_set[m] = 0;
+          if (!(res[m] <= best[m]))  // finish on the best iterate
+            CUDA_TRY(cudaMemcpyAsync(phi[m], best_phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
           // park it: no further iterations for this right-hand side
           const int zero = 0;
           CUDA_TRY(cudaMemcpyAsync(&MS->active[m], &zero, sizeof(int), cudaMemcpyHostToDevice, st));
         } else {
           const double ns = res[m] > 0 ? 1.0 / res[m] : 1.0;
-          if (sc.pmul[m] != 0.0) sc.pmul[m] = ns / scale[m];
+          sc.pmul[m] = (sc.pmul[m] == 0.0 || restart) ? 0.0 : ns / scale[m];
           scale[m] = ns;
           sc.scale[m] = ns;
         }
@@ -562,7 +619,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
                    nrhs > 1 ? res[1] : 0.0, nrhs > 2 ? res[2] : 0.0);
     bool refresh = false;
     for (int m = 0; m < nrhs; m++) refresh = refresh || sc.in_set[m];
-    if (refresh) CUDA_TRY(launch_mx_start(d, v, r64, sc, MS, cm.rb, st));
+    if (refresh) CUDA_TRY(launch_mx_start(G, v, r64, sc, MS, rbm, st));
   }
   // Fold in any correction still pending (right-hand sides stopped by the cap).
   std::memset(&sc, 0, sizeof(sc));
@@ -573,7 +630,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
       sc.scale[m] = scale[m];
       pend = true;
     }
-  if (pend) CUDA_TRY(launch_mx_apply(d, v, phis, sc, st));
+  if (pend) CUDA_TRY(launch_mx_apply(G, v, phis, sc, st));
   for (int m = 0; m < nrhs; m++) sweeps_out[m] = total;
 }
 
@@ -584,7 +641,46 @@ static bool valid_method(int m) {
   return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED;
 }
 
-static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double* residual, cudaStream_t st) {
+// Learned initial guess for every right-hand side (see fpm_learned.cu): the
+// network's output, scaled by the A-norm projection, replaces the caller's
+// phi unless it fails to lower the max-norm residual (a fallback).
+static void learned_guess(void* net, const Dims& d, int nrhs, const SolveArgs* args, double* const src[],
+                          const double* diag, const Coefs& c, Scratch& A, Common& cm, int* fallbacks,
+                          cudaStream_t st) {
+  Trace tl("learned initial guess");
+  const long long nc = d.ncell();
+  uint8_t* fluid = A.get<uint8_t>(nc);
+  float* mx = A.get<float>(d.nx);
+  float* my = A.get<float>(d.ny);
+  float* mz = A.get<float>(d.nz);
+  float* b = A.get<float>(nc);
+  float* y = A.get<float>(nc);
+  double* sc = A.get<double>(4);
+  double* backup = A.get<double>(d.npad());
+  for (int m = 0; m < nrhs; m++) {
+    const SolveArgs& a = args[m];
+    CUDA_TRY(launch_operator_residual(d, a.phi, src[m], diag, c, cm.S, cm.rb, st));
+    const double before = read_scalars(cm.S, st).res;
+    CUDA_TRY(cudaMemcpyAsync(backup, a.phi, d.npad() * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(launch_learn_inputs(d, src[m], diag, a.ax, fluid, mx, my, mz, b, sc + 2, cm.rb, st));
+    std::string err;
+    const int rc = net::forward_into(net, d.nx, d.ny, d.nz, fluid, mx, my, mz, b, y, st, &err);
+    if (rc != FPM_OK) throw Error{rc, err};
+    CUDA_TRY(launch_learn_apply(d, y, src[m], diag, c, a.ax, a.phi, sc, cm.rb, st));
+    CUDA_TRY(launch_operator_residual(d, a.phi, src[m], diag, c, cm.S, cm.rb, st));
+    const double after = read_scalars(cm.S, st).res;
+    if (verbose()) std::fprintf(stderr, "fpm learned guess: rhs %d residual %.3e -> %.3e\n", m, before, after);
+    if (!(after < before)) {
+      CUDA_TRY(cudaMemcpyAsync(a.phi, backup, d.npad() * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (fallbacks) fallbacks[m] = 1;
+    } else if (fallbacks) {
+      fallbacks[m] = 0;
+    }
+  }
+}
+
+static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double* residual, cudaStream_t st,
+                            void* net = nullptr, int* fallbacks = nullptr) {
   const SolveArgs& a0 = args[0];
   if (!valid_method(a0.method)) throw Error{FPM_E_METHOD, "stair-step method must be pcg or jacobi"};
   if (nrhs < 1 || nrhs > kMaxRhs) throw Error{FPM_E_LIMIT, "between 1 and 4 right-hand sides per call"};
@@ -610,6 +706,7 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
   }
   if (read_scalars(cm.S, st).isolated > 0) throw Error{FPM_E_ISOLATED, "stair-step fluid cell has no fluid neighbour"};
   for (int m = 0; m < nrhs; m++) CUDA_TRY(launch_init_fields(d, args[m].solid, args[m].phi, next, st));
+  if (net) learned_guess(net, d, nrhs, args, src, diag, c, A, cm, fallbacks, st);
   {
     Trace t1("stair-step iterations");
     if (a0.method == FPM_METHOD_PCG_MIXED) {
@@ -863,41 +960,85 @@ int fpm_solve_stairstep_poisson_3d(double* phi, const double* rhs, const int32_t
   });
 }
 
+static void multi_args(int nrhs, double* const* phi, const double* const* rhs, const int32_t* solid,
+                       const double* body_grads, const double* const* faces, const double* xc, const double* yc,
+                       const double* zc, const double* dx, const double* dy, const double* dz, int nx, int ny,
+                       int nz, double tolerance, int max_sweeps, int check_interval, int method, int* sweeps,
+                       double* residual, SolveArgs* args) {
+  if (!phi || !rhs || !solid || !body_grads || !faces || !xc || !yc || !zc || !dx || !dy || !dz || !sweeps ||
+      !residual)
+    throw Error{FPM_E_ARG, "null argument"};
+  if (nrhs < 1 || nrhs > kMaxRhs) throw Error{FPM_E_LIMIT, "between 1 and 4 right-hand sides per call"};
+  for (int m = 0; m < nrhs; m++) {
+    SolveArgs& a = args[m];
+    if (!phi[m] || !rhs[m]) throw Error{FPM_E_ARG, "null phi or rhs"};
+    for (int f = 0; f < 6; f++)
+      if (!faces[6 * m + f]) throw Error{FPM_E_ARG, "null face array"};
+    a.phi = phi[m];
+    a.rhs = rhs[m];
+    a.solid = solid;
+    for (int q = 0; q < 3; q++) a.bg[q] = body_grads[3 * m + q];
+    a.f = Faces{const_cast<double*>(faces[6 * m]), const_cast<double*>(faces[6 * m + 1]),
+                const_cast<double*>(faces[6 * m + 2]), const_cast<double*>(faces[6 * m + 3]),
+                const_cast<double*>(faces[6 * m + 4]), const_cast<double*>(faces[6 * m + 5])};
+    a.ax = Axes{xc, yc, zc, dx, dy, dz};
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.tol = tolerance;
+    a.max_sweeps = max_sweeps;
+    a.ci = check_interval;
+    a.method = method;
+    sweeps[m] = 0;
+    residual[m] = HUGE_VAL;
+  }
+}
+
 int fpm_solve_stairstep_multi_dev(int nrhs, double* const* phi, const double* const* rhs, const int32_t* solid,
                                   const double* body_grads, const double* const* faces, const double* xc,
                                   const double* yc, const double* zc, const double* dx, const double* dy,
                                   const double* dz, int nx, int ny, int nz, double tolerance, int max_sweeps,
                                   int check_interval, int method, int* sweeps, double* residual, void* stream) {
   return guarded([&] {
-    if (!phi || !rhs || !solid || !body_grads || !faces || !xc || !yc || !zc || !dx || !dy || !dz || !sweeps ||
-        !residual)
-      throw Error{FPM_E_ARG, "null argument"};
-    if (nrhs < 1 || nrhs > kMaxRhs) throw Error{FPM_E_LIMIT, "between 1 and 4 right-hand sides per call"};
     SolveArgs args[kMaxRhs];
-    for (int m = 0; m < nrhs; m++) {
-      SolveArgs& a = args[m];
-      if (!phi[m] || !rhs[m]) throw Error{FPM_E_ARG, "null phi or rhs"};
-      for (int f = 0; f < 6; f++)
-        if (!faces[6 * m + f]) throw Error{FPM_E_ARG, "null face array"};
-      a.phi = phi[m];
-      a.rhs = rhs[m];
-      a.solid = solid;
-      for (int q = 0; q < 3; q++) a.bg[q] = body_grads[3 * m + q];
-      a.f = Faces{const_cast<double*>(faces[6 * m]), const_cast<double*>(faces[6 * m + 1]),
-                  const_cast<double*>(faces[6 * m + 2]), const_cast<double*>(faces[6 * m + 3]),
-                  const_cast<double*>(faces[6 * m + 4]), const_cast<double*>(faces[6 * m + 5])};
-      a.ax = Axes{xc, yc, zc, dx, dy, dz};
-      a.nx = nx;
-      a.ny = ny;
-      a.nz = nz;
-      a.tol = tolerance;
-      a.max_sweeps = max_sweeps;
-      a.ci = check_interval;
-      a.method = method;
-      sweeps[m] = 0;
-      residual[m] = HUGE_VAL;
-    }
+    multi_args(nrhs, phi, rhs, solid, body_grads, faces, xc, yc, zc, dx, dy, dz, nx, ny, nz, tolerance, max_sweeps,
+               check_interval, method, sweeps, residual, args);
     solve_multi_dev(nrhs, args, sweeps, residual, (cudaStream_t)stream);
+  });
+}
+
+int fpm_solve_stairstep_learned_dev(void* net, int nrhs, double* const* phi, const double* const* rhs,
+                                    const int32_t* solid, const double* body_grads, const double* const* faces,
+                                    const double* xc, const double* yc, const double* zc, const double* dx,
+                                    const double* dy, const double* dz, int nx, int ny, int nz, double tolerance,
+                                    int max_sweeps, int check_interval, int method, int* sweeps, double* residual,
+                                    int* fallbacks, void* stream) {
+  return guarded([&] {
+    if (!net) throw Error{FPM_E_ARG, "null network handle"};
+    SolveArgs args[kMaxRhs];
+    multi_args(nrhs, phi, rhs, solid, body_grads, faces, xc, yc, zc, dx, dy, dz, nx, ny, nz, tolerance, max_sweeps,
+               check_interval, method, sweeps, residual, args);
+    if (fallbacks)
+      for (int m = 0; m < nrhs; m++) fallbacks[m] = 0;
+    solve_multi_dev(nrhs, args, sweeps, residual, (cudaStream_t)stream, net, fallbacks);
+  });
+}
+
+int fpm_net_prepare_inputs_dev(const double* src, const double* diag, const double* dx, const double* dy,
+                               const double* dz, int nx, int ny, int nz, uint8_t* fluid, float* mx, float* my,
+                               float* mz, float* b, void* stream) {
+  return guarded([&] {
+    if (!src || !diag || !dx || !dy || !dz || !fluid || !mx || !my || !mz || !b) throw Error{FPM_E_ARG, "null argument"};
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = (cudaStream_t)stream;
+    const Dims d{nx, ny, nz};
+    Scratch A(st);
+    Common cm = make_common(A, d, st);
+    double* bmax = A.get<double>(1);
+    Axes ax{nullptr, nullptr, nullptr, dx, dy, dz};
+    CUDA_TRY(launch_learn_inputs(d, src, diag, ax, fluid, mx, my, mz, b, bmax, cm.rb, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
   });
 }
 
@@ -1470,6 +1611,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       b.src[r] = A.get<double>(nint);
       b.phi[r] = A.get<double>(npad);
       CUDA_TRY(cudaMemsetAsync(b.phi[r], 0, npad * sizeof(double), st));
+      b.phi_best[r] = A.get<double>(npad);
+      CUDA_TRY(cudaMemsetAsync(b.phi_best[r], 0, npad * sizeof(double), st));
       b.r64[r] = A.get<double>(nint);
       b.r32[r] = A.get<float>(nint);
       b.p32[r] = A.get<float>(npad);
@@ -1502,8 +1645,9 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     b.iters = A.get<int>(nq);
     CUDA_TRY(cudaMemsetAsync(b.iters, 0, nq * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(b.active, 0, nq * sizeof(int), st));
-    b.tol2 = 0.0;  // the host decides the residual replacements
+    b.tol2 = kUpdateDrop * kUpdateDrop;  // each (frame, direction) stops its FP32 iteration at the update drop
     b.pmul = A.get<double>(nq);
+    b.keep = A.get<int>(nq);
     b.partials = A.get<double>(8 * (size_t)ntiles);
     b.tickets = A.get<unsigned int>(nframes);
     CUDA_TRY(cudaMemsetAsync(b.tickets, 0, nframes * sizeof(unsigned int), st));
@@ -1531,8 +1675,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     // Reliable updates per (frame, direction), as in mixed_solve.
     const int chunk_len = check_interval < 1 ? 1 : check_interval;
     long long total = 0;
-    std::vector<double> best(res), pmul(nq, 0.0), rz(nq), rz0(nq);
-    std::vector<int> live(nq), since(nq, 0);
+    std::vector<double> best(res), prev(res), pmul(nq, 0.0), rz(nq), rz0(nq);
+    std::vector<int> live(nq), since(nq, 0), keepv(nq, 0);
     bool any = false;
     for (size_t q = 0; q < nq; q++) {
       live[q] = res[q] > tolerance && res[q] == res[q];
@@ -1563,8 +1707,9 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         set[q] = 0;
         if (!live[q]) continue;
         since[q] += chunk;
-        const bool broke = !act[q];
-        if (broke || rz[q] < kUpdateDrop * kUpdateDrop * rz0[q] || since[q] >= kUpdateMax || total >= max_sweeps) {
+        const bool dropped = rz[q] <= kUpdateDrop * kUpdateDrop * rz0[q];
+        const bool broke = !act[q] && !dropped;
+        if (broke || dropped || since[q] >= kUpdateMax || total >= max_sweeps) {
           set[q] = 1;
           pmul[q] = broke ? 0.0 : 1.0;
           upd = true;
@@ -1575,27 +1720,58 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
       CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
       pull(res.data(), b.res, nq * sizeof(double));
+      {
+        // corrections that made things much worse: back to the best iterate,
+        // restart the direction there
+        bool back = false;
+        for (size_t q = 0; q < nq; q++) {
+          keepv[q] = 0;
+          if (set[q] && !(res[q] <= kBlowup * best[q])) {
+            keepv[q] = 2;
+            pmul[q] = 0.0;
+            back = true;
+          }
+        }
+        if (back) {
+          CUDA_TRY(cudaMemcpyAsync(b.keep, keepv.data(), nq * sizeof(int), cudaMemcpyHostToDevice, st));
+          CUDA_TRY(launch_k_b2_keep(dfr, dtf, ntiles, b, st));
+          CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
+          pull(res.data(), b.res, nq * sizeof(double));
+        }
+      }
       any = false;
+      bool keep_any = false;
       for (size_t q = 0; q < nq; q++) {
+        keepv[q] = 0;
         if (set[q]) {
           since[q] = 0;
-          if (res[q] < 0.99 * best[q]) {
+          stall[q] = res[q] < 0.99 * best[q] ? 0 : stall[q] + 1;
+          if (res[q] < best[q]) {
             best[q] = res[q];
-            stall[q] = 0;
-          } else {
-            stall[q]++;
+            keepv[q] = 1;
           }
+          const bool restart = !(res[q] < kUpdateGain * prev[q]);
+          if (verbose_level() >= 2)
+            std::fprintf(stderr, "fpm frames: q %zu iterations %lld residual %.3e previous %.3e %s%s\n", q, total,
+                         res[q], prev[q], act[q] ? "" : "breakdown ", restart ? "restart" : "keep");
+          prev[q] = res[q];
           if (!(res[q] > tolerance) || !(res[q] == res[q]) || stall[q] >= kStallUpdates) {
             live[q] = 0;
             set[q] = 0;
             act[q] = 0;
+            if (!(res[q] <= best[q])) keepv[q] = 2;  // finish on the best iterate
           } else {
             const double ns = res[q] > 0 ? 1.0 / res[q] : 1.0;
-            if (pmul[q] != 0.0) pmul[q] = ns / scale[q];
+            pmul[q] = (pmul[q] == 0.0 || restart) ? 0.0 : ns / scale[q];
             scale[q] = ns;
           }
+          keep_any = keep_any || keepv[q] != 0;
         }
         any = any || live[q];
+      }
+      if (keep_any) {
+        CUDA_TRY(cudaMemcpyAsync(b.keep, keepv.data(), nq * sizeof(int), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_k_b2_keep(dfr, dtf, ntiles, b, st));
       }
       CUDA_TRY(cudaMemcpyAsync(b.active, act.data(), nq * sizeof(int), cudaMemcpyHostToDevice, st));
       bool refresh = false;

@@ -434,6 +434,22 @@ __global__ void k_b2_apply(const Frame2* __restrict__ fr, const int* __restrict_
   }
 }
 
+// Best-iterate bookkeeping: copy phi to phi_best (keep = 1) or back (keep = 2).
+__global__ void k_b2_keep(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
+  const TileRef t = tile_ref(fr, tile_frame);
+  if (!t.live) return;
+  const Frame2& F = fr[t.f];
+  for (int r = 0; r < kR; r++) {
+    const int cmd = b.keep[t.f * kR + r];
+    if (cmd == 0) continue;
+    for (int k = 1; k <= 2; k++) {
+      const long long p = ph(F, t.i, t.j, k);
+      if (cmd == 1) b.phi_best[r][p] = b.phi[r][p];
+      else b.phi[r][p] = b.phi_best[r][p];
+    }
+  }
+}
+
 // ---------------------------------------------------------------- gauge
 // src/fpm_stairstep_mpi_3d.f90:170-185 per frame and direction.
 __global__ void k_b2_gauge_sum(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
@@ -633,6 +649,7 @@ B2_LAUNCH(k_b2_build)
 B2_LAUNCH(k_b2_tres)
 B2_LAUNCH(k_b2_start)
 B2_LAUNCH(k_b2_apply)
+B2_LAUNCH(k_b2_keep)
 B2_LAUNCH(k_b2_gauge_sum)
 B2_LAUNCH(k_b2_gauge_sub)
 B2_LAUNCH(k_b2_part1)

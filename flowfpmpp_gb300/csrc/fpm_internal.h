@@ -108,9 +108,20 @@ cudaError_t jacobi_df_unpack(const JacobiDfPlan& pl, const float2* cur, double* 
 
 // Mixed-precision multi-right-hand-side PCG (fpm_pcg_mixed.cu).
 constexpr int kMaxRhs = 4;
+// FP32 vector layout: cell (i, j, k), i in [0, nx+1], j in [0, ny+1], k in
+// [1, nz], at 3 + i + px (j + (ny + 2)(k - 1)), px a multiple of 4; groups of
+// four cells along x are 16-byte aligned.
+struct MixedGrid {
+  int nx, ny, nz, px, ng, kc, nblocks;
+  long long plane, size;
+};
+MixedGrid mixed_grid(int nx, int ny, int nz, int kc);
 struct MixedVecs {
   int nrhs;
-  const float *diag, *rdiag, *coef, *dx, *dy, *dz;  // FP32 copies of the operator
+  const float *diag, *rdiag;         // FP32 operator, MixedGrid layout
+  const float *cw, *ce, *dx;         // x-axis: row layout (index 3 + i)
+  const float *cs, *cn, *dy;         // y-axis: index j - 1
+  const float *cb, *ct, *dz;         // z-axis: index k - 1
   float *p[kMaxRhs], *q[kMaxRhs], *r[kMaxRhs], *e[kMaxRhs];
 };
 struct MixedScale {
@@ -127,12 +138,14 @@ struct MixedScalars {
 struct DPtr4 {
   double* p[kMaxRhs];
 };
+cudaError_t launch_mx_layout(const MixedGrid& G, const double* a, float* b, cudaStream_t st);
+cudaError_t launch_mx_row(int n, int len, const double* a, float* b, cudaStream_t st);
 cudaError_t launch_mx_convert(const double* a, float* b, long long n, cudaStream_t st);
-cudaError_t launch_mx_start(const Dims& d, const MixedVecs& v, const DPtr4& rv64, const MixedScale& sc,
+cudaError_t launch_mx_start(const MixedGrid& G, const MixedVecs& v, const DPtr4& rv64, const MixedScale& sc,
                             MixedScalars* S, const RedBuf& rb, cudaStream_t st);
-cudaError_t launch_mx_iteration(const Dims& d, const MixedVecs& v, MixedScalars* S, const RedBuf& rb,
+cudaError_t launch_mx_iteration(const MixedGrid& G, const MixedVecs& v, MixedScalars* S, const RedBuf& rb,
                                 cudaStream_t st);
-cudaError_t launch_mx_apply(const Dims& d, const MixedVecs& v, const DPtr4& phi, const MixedScale& sc,
+cudaError_t launch_mx_apply(const MixedGrid& G, const MixedVecs& v, const DPtr4& phi, const MixedScale& sc,
                             cudaStream_t st);
 
 // Batched uneven 2-D frames (fpm_frames2d.cu).
@@ -154,13 +167,14 @@ struct Batch2 {
   const double *u, *v, *ring, *kin, *dt;
   double nu;
   // operator and solution (two directions)
-  double *src[2], *diag, *rdiag, *phi[2], *r64[2];
+  double *src[2], *diag, *rdiag, *phi[2], *phi_best[2], *r64[2];
   float *diag32, *rdiag32, *r32[2], *p32[2], *q32[2], *e32[2];
   // partition
   double *nxf, *nyf, *omega, *gpx[2], *gpy[2], *vif[2], *terms;
   // per (frame, direction) scalars, index 2*f + r
   double *corr, *res, *rmean, *scale, *pmul, *rz, *rz0, *alpha, *beta;
   int *in_set, *active, *iters;
+  int* keep;  // per (frame, direction): 1 = save phi as the best iterate, 2 = restore it
   double tol2;
   double* partials;       // ntiles * 8
   unsigned int* tickets;  // one per frame
@@ -173,6 +187,7 @@ B2_DECL(k_b2_build)
 B2_DECL(k_b2_tres)
 B2_DECL(k_b2_start)
 B2_DECL(k_b2_apply)
+B2_DECL(k_b2_keep)
 B2_DECL(k_b2_gauge_sum)
 B2_DECL(k_b2_gauge_sub)
 B2_DECL(k_b2_part1)
@@ -217,6 +232,19 @@ int operator_residual_noalloc(const double* phi, const double* src, const double
 
 // Host-side count of kernel launches made by this library (fpm_capi.cu).
 void note_launch();
+
+// ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
+cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,
+                                float* mx, float* my, float* mz, float* b, double* bmax, const RedBuf& rb,
+                                cudaStream_t st);
+cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src, const double* diag, const Coefs& c,
+                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st);
+namespace net {
+// Network forward pass into out (FP32, one value per cell); returns an FPM_*
+// status and fills *err on failure.
+int forward_into(void* net, int nx, int ny, int nz, const uint8_t* fluid, const float* mx, const float* my,
+                 const float* mz, const float* rhs, float* out, cudaStream_t st, std::string* err);
+}  // namespace net
 
 // ---- 3-D four-term partition (fpm_partition3d.cu) --------------------------
 struct Part3D {

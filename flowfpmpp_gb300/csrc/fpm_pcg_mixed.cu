@@ -1,16 +1,21 @@
-// Mixed-precision, multi-right-hand-side stair-step PCG.
+// Mixed-precision, multi-right-hand-side stair-step PCG: the FP32 kernels.
 //
-// Outer loop (FP64): the true residual r = V(src + sum c phi_nb - diag phi),
-// projected by its fluid mean as in true_residual
-// (src/fpm_stairstep_mpi_3d.f90:297-329), and the max-norm of L(phi)-f that
-// decides convergence exactly as the reference does.
-// Inner loop (FP32): diagonally preconditioned CG on A e = r/|res| for every
-// right-hand side at once (phi_x, phi_y, phi_z share diag, rdiag, the
-// coefficients and the cell volumes), FP32 stencil, preconditioner and
-// direction updates, dot products accumulated per thread as error-free f32
-// pairs and combined across the grid in FP64.  Each right-hand side stops its
-// inner iteration when its preconditioned residual norm drops by kInnerDrop;
-// the correction is then added to phi in FP64 and the outer loop repeats.
+// The FP64 side (true residual, projection, max-norm test, phi update) lives
+// in the solver driver; these kernels run diagonally preconditioned CG in
+// FP32 on A e = scale * r for up to four right-hand sides at once (phi_x,
+// phi_y, phi_z share diag, rdiag, the coefficients and the cell volumes).
+// Dot products are accumulated per thread as error-free f32 pairs and
+// combined across the grid in FP64.
+//
+// FP32 vectors use the layout of MixedGrid: cell (i, j, k), i in [0, nx+1],
+// j in [0, ny+1], k in [1, nz], at 3 + i + px (j + (ny+2)(k-1)) with px a
+// multiple of four, so the four cells i = 4g+1 .. 4g+4 of group g start on a
+// 16-byte boundary and move as one float4.  Halo and padding entries are zero
+// and every kernel maps zero inputs there to zero outputs, so they stay zero.
+// A thread owns one group of four cells of one (j) row and marches through a
+// chunk of kc planes in k, keeping the planes k-1 and k of the search
+// direction in registers (the stencil's z neighbours); x neighbours across
+// groups come from the adjacent lane by shuffle.
 #include "fpm_internal.h"
 
 namespace fpm {
@@ -26,51 +31,106 @@ struct F2Acc {
     e += ((s - (t - bb)) + (p - bb)) + pe;
     s = t;
   }
+  __device__ __forceinline__ void add4(const float4& a, const float4& b) {
+    add_prod(a.x, b.x);
+    add_prod(a.y, b.y);
+    add_prod(a.z, b.z);
+    add_prod(a.w, b.w);
+  }
   __device__ __forceinline__ double value() const { return (double)s + (double)e; }
 };
 
-#define MX_CELL_BEGIN                                      \
-  const int i = blockIdx.x * 32 + threadIdx.x + 1;         \
-  const int j = blockIdx.y * 8 + threadIdx.y + 1;          \
-  const bool inxy = (i <= d.nx) && (j <= d.ny);            \
-  for (int k = blockIdx.z + 1; k <= d.nz; k += gridDim.z) { \
-    if (inxy) {
-#define MX_CELL_END \
-  }                 \
-  }
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 zero4() { return make_float4(0.f, 0.f, 0.f, 0.f); }
 
+// Per-thread position: group g (cells 4g+1 .. 4g+4) of row j, planes k0..k1.
+struct MxPos {
+  int g, j, k0, k1;
+  bool live;
+  long long base;  // layout index of cell (4g+1, j, k0)
+};
+__device__ __forceinline__ MxPos mx_pos(const MixedGrid& G) {
+  MxPos t;
+  t.g = blockIdx.x * 32 + threadIdx.x;
+  t.j = blockIdx.y * 4 + threadIdx.y + 1;
+  t.live = t.g < G.ng && t.j <= G.ny;
+  t.k0 = blockIdx.z * G.kc + 1;
+  t.k1 = min(G.nz, t.k0 + G.kc - 1);
+  t.base = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (t.k0 - 1));
+  return t;
+}
+
+// FP64 operator arrays (compact (nx, ny, nz)) into the FP32 layout.
+__global__ void k_mx_layout(MixedGrid G, const double* __restrict__ a, float* __restrict__ b) {
+  const MxPos t = mx_pos(G);
+  if (!t.live) return;
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+    float4 v;
+    float* vv = &v.x;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int i = 4 * t.g + 1 + c;
+      vv[c] = i <= G.nx ? (float)a[(i - 1) + (long long)G.nx * ((t.j - 1) + (long long)G.ny * (k - 1))] : 0.f;
+    }
+    st4(b + base, v);
+  }
+}
+
+// One FP64 x-axis array a(1:n) into the row layout b(3 + i), zero elsewhere.
+__global__ void k_mx_row(int n, int len, const double* __restrict__ a, float* __restrict__ b) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < len; m += gridDim.x * blockDim.x) {
+    const int i = m - 3;
+    b[m] = (i >= 1 && i <= n) ? (float)a[i - 1] : 0.f;
+  }
+}
 __global__ void k_mx_convert(long long n, const double* __restrict__ a, float* __restrict__ b) {
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n; m += (long long)gridDim.x * blockDim.x)
     b[m] = (float)a[m];
 }
 
 // Residual replacement for the right-hand sides in the set: r = scale * rV
-// (the projected FP64 true residual), e = 0, and either a restart from the
-// steepest-descent direction p = rdiag r (pmul == 0) or the current direction
-// rescaled to the new residual scale (p *= pmul); rz = r.(rdiag r).
-__global__ void k_mx_start(Dims d, MixedVecs v, DPtr4 rv64, MixedScale sc,
-                           MixedScalars* S, RedBuf rb) {
-  double s[kMaxRhs] = {0.0, 0.0, 0.0, 0.0}, mm[1] = {0.0};
+// (the projected FP64 true residual, compact layout), e = 0, and either a
+// restart from the steepest-descent direction p = rdiag r (pmul == 0) or the
+// current direction rescaled to the new residual scale (p *= pmul);
+// rz = r.(rdiag r).
+__global__ void __launch_bounds__(128) k_mx_start(MixedGrid G, MixedVecs v, DPtr4 rv64, MixedScale sc,
+                                                  MixedScalars* S, RedBuf rb) {
   F2Acc acc[kMaxRhs];
-  MX_CELL_BEGIN
-  const long long c = d.in(i, j, k), p = d.ph(i, j, k);
-  const float rd = v.rdiag[c];
+  const MxPos t = mx_pos(G);
+  if (t.live) {
+    long long base = t.base;
+    for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+      const float4 rd = ld4(v.rdiag + base);
+      const long long c0 = (long long)G.nx * ((t.j - 1) + (long long)G.ny * (k - 1)) + 4 * t.g;
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++) {
-    if (m < v.nrhs && sc.in_set[m]) {
-      const float r = (float)(rv64.p[m][c] * sc.scale[m]);
-      const float z = rd * r;
-      v.r[m][c] = r;
-      const float pm = (float)sc.pmul[m];
-      v.p[m][p] = pm == 0.f ? z : v.p[m][p] * pm;
-      v.e[m][c] = 0.f;
-      acc[m].add_prod(z, r);
+      for (int m = 0; m < kMaxRhs; m++) {
+        if (!(m < v.nrhs && sc.in_set[m])) continue;
+        float4 r;
+        float* rr = &r.x;
+#pragma unroll
+        for (int c = 0; c < 4; c++) rr[c] = 4 * t.g + 1 + c <= G.nx ? (float)(rv64.p[m][c0 + c] * sc.scale[m]) : 0.f;
+        const float4 z = make_float4(rd.x * r.x, rd.y * r.y, rd.z * r.z, rd.w * r.w);
+        st4(v.r[m] + base, r);
+        const float pm = (float)sc.pmul[m];
+        float4 p;
+        if (pm == 0.f) {
+          p = z;
+        } else {
+          p = ld4(v.p[m] + base);
+          p = make_float4(p.x * pm, p.y * pm, p.z * pm, p.w * pm);
+        }
+        st4(v.p[m] + base, p);
+        st4(v.e[m] + base, zero4());
+        acc[m].add4(z, r);
+      }
     }
   }
-  MX_CELL_END
+  double s[kMaxRhs], mm[1] = {0.0}, out[kMaxRhs];
 #pragma unroll
   for (int m = 0; m < kMaxRhs; m++) s[m] = acc[m].value();
-  double out[kMaxRhs];
   if (grid_reduce<kMaxRhs, 0>(s, mm, rb.partials, rb.ticket, out)) {
     if (lin_tid() == 0) {
       for (int m = 0; m < kMaxRhs; m++) {
@@ -83,8 +143,11 @@ __global__ void k_mx_start(Dims d, MixedVecs v, DPtr4 rv64, MixedScale sc,
   }
 }
 
-// q = V (diag p - sum c p_nb) on diag > 0, pq = p.q, alpha = rz / pq.
-__global__ void k_mx_spmv(Dims d, MixedVecs v, MixedScalars* S, RedBuf rb) {
+// q = V (diag p - sum c p_nb) on diag > 0 (same FP32 operation order for
+// every cell: centre, west, east, south, north, bottom, top, then the volume),
+// pq = p.q, alpha = rz / pq.
+template <int NR>
+__global__ void __launch_bounds__(128, 4) k_mx_spmv(MixedGrid G, MixedVecs v, MixedScalars* S, RedBuf rb) {
   int act[kMaxRhs];
   bool any = false;
 #pragma unroll
@@ -93,41 +156,93 @@ __global__ void k_mx_spmv(Dims d, MixedVecs v, MixedScalars* S, RedBuf rb) {
     any = any || act[m];
   }
   if (!any) return;
-  double s[kMaxRhs] = {0.0, 0.0, 0.0, 0.0}, mm[1] = {0.0};
-  F2Acc acc[kMaxRhs];
-  const long long px = d.nx + 2, pl = d.plane();
-  MX_CELL_BEGIN
-  const long long c = d.in(i, j, k), p = d.ph(i, j, k);
-  const float dg = v.diag[c];
-  const float cw = v.coef[i - 1], ce = v.coef[d.nx + i - 1], cs = v.coef[2 * d.nx + j - 1],
-              cn = v.coef[2 * d.nx + d.ny + j - 1], cb = v.coef[2 * d.nx + 2 * d.ny + k - 1],
-              ct = v.coef[2 * d.nx + 2 * d.ny + d.nz + k - 1];
-  const float vol = v.dx[i - 1] * v.dy[j - 1] * v.dz[k - 1];
-  const long long pb = k > 1 ? p - pl : p, pt = k < d.nz ? p + pl : p;
+  F2Acc acc[NR];
+  const MxPos t = mx_pos(G);
+  const int lane = threadIdx.x;
+  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
+  float4 cw = zero4(), ce = zero4(), dx = zero4();
+  float cs = 0.f, cn = 0.f, dy = 0.f;
+  if (t.live) {
+    const int o = 4 * (t.g + 1);
+    cw = ld4(v.cw + o);
+    ce = ld4(v.ce + o);
+    dx = ld4(v.dx + o);
+    cs = v.cs[t.j - 1];
+    cn = v.cn[t.j - 1];
+    dy = v.dy[t.j - 1];
+  }
+  const long long px = G.px, pl = G.plane;
+  float4 pb[NR], pc[NR];
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++) {
-    if (act[m]) {
-      const float* pm = v.p[m];
-      const float pc = pm[p];
-      float q = 0.f;
-      if (dg > 0.f) {
-        float t = dg * pc;
-        t = fmaf(-cw, pm[p - 1], t);
-        t = fmaf(-ce, pm[p + 1], t);
-        t = fmaf(-cs, pm[p - px], t);
-        t = fmaf(-cn, pm[p + px], t);
-        t = fmaf(-cb, pm[pb], t);
-        t = fmaf(-ct, pm[pt], t);
-        q = vol * t;
-      }
-      v.q[m][c] = q;
-      acc[m].add_prod(pc, q);
+  for (int m = 0; m < NR; m++) {
+    pb[m] = pc[m] = zero4();
+    if (act[m] && t.live) {
+      pc[m] = ld4(v.p[m] + t.base);
+      pb[m] = t.k0 > 1 ? ld4(v.p[m] + t.base - pl) : pc[m];
     }
   }
-  MX_CELL_END
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += pl) {
+    const float cb = __ldg(v.cb + k - 1), ct = __ldg(v.ct + k - 1), dz = __ldg(v.dz + k - 1);
+    // Phase 1: every load of this plane (read-only path, no aliasing with the
+    // q stores below), so they are all in flight together.
+    float4 dg = zero4(), pt[NR], ps[NR], pn[NR];
+    float lft[NR], rgt[NR];
+    if (t.live) dg = ldg4(v.diag + base);
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++) s[m] = acc[m].value();
-  double out[kMaxRhs];
+    for (int m = 0; m < NR; m++) {
+      pt[m] = pc[m];
+      ps[m] = pn[m] = zero4();
+      lft[m] = rgt[m] = 0.f;
+      if (act[m] && t.live) {
+        const float* p = v.p[m];
+        if (k < G.nz) pt[m] = ldg4(p + base + pl);
+        ps[m] = ldg4(p + base - px);
+        pn[m] = ldg4(p + base + px);
+        if (lane == 0) lft[m] = __ldg(p + base - 1);
+        if (fetch_right) rgt[m] = __ldg(p + base + 4);
+      }
+    }
+    const float4 vol = make_float4(dx.x * dy * dz, dx.y * dy * dz, dx.z * dy * dz, dx.w * dy * dz);
+    // Phase 2: x neighbours across lanes, the stencil, stores and dots.
+#pragma unroll
+    for (int m = 0; m < NR; m++) {
+      if (!act[m]) continue;
+      float left = __shfl_up_sync(0xffffffffu, pc[m].w, 1);
+      float right = __shfl_down_sync(0xffffffffu, pc[m].x, 1);
+      if (lane == 0) left = lft[m];
+      if (fetch_right) right = rgt[m];
+      const float4 c = pc[m], b = pb[m];
+      const float pw[4] = {left, c.x, c.y, c.z}, pe[4] = {c.y, c.z, c.w, right};
+      const float pcv[4] = {c.x, c.y, c.z, c.w}, psv[4] = {ps[m].x, ps[m].y, ps[m].z, ps[m].w},
+                  pnv[4] = {pn[m].x, pn[m].y, pn[m].z, pn[m].w}, pbv[4] = {b.x, b.y, b.z, b.w},
+                  ptv[4] = {pt[m].x, pt[m].y, pt[m].z, pt[m].w}, dgv[4] = {dg.x, dg.y, dg.z, dg.w},
+                  cwv[4] = {cw.x, cw.y, cw.z, cw.w}, cev[4] = {ce.x, ce.y, ce.z, ce.w},
+                  vv[4] = {vol.x, vol.y, vol.z, vol.w};
+      float q[4];
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        float u = dgv[n] * pcv[n];
+        u = fmaf(-cwv[n], pw[n], u);
+        u = fmaf(-cev[n], pe[n], u);
+        u = fmaf(-cs, psv[n], u);
+        u = fmaf(-cn, pnv[n], u);
+        u = fmaf(-cb, pbv[n], u);
+        u = fmaf(-ct, ptv[n], u);
+        q[n] = dgv[n] > 0.f ? vv[n] * u : 0.f;
+      }
+      const float4 q4 = make_float4(q[0], q[1], q[2], q[3]);
+      if (t.live) {
+        st4(v.q[m] + base, q4);
+        acc[m].add4(c, q4);
+      }
+      pb[m] = c;
+      pc[m] = pt[m];
+    }
+  }
+  double s[kMaxRhs], mm[1] = {0.0}, out[kMaxRhs];
+#pragma unroll
+  for (int m = 0; m < kMaxRhs; m++) s[m] = m < NR ? acc[m < NR ? m : 0].value() : 0.0;
   if (grid_reduce<kMaxRhs, 0>(s, mm, rb.partials, rb.ticket, out)) {
     if (lin_tid() == 0) {
       for (int m = 0; m < kMaxRhs; m++) {
@@ -145,7 +260,8 @@ __global__ void k_mx_spmv(Dims d, MixedVecs v, MixedScalars* S, RedBuf rb) {
 }
 
 // e += alpha p; r -= alpha q; rz_new = r.(rdiag r); beta = rz_new / rz.
-__global__ void k_mx_update(Dims d, MixedVecs v, MixedScalars* S, RedBuf rb) {
+template <int NR>
+__global__ void __launch_bounds__(128) k_mx_update(MixedGrid G, MixedVecs v, MixedScalars* S, RedBuf rb) {
   int act[kMaxRhs];
   float alpha[kMaxRhs];
   bool any = false;
@@ -156,24 +272,38 @@ __global__ void k_mx_update(Dims d, MixedVecs v, MixedScalars* S, RedBuf rb) {
     any = any || act[m];
   }
   if (!any) return;
-  double s[kMaxRhs] = {0.0, 0.0, 0.0, 0.0}, mm[1] = {0.0};
-  F2Acc acc[kMaxRhs];
-  MX_CELL_BEGIN
-  const long long c = d.in(i, j, k), p = d.ph(i, j, k);
-  const float rd = v.rdiag[c];
+  F2Acc acc[NR];
+  const MxPos t = mx_pos(G);
+  if (t.live) {
+    long long base = t.base;
+    for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+      const float4 rd = ldg4(v.rdiag + base);
+      float4 pp[NR], qq[NR], ee[NR], rr[NR];
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++) {
-    if (act[m]) {
-      v.e[m][c] = fmaf(alpha[m], v.p[m][p], v.e[m][c]);
-      const float r = fmaf(-alpha[m], v.q[m][c], v.r[m][c]);
-      v.r[m][c] = r;
-      acc[m].add_prod(rd * r, r);
+      for (int m = 0; m < NR; m++) {
+        if (!act[m]) continue;
+        pp[m] = ldg4(v.p[m] + base);
+        qq[m] = ldg4(v.q[m] + base);
+        ee[m] = ld4(v.e[m] + base);
+        rr[m] = ld4(v.r[m] + base);
+      }
+#pragma unroll
+      for (int m = 0; m < NR; m++) {
+        if (!act[m]) continue;
+        const float a = alpha[m];
+        const float4 p = pp[m], q = qq[m];
+        float4 e = ee[m], r = rr[m];
+        e = make_float4(fmaf(a, p.x, e.x), fmaf(a, p.y, e.y), fmaf(a, p.z, e.z), fmaf(a, p.w, e.w));
+        r = make_float4(fmaf(-a, q.x, r.x), fmaf(-a, q.y, r.y), fmaf(-a, q.z, r.z), fmaf(-a, q.w, r.w));
+        st4(v.e[m] + base, e);
+        st4(v.r[m] + base, r);
+        acc[m].add4(make_float4(rd.x * r.x, rd.y * r.y, rd.z * r.z, rd.w * r.w), r);
+      }
     }
   }
-  MX_CELL_END
+  double s[kMaxRhs], mm[1] = {0.0}, out[kMaxRhs];
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++) s[m] = acc[m].value();
-  double out[kMaxRhs];
+  for (int m = 0; m < kMaxRhs; m++) s[m] = m < NR ? acc[m < NR ? m : 0].value() : 0.0;
   if (grid_reduce<kMaxRhs, 0>(s, mm, rb.partials, rb.ticket, out)) {
     if (lin_tid() == 0) {
       for (int m = 0; m < kMaxRhs; m++) {
@@ -192,7 +322,8 @@ __global__ void k_mx_update(Dims d, MixedVecs v, MixedScalars* S, RedBuf rb) {
 }
 
 // p = rdiag r + beta p for the right-hand sides still iterating.
-__global__ void k_mx_direction(Dims d, MixedVecs v, MixedScalars* S) {
+template <int NR>
+__global__ void __launch_bounds__(128) k_mx_direction(MixedGrid G, MixedVecs v, MixedScalars* S) {
   int act[kMaxRhs];
   float beta[kMaxRhs];
   bool any = false;
@@ -203,26 +334,77 @@ __global__ void k_mx_direction(Dims d, MixedVecs v, MixedScalars* S) {
     any = any || act[m];
   }
   if (!any) return;
-  MX_CELL_BEGIN
-  const long long c = d.in(i, j, k), p = d.ph(i, j, k);
-  const float rd = v.rdiag[c];
+  const MxPos t = mx_pos(G);
+  if (t.live) {
+    long long base = t.base;
+    for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+      const float4 rd = ldg4(v.rdiag + base);
+      float4 rr[NR], pp[NR];
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++)
-    if (act[m]) v.p[m][p] = fmaf(rd, v.r[m][c], beta[m] * v.p[m][p]);
-  MX_CELL_END
+      for (int m = 0; m < NR; m++) {
+        if (!act[m]) continue;
+        rr[m] = ldg4(v.r[m] + base);
+        pp[m] = ld4(v.p[m] + base);
+      }
+#pragma unroll
+      for (int m = 0; m < NR; m++) {
+        if (!act[m]) continue;
+        const float b = beta[m];
+        const float4 r = rr[m], p = pp[m];
+        st4(v.p[m] + base, make_float4(fmaf(rd.x, r.x, b * p.x), fmaf(rd.y, r.y, b * p.y),
+                                       fmaf(rd.z, r.z, b * p.z), fmaf(rd.w, r.w, b * p.w)));
+      }
+    }
+  }
   if (lin_bid() == 0 && lin_tid() == 0) S->iters += 1;
 }
 
-// phi += e / scale (FP64) for the right-hand sides of this outer step.
-__global__ void k_mx_apply(Dims d, MixedVecs v, DPtr4 phi, MixedScale sc) {
-  MX_CELL_BEGIN
-  const long long c = d.in(i, j, k), p = d.ph(i, j, k);
+// phi += e / scale (FP64, padded (0:nx+1, 0:ny+1, nz)) for the set.
+__global__ void __launch_bounds__(128) k_mx_apply(MixedGrid G, MixedVecs v, DPtr4 phi, MixedScale sc) {
+  const MxPos t = mx_pos(G);
+  if (!t.live) return;
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+    const long long p0 = 4LL * t.g + 1 + (long long)(G.nx + 2) * (t.j + (long long)(G.ny + 2) * (k - 1));
 #pragma unroll
-  for (int m = 0; m < kMaxRhs; m++)
-    if (m < v.nrhs && sc.in_set[m]) phi.p[m][p] += (double)v.e[m][c] / sc.scale[m];
-  MX_CELL_END
+    for (int m = 0; m < kMaxRhs; m++) {
+      if (!(m < v.nrhs && sc.in_set[m])) continue;
+      const float4 e = ld4(v.e[m] + base);
+      const float ev[4] = {e.x, e.y, e.z, e.w};
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (4 * t.g + 1 + c <= G.nx) phi.p[m][p0 + c] += (double)ev[c] / sc.scale[m];
+    }
+  }
 }
 
+static dim3 mx_grid(const MixedGrid& G) {
+  return dim3((unsigned)((G.ng + 31) / 32), (unsigned)((G.ny + 3) / 4), (unsigned)((G.nz + G.kc - 1) / G.kc));
+}
+
+MixedGrid mixed_grid(int nx, int ny, int nz, int kc) {
+  MixedGrid G;
+  G.nx = nx;
+  G.ny = ny;
+  G.nz = nz;
+  G.px = ((nx + 5) + 3) / 4 * 4;
+  G.ng = (nx + 3) / 4;
+  G.kc = kc < 1 ? 1 : kc;
+  G.plane = (long long)G.px * (ny + 2);
+  G.size = G.plane * nz + G.px;
+  const dim3 g = mx_grid(G);
+  G.nblocks = (int)(g.x * g.y * g.z);
+  return G;
+}
+
+cudaError_t launch_mx_layout(const MixedGrid& G, const double* a, float* b, cudaStream_t st) {
+  k_mx_layout<<<mx_grid(G), dim3(32, 4), 0, st>>>(G, a, b); note_launch();
+  return cudaGetLastError();
+}
+cudaError_t launch_mx_row(int n, int len, const double* a, float* b, cudaStream_t st) {
+  k_mx_row<<<(len + 255) / 256, 256, 0, st>>>(n, len, a, b); note_launch();
+  return cudaGetLastError();
+}
 cudaError_t launch_mx_convert(const double* a, float* b, long long n, cudaStream_t st) {
   long long nb = (n + 255) / 256;
   if (nb > 152LL * 32) nb = 152LL * 32;
@@ -230,24 +412,34 @@ cudaError_t launch_mx_convert(const double* a, float* b, long long n, cudaStream
   k_mx_convert<<<(unsigned)nb, 256, 0, st>>>(n, a, b); note_launch();
   return cudaGetLastError();
 }
-cudaError_t launch_mx_start(const Dims& d, const MixedVecs& v, const DPtr4& rv64, const MixedScale& sc,
+cudaError_t launch_mx_start(const MixedGrid& G, const MixedVecs& v, const DPtr4& rv64, const MixedScale& sc,
                             MixedScalars* S, const RedBuf& rb, cudaStream_t st) {
-  Launch L = cells_launch(d);
-  k_mx_start<<<L.grid, L.block, 0, st>>>(d, v, rv64, sc, S, rb); note_launch();
+  k_mx_start<<<mx_grid(G), dim3(32, 4), 0, st>>>(G, v, rv64, sc, S, rb); note_launch();
   return cudaGetLastError();
 }
-cudaError_t launch_mx_iteration(const Dims& d, const MixedVecs& v, MixedScalars* S, const RedBuf& rb,
+cudaError_t launch_mx_iteration(const MixedGrid& G, const MixedVecs& v, MixedScalars* S, const RedBuf& rb,
                                 cudaStream_t st) {
-  Launch L = cells_launch(d);
-  k_mx_spmv<<<L.grid, L.block, 0, st>>>(d, v, S, rb); note_launch();
-  k_mx_update<<<L.grid, L.block, 0, st>>>(d, v, S, rb); note_launch();
-  k_mx_direction<<<L.grid, L.block, 0, st>>>(d, v, S); note_launch();
+  const dim3 g = mx_grid(G), b(32, 4);
+  switch (v.nrhs) {
+    case 1: k_mx_spmv<1><<<g, b, 0, st>>>(G, v, S, rb); break;
+    case 2: k_mx_spmv<2><<<g, b, 0, st>>>(G, v, S, rb); break;
+    case 3: k_mx_spmv<3><<<g, b, 0, st>>>(G, v, S, rb); break;
+    default: k_mx_spmv<4><<<g, b, 0, st>>>(G, v, S, rb); break;
+  }
+  note_launch();
+  switch (v.nrhs) {
+    case 1: k_mx_update<1><<<g, b, 0, st>>>(G, v, S, rb); k_mx_direction<1><<<g, b, 0, st>>>(G, v, S); break;
+    case 2: k_mx_update<2><<<g, b, 0, st>>>(G, v, S, rb); k_mx_direction<2><<<g, b, 0, st>>>(G, v, S); break;
+    case 3: k_mx_update<3><<<g, b, 0, st>>>(G, v, S, rb); k_mx_direction<3><<<g, b, 0, st>>>(G, v, S); break;
+    default: k_mx_update<4><<<g, b, 0, st>>>(G, v, S, rb); k_mx_direction<4><<<g, b, 0, st>>>(G, v, S); break;
+  }
+  note_launch();
+  note_launch();
   return cudaGetLastError();
 }
-cudaError_t launch_mx_apply(const Dims& d, const MixedVecs& v, const DPtr4& phi, const MixedScale& sc,
+cudaError_t launch_mx_apply(const MixedGrid& G, const MixedVecs& v, const DPtr4& phi, const MixedScale& sc,
                             cudaStream_t st) {
-  Launch L = cells_launch(d);
-  k_mx_apply<<<L.grid, L.block, 0, st>>>(d, v, phi, sc); note_launch();
+  k_mx_apply<<<mx_grid(G), dim3(32, 4), 0, st>>>(G, v, phi, sc); note_launch();
   return cudaGetLastError();
 }
 

@@ -11,8 +11,17 @@ Configurations (sizes in cells):
       z-tubes (core 0.2, circulation N(0,1)), acceleration = 6 Fourier modes.
   c2  256^3, ratio 1.01, four seeded axis-aligned boxes of 8-40 cells per
       side, one touching the outer boundary; phi_x right-hand side.
-  c3  384x384x192, ratio 1.02, union of 3 random ellipsoids (semi-axes
-      0.3-1.0, random orientation).
+  c3  384x384x192, ratio 1.02 from a smallest cell of 0.01 at the centre
+      planes (so [-21.8,21.8]^2 x [-2.85,2.85]), union of 3 random ellipsoids
+      (semi-axes 0.3-1.0, random orientation).
+  c4  uneven 2-D foil frames, ratio 1.02 from a smallest cell of 0.01, the
+      domain widened to at least [-4,4]^2 for small frames.
+
+The smallest cell fixes the FP64 rounding floor of the solver's convergence
+measure, max |src + sum c phi_nb - diag phi|: its terms are of size
+diag |phi| ~ 6 |phi| / w^2, so w = 0.01 puts the floor near 1e-12, below the
+1e-10 tolerance, while w = 0.0018 (384 cells of ratio 1.02 squeezed into
+[-4,4]) puts it at about 1e-10 and no FP64 solver can meet the tolerance.
 """
 from __future__ import annotations
 
@@ -38,6 +47,17 @@ def geometric_axis(n: int, lo: float, hi: float, ratio: float):
     c = 0.5 * (faces[:-1] + faces[1:])
     centres = np.concatenate([[c[0] - w[0]], c, [c[-1] + w[-1]]])
     return faces, centres, w
+
+
+def geometric_axis_w0(n: int, w0: float, ratio: float, min_half: float = 0.0):
+    """n cells symmetric about 0, the two centre cells of width w0 and widths
+    growing by `ratio` per cell outward; if that spans less than
+    [-min_half, min_half] the axis is rescaled to exactly that interval."""
+    half = n // 2
+    side = ratio ** np.arange(half) if n % 2 == 0 else ratio ** np.arange(1, half + 1)
+    extent = w0 * (2 * side.sum() + (0 if n % 2 == 0 else 1.0))
+    h = max(0.5 * extent, min_half)
+    return geometric_axis(n, -h, h, ratio)
 
 
 def _empty_faces(nx, ny, nz):
@@ -93,13 +113,14 @@ def _rotation(rng):
                      [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
 
 
-def ellipsoids_c3(nx=384, ny=384, nz=192, ratio=1.02, seed=3, count=3, axis=0):
+def ellipsoids_c3(nx=384, ny=384, nz=192, ratio=1.02, seed=3, count=3, axis=0, w0=0.01):
     """Config 3: union of `count` random ellipsoids (semi-axes 0.3-1.0, random
-    orientation, centres within 1.0 of the origin) on [-4,4]^2 x [-2,2]."""
+    orientation, centres within 1.0 of the origin, 0.5 in z) on axes of
+    smallest cell w0 (at least [-2,2] in z)."""
     rng = np.random.default_rng(seed)
-    ax = geometric_axis(nx, -4.0, 4.0, ratio)
-    ay = geometric_axis(ny, -4.0, 4.0, ratio)
-    az = geometric_axis(nz, -2.0, 2.0, ratio)
+    ax = geometric_axis_w0(nx, w0, ratio, 2.0)
+    ay = geometric_axis_w0(ny, w0, ratio, 2.0)
+    az = geometric_axis_w0(nz, w0, ratio, 2.0)
     X = ax[1][1:nx + 1][:, None, None]
     Y = ay[1][1:ny + 1][None, :, None]
     Z = az[1][1:nz + 1][None, None, :]
@@ -159,10 +180,11 @@ def flow_c1(frame, seed=11, ntubes=8, core=0.2, nmodes=6):
 
 
 def foil_frames_c4(nframes=256, seed=4, nmin=96, nmax=512, ratio=1.02, half_x=4.0, half_y=4.0, nvort=12,
-                   dt=0.4, nu=1e-4):
+                   dt=0.4, nu=1e-4, w0=0.01):
     """Config 4: uneven 2-D frames in the fpm_partition_2d form.  Each frame:
     nx, ny ~ U[nmin, nmax], geometric stretching `ratio` away from the centre
-    lines; an elliptic foil (chord 1, thickness 0.12) at pitch U[-30, 30]
+    lines from a smallest cell w0, the domain at least [-half_x, half_x] x
+    [-half_y, half_y]; vortex centres lie in that box; an elliptic foil (chord 1, thickness 0.12) at pitch U[-30, 30]
     degrees and heave U[-0.5, 0.5], blocked by cell centre; rigid-body
     kinematics kin ~ N(0,1); velocity U=1 plus `nvort` Lamb-Oseen vortices
     (circulation N(0,1), core U[0.05, 0.2]); the outer ring at t -/+ dt is
@@ -171,8 +193,8 @@ def foil_frames_c4(nframes=256, seed=4, nmin=96, nmax=512, ratio=1.02, half_x=4.
     frames = []
     for _ in range(nframes):
         nx, ny = (int(v) for v in rng.integers(nmin, nmax + 1, size=2))
-        xf, xc, dx = geometric_axis(nx, -half_x, half_x, ratio)
-        yf, yc, dy = geometric_axis(ny, -half_y, half_y, ratio)
+        xf, xc, dx = geometric_axis_w0(nx, w0, ratio, half_x)
+        yf, yc, dy = geometric_axis_w0(ny, w0, ratio, half_y)
         X = xc[1:nx + 1][:, None] * np.ones((nx, ny))
         Y = yc[1:ny + 1][None, :] * np.ones((nx, ny))
         pitch = math.radians(rng.uniform(-30, 30))

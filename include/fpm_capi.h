@@ -300,6 +300,56 @@ int fpm_stairstep_operator_residual_noalloc_dev(const double* phi, const double*
                                                 const double* dx, const double* dy, const double* dz, int nx, int ny,
                                                 int nz, double* value, void* stream);
 
+/* ---- learned initial guess (no counterpart in the reference) ---------------
+ * A small 3-D convolutional encoder-decoder (4 levels, 16-64 channels, 3x3x3
+ * convolutions, BF16 tensor-core kernels with FP32 accumulation, FP32 master
+ * weights and Adam) that maps the fluid mask, the cell-size metrics and the
+ * right-hand side to an initial guess for the stair-step solve.  Grids must
+ * have nx, ny, nz multiples of 8.  All arrays of the _dev functions are
+ * device pointers in the solver's compact cell order (x fastest); stream is
+ * a cudaStream_t (NULL = legacy default stream).
+ *
+ * Parameters are exchanged as one flat FP32 array: for each of the 8 layers,
+ * its weights [27][cout][cin] (tap t = (dk+1)*9 + (dj+1)*3 + (di+1)) and then
+ * its biases [cout]. */
+int fpm_net_create(unsigned long long seed, void** net);
+int fpm_net_destroy(void* net);
+long long fpm_net_param_count(void* net);
+int fpm_net_get_params(void* net, float* host, long long n);
+int fpm_net_set_params(void* net, const float* host, long long n);
+/* Gradients of the last fpm_net_backward_dev / fpm_net_train_step_dev. */
+int fpm_net_get_grads(void* net, float* host, long long n);
+/* Network inputs of a stair-step problem from its operator (src, diag of
+ * fpm_stairstep_build_operator_dev with for_pcg = 1): fluid = diag > 0,
+ * mx = w_min / dx (w_min = smallest cell width), my, mz likewise, and
+ * b = V src / max |V src| on fluid cells (0 elsewhere). */
+int fpm_net_prepare_inputs_dev(const double* src, const double* diag, const double* dx, const double* dy,
+                               const double* dz, int nx, int ny, int nz, uint8_t* fluid, float* mx, float* my,
+                               float* mz, float* b, void* stream);
+/* out (FP32, nx*ny*nz) = network output for the inputs. */
+int fpm_net_forward_dev(void* net, int nx, int ny, int nz, const uint8_t* fluid, const float* mx, const float* my,
+                        const float* mz, const float* rhs, float* out, void* stream);
+/* Forward, loss (1 - cos^2 of the angle between output and target over fluid
+ * cells, both with their fluid mean removed) and parameter gradients; no
+ * update. */
+int fpm_net_backward_dev(void* net, int nx, int ny, int nz, const uint8_t* fluid, const float* mx, const float* my,
+                         const float* mz, const float* rhs, const float* target, double* loss, void* stream);
+/* fpm_net_backward_dev followed by one Adam step (beta 0.9 / 0.999). */
+int fpm_net_train_step_dev(void* net, int nx, int ny, int nz, const uint8_t* fluid, const float* mx,
+                           const float* my, const float* mz, const float* rhs, const float* target, float lr,
+                           double* loss, void* stream);
+/* fpm_solve_stairstep_multi_dev with the network's initial guess: for each
+ * right-hand side, phi0 = gamma * net(...) (gamma from the A-norm projection)
+ * replaces the caller's phi unless its max-norm residual is not lower, in
+ * which case the caller's phi is kept and fallbacks[m] = 1 (fallbacks may be
+ * NULL).  Any method; nx, ny, nz multiples of 8. */
+int fpm_solve_stairstep_learned_dev(void* net, int nrhs, double* const* phi, const double* const* rhs,
+                                    const int32_t* solid, const double* body_grads, const double* const* faces,
+                                    const double* xc, const double* yc, const double* zc, const double* dx,
+                                    const double* dy, const double* dz, int nx, int ny, int nz, double tolerance,
+                                    int max_sweeps, int check_interval, int method, int* sweeps, double* residual,
+                                    int* fallbacks, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
