@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["jacobi256", "pcg_c1", "pcg_c3", "frames_c4"], default="jacobi256",
+    ap.add_argument("--workload", choices=["jacobi256", "pcg_c1", "pcg_c3", "frames_c4", "learned_c5"],
+                    default="jacobi256",
                     help="jacobi256: the headline bandwidth benchmark; pcg_c1 / pcg_c3: three-potential PCG "
                          "time to 1e-10 (plain FP64 vs mixed precision)")
     return ap.parse_args()
@@ -230,33 +231,44 @@ def run_pcg(args):
     bg = np.ascontiguousarray(np.concatenate(bgs))
     stream = torch.cuda.current_stream()
 
-    def solve(method):
+    from flowfpmpp_gb300 import learned as lg
+    net = lg.LearnedGuess.load() if os.path.exists(lg.WEIGHTS) and nx % 8 == 0 and ny % 8 == 0 and nz % 8 == 0 \
+        else None
+    fallbacks = (ctypes.c_int * 3)()
+
+    def solve(method, use_net=False):
         for t in phis:
             t.zero_()
         sweeps = (ctypes.c_int * 3)()
         res = (ctypes.c_double * 3)()
-        rc = lib.fpm_solve_stairstep_multi_dev(
-            3, (VP * 3)(*[t.data_ptr() for t in phis]), (VP * 3)(*[t.data_ptr() for t in rhss]),
-            VP(dsolid.data_ptr()), bg.ctypes.data_as(VP), (VP * 18)(*[t.data_ptr() for t in faces_dev]),
-            *[VP(t.data_ptr()) for t in dax], nx, ny, nz, ctypes.c_double(1e-10), 2000000, 50, method, sweeps, res,
-            VP(stream.cuda_stream))
+        args_ = (3, (VP * 3)(*[t.data_ptr() for t in phis]), (VP * 3)(*[t.data_ptr() for t in rhss]),
+                 VP(dsolid.data_ptr()), bg.ctypes.data_as(VP), (VP * 18)(*[t.data_ptr() for t in faces_dev]),
+                 *[VP(t.data_ptr()) for t in dax], nx, ny, nz, ctypes.c_double(1e-10), 2000000, 50, method, sweeps,
+                 res)
+        if use_net:
+            rc = lib.fpm_solve_stairstep_learned_dev(net.h, *args_, fallbacks, VP(stream.cuda_stream))
+        else:
+            rc = lib.fpm_solve_stairstep_multi_dev(*args_, VP(stream.cuda_stream))
         if rc != 0:
             raise RuntimeError(lib.fpm_last_error().decode())
         return list(sweeps), list(res)
 
     out = {}
-    for method, label in ((0, "fp64"), (3, "mixed")):
+    arms = [(0, "fp64", False), (3, "mixed", False)] + ([(3, "learned_mixed", True)] if net is not None else [])
+    for method, label, use_net in arms:
         for _ in range(args.warmup):
-            solve(method)
+            solve(method, use_net)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            sw, res = solve(method)
+            sw, res = solve(method, use_net)
         e1.record(stream)
         torch.cuda.synchronize()
         out[label] = {"seconds": e0.elapsed_time(e1) / args.steps / 1e3, "iterations": sw, "residual": res,
                       "phi": [t.cpu().numpy().copy() for t in phis]}
+        if use_net:
+            out[label]["fallbacks"] = list(fallbacks)
     err = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
               for a, b in zip(out["mixed"]["phi"], out["fp64"]["phi"]))
     line = {"metric": "PCG solve time to 1e-10 max-norm residual, three potentials (mixed vs plain FP64)",
@@ -267,6 +279,54 @@ def run_pcg(args):
             "mixed": {k: v for k, v in out["mixed"].items() if k != "phi"},
             "speedup_vs_fp64": out["fp64"]["seconds"] / out["mixed"]["seconds"],
             "mixed_vs_fp64_rel_linf": err}
+    if "learned_mixed" in out:
+        lm = out["learned_mixed"]
+        line["learned_mixed"] = {k: v for k, v in lm.items() if k != "phi"}
+        line["learned_mixed"]["speedup_vs_fp64"] = out["fp64"]["seconds"] / lm["seconds"]
+        line["learned_mixed"]["vs_fp64_rel_linf"] = max(
+            float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(lm["phi"], out["fp64"]["phi"]))
+    print(json.dumps(line), flush=True)
+
+
+def run_learned(args):
+    """Config 5: the committed trained network as initial guess on unseen
+    random bodies at 256x256x128 (the training set was 128x128x64), FP64 PCG
+    to 1e-10 from phi = 0 and from the learned guess; iterations, time and
+    fallbacks over `steps` bodies (after `warmup` bodies)."""
+    import torch
+    from flowfpmpp_gb300 import build as fbuild
+    fbuild.build()
+    from flowfpmpp_gb300 import learned as lg
+    if not os.path.exists(lg.WEIGHTS):
+        raise SystemExit("no trained weights: run python -m flowfpmpp_gb300.train_learned --out " + lg.WEIGHTS)
+    net = lg.LearnedGuess.load()
+    rng = np.random.default_rng(20261)
+    ax, ay, az = lg.training_grid(256, 256, 128)
+    rows = []
+    for s_ in range(args.warmup + args.steps):
+        axis = int(rng.integers(0, 3))
+        p = lg.DeviceProblem(lg.frame_for(lg.random_bodies(rng, ax, ay, az), ax, ay, az, axis))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        _, sw0, r0, _ = p.solve("pcg", tol=1e-10)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        _, sw1, r1, fb = p.solve("pcg", tol=1e-10, net=net)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        if s_ >= args.warmup:
+            rows.append((sw0, t2 - t1, r0, sw1, t3 - t2, r1, fb))
+    a = np.array(rows, dtype=np.float64)
+    line = {"metric": "FP64 PCG solve time to 1e-10 with the learned initial guess vs from phi = 0",
+            "value": float(a[:, 4].mean()), "unit": "s per body", "higher_is_better": False, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded random bodies)",
+            "config": {"workload": "C5 unseen bodies 256x256x128, network trained on 2000 bodies at 128x128x64",
+                       "tolerance": 1e-10, "bodies": len(rows)},
+            "plain": {"seconds": float(a[:, 1].mean()), "iterations": float(a[:, 0].mean())},
+            "learned": {"seconds": float(a[:, 4].mean()), "iterations": float(a[:, 3].mean()),
+                        "fallbacks": int(a[:, 6].sum()), "max_residual": float(a[:, 5].max())},
+            "iteration_ratio": float(a[:, 0].sum() / a[:, 3].sum()),
+            "time_ratio": float(a[:, 1].sum() / a[:, 4].sum())}
     print(json.dumps(line), flush=True)
 
 
@@ -312,6 +372,10 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if args.workload == "learned_c5":
+        if rank == 0:
+            run_learned(args)
+        return
     if args.workload != "jacobi256":
         if rank == 0:
             run_frames(args) if args.workload == "frames_c4" else run_pcg(args)

@@ -27,6 +27,7 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 
 static std::atomic<long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 struct Error {
   int code;
@@ -199,6 +200,71 @@ struct SolveArgs {
   int max_sweeps, ci, method;
 };
 
+// ---------------------------------------------------------------- chunk graphs
+// The iterations between two convergence checks are replayed as one CUDA
+// graph: captured once per solve and chunk length on a private capture stream
+// (so the caller's stream may be the legacy default stream), launched on the
+// solve's stream.  The kernels read their per-iteration scalars and halt
+// flags from device memory, so a replay is exactly the sequence of launches
+// it replaces.  FPM_GRAPHS=0 launches the kernels one by one instead.
+static bool graphs_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("FPM_GRAPHS");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
+class ChunkGraphs {
+ public:
+  explicit ChunkGraphs(int kernels_per_iteration) : kpi_(kernels_per_iteration) {}
+  ~ChunkGraphs() {
+    for (auto& kv : exec_) cudaGraphExecDestroy(kv.second);
+  }
+  // Runs `launch_one(stream)` n times on st, through a cached graph.
+  template <class F>
+  void run(int n, cudaStream_t st, F&& launch_one) {
+    if (n <= 0) return;
+    if (!graphs_enabled()) {
+      for (int i = 0; i < n; i++) launch_one(st);
+      return;
+    }
+    auto it = exec_.find(n);
+    if (it == exec_.end()) {
+      cudaStream_t cs = capture_stream();
+      CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int i = 0; i < n; i++) launch_one(cs);
+      } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(cs, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      cudaGraph_t g = nullptr;
+      CUDA_TRY(cudaStreamEndCapture(cs, &g));
+      cudaGraphExec_t x = nullptr;
+      const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+      cudaGraphDestroy(g);
+      CUDA_TRY(e);
+      it = exec_.emplace(n, x).first;
+      note_launches(-(long long)n * kpi_);  // counted again below, when they run
+    }
+    CUDA_TRY(cudaGraphLaunch(it->second, st));
+    note_launches((long long)n * kpi_);
+  }
+
+ private:
+  static cudaStream_t capture_stream() {
+    static thread_local cudaStream_t cs = nullptr;
+    if (!cs) CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    return cs;
+  }
+  int kpi_;
+  std::map<int, cudaGraphExec_t> exec_;
+};
+
 // PCG with the control flow of pcg_iterate (src/fpm_stairstep_mpi_3d.f90:235-293):
 // breakdown restarts once from the steepest-descent direction, the recursive
 // residual is replaced by the true one at every check, and the iteration stops
@@ -216,14 +282,16 @@ static double pcg_loop(const SolveArgs& a, const Dims& d, double* p, const doubl
   int it = 0, restarts = 0, stalled = 0;
   double best = res;
   int sw = 0;
+  ChunkGraphs graphs(3);
   while (sw < a.max_sweeps && res > a.tol) {
     int chunk = ci - it % ci;
     if (chunk > a.max_sweeps - sw) chunk = a.max_sweeps - sw;
     CUDA_TRY(cudaMemsetAsync(&cm.S->iters, 0, sizeof(int), st));
     {
       TimedRun t(FPM_TIMER_PCG_ITER, chunk, st);
-      for (int n = 0; n < chunk; n++)
-        CUDA_TRY(launch_pcg_iteration(d, a.phi, p, q, r, diag, rdiag, c, a.ax, cm.S, cm.rb, st));
+      graphs.run(chunk, st, [&](cudaStream_t s2) {
+        CUDA_TRY(launch_pcg_iteration(d, a.phi, p, q, r, diag, rdiag, c, a.ax, cm.S, cm.rb, s2));
+      });
     }
     const SolveScalars& h = read_scalars(cm.S, st);
     const int done = h.iters, halt = h.halt;
@@ -436,7 +504,19 @@ static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src,
 // An update whose true residual is not below kUpdateGain times the previous
 // one restarts the direction (p = rdiag r) instead of keeping it, and every
 // right-hand side finishes on its best iterate.
-constexpr double kUpdateDrop = 1e-3;
+// Tunables of the reliable updates (defaults; FPM_MIXED_UPDATE_DROP,
+// FPM_MIXED_UPDATE_MAX and FPM_MIXED_UPDATE_GAIN override them).
+static double env_double(const char* name, double dflt) {
+  const char* e = std::getenv(name);
+  if (!e || !e[0]) return dflt;
+  const double v = std::atof(e);
+  return v > 0 ? v : dflt;
+}
+static const double kUpdateDrop = env_double("FPM_MIXED_UPDATE_DROP", 1e-3);
+static const double kUpdateGain = env_double("FPM_MIXED_UPDATE_GAIN", 0.5);
+static const int kUpdateMax = (int)env_double("FPM_MIXED_UPDATE_MAX", 1000);
+constexpr double kBlowup = 4.0;
+constexpr int kStallUpdates = 4;
 // Planes per thread in the FP32 kernels (FPM_MIXED_KCHUNK overrides).
 static int mixed_kchunk() {
   static int v = -1;
@@ -446,10 +526,6 @@ static int mixed_kchunk() {
   }
   return v;
 }
-constexpr double kUpdateGain = 0.5;
-constexpr double kBlowup = 4.0;
-constexpr int kUpdateMax = 1000;
-constexpr int kStallUpdates = 4;
 
 static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
                         const double* rdiag, const double* coef64, const Axes& ax, const Coefs& c, double tol,
@@ -550,13 +626,14 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
   if (any) CUDA_TRY(launch_mx_start(G, v, r64, sc, MS, rbm, st));
   const int chunk_len = ci < 1 ? 1 : ci;
   int total = 0;
+  ChunkGraphs graphs(3);
   while (any && total < max_sweeps) {
     int chunk = chunk_len;
     if (chunk > max_sweeps - total) chunk = max_sweeps - total;
     CUDA_TRY(cudaMemsetAsync(&MS->iters, 0, sizeof(int), st));
     {
       TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
-      for (int n = 0; n < chunk; n++) CUDA_TRY(launch_mx_iteration(G, v, MS, rbm, st));
+      graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(launch_mx_iteration(G, v, MS, rbm, s2)); });
     }
     CUDA_TRY(cudaMemcpyAsync(hms, MS, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
@@ -643,10 +720,11 @@ static bool valid_method(int m) {
 
 // Learned initial guess for every right-hand side (see fpm_learned.cu): the
 // network's output, scaled by the A-norm projection, replaces the caller's
-// phi unless it fails to lower the max-norm residual (a fallback).
+// phi unless it is not closer to the solution in the energy norm (the norm CG
+// minimises), which counts as a fallback.
 static void learned_guess(void* net, const Dims& d, int nrhs, const SolveArgs* args, double* const src[],
-                          const double* diag, const Coefs& c, Scratch& A, Common& cm, int* fallbacks,
-                          cudaStream_t st) {
+                          const double* diag, const double* rdiag, const Coefs& c, Scratch& A, Common& cm,
+                          int* fallbacks, cudaStream_t st) {
   Trace tl("learned initial guess");
   const long long nc = d.ncell();
   uint8_t* fluid = A.get<uint8_t>(nc);
@@ -655,27 +733,32 @@ static void learned_guess(void* net, const Dims& d, int nrhs, const SolveArgs* a
   float* mz = A.get<float>(d.nz);
   float* b = A.get<float>(nc);
   float* y = A.get<float>(nc);
-  double* sc = A.get<double>(4);
+  double* sc = A.get<double>(8);
   double* backup = A.get<double>(d.npad());
+  double* r = A.get<double>(nc);
+  double h[8];
   for (int m = 0; m < nrhs; m++) {
     const SolveArgs& a = args[m];
-    CUDA_TRY(launch_operator_residual(d, a.phi, src[m], diag, c, cm.S, cm.rb, st));
-    const double before = read_scalars(cm.S, st).res;
+    CUDA_TRY(launch_energy(d, a.phi, src[m], diag, c, a.ax, sc + 4, cm.rb, st));
     CUDA_TRY(cudaMemcpyAsync(backup, a.phi, d.npad() * sizeof(double), cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(launch_learn_inputs(d, src[m], diag, a.ax, fluid, mx, my, mz, b, sc + 2, cm.rb, st));
     std::string err;
     const int rc = net::forward_into(net, d.nx, d.ny, d.nz, fluid, mx, my, mz, b, y, st, &err);
     if (rc != FPM_OK) throw Error{rc, err};
     CUDA_TRY(launch_learn_apply(d, y, src[m], diag, c, a.ax, a.phi, sc, cm.rb, st));
-    CUDA_TRY(launch_operator_residual(d, a.phi, src[m], diag, c, cm.S, cm.rb, st));
-    const double after = read_scalars(cm.S, st).res;
-    if (verbose()) std::fprintf(stderr, "fpm learned guess: rhs %d residual %.3e -> %.3e\n", m, before, after);
-    if (!(after < before)) {
-      CUDA_TRY(cudaMemcpyAsync(a.phi, backup, d.npad() * sizeof(double), cudaMemcpyDeviceToDevice, st));
-      if (fallbacks) fallbacks[m] = 1;
-    } else if (fallbacks) {
-      fallbacks[m] = 0;
+    CUDA_TRY(launch_energy(d, a.phi, src[m], diag, c, a.ax, sc + 6, cm.rb, st));
+    CUDA_TRY(cudaMemcpyAsync(h, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const double e_old = 0.5 * h[5] - h[4], e_new = 0.5 * h[7] - h[6];
+    const bool fail = !(e_new < e_old);
+    if (verbose()) {
+      CUDA_TRY(launch_true_residual(d, a.phi, src[m], diag, rdiag, r, nullptr, c, a.ax, 0, cm.S, cm.rb, st));
+      const SolveScalars& hs = read_scalars(cm.S, st);
+      std::fprintf(stderr, "fpm learned guess: rhs %d energy %.6e -> %.6e, guess residual max %.3e, r.(rdiag r) %.3e%s\n",
+                   m, e_old, e_new, hs.res, hs.rz, fail ? " (fallback)" : "");
     }
+    if (fail) CUDA_TRY(cudaMemcpyAsync(a.phi, backup, d.npad() * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (fallbacks) fallbacks[m] = fail ? 1 : 0;
   }
 }
 
@@ -706,7 +789,7 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
   }
   if (read_scalars(cm.S, st).isolated > 0) throw Error{FPM_E_ISOLATED, "stair-step fluid cell has no fluid neighbour"};
   for (int m = 0; m < nrhs; m++) CUDA_TRY(launch_init_fields(d, args[m].solid, args[m].phi, next, st));
-  if (net) learned_guess(net, d, nrhs, args, src, diag, c, A, cm, fallbacks, st);
+  if (net) learned_guess(net, d, nrhs, args, src, diag, rdiag, c, A, cm, fallbacks, st);
   {
     Trace t1("stair-step iterations");
     if (a0.method == FPM_METHOD_PCG_MIXED) {
@@ -1648,6 +1731,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     b.tol2 = kUpdateDrop * kUpdateDrop;  // each (frame, direction) stops its FP32 iteration at the update drop
     b.pmul = A.get<double>(nq);
     b.keep = A.get<int>(nq);
+    b.dir = A.get<int>(nq);
+    CUDA_TRY(cudaMemsetAsync(b.dir, 0, nq * sizeof(int), st));
     b.partials = A.get<double>(8 * (size_t)ntiles);
     b.tickets = A.get<unsigned int>(nframes);
     CUDA_TRY(cudaMemsetAsync(b.tickets, 0, nframes * sizeof(unsigned int), st));
@@ -1675,6 +1760,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     // Reliable updates per (frame, direction), as in mixed_solve.
     const int chunk_len = check_interval < 1 ? 1 : check_interval;
     long long total = 0;
+    ChunkGraphs graphs(3);
     std::vector<double> best(res), prev(res), pmul(nq, 0.0), rz(nq), rz0(nq);
     std::vector<int> live(nq), since(nq, 0), keepv(nq, 0);
     bool any = false;
@@ -1696,7 +1782,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       if (chunk > max_sweeps - total) chunk = (int)(max_sweeps - total);
       {
         TimedRun t(FPM_TIMER_FRAMES_ITER, chunk, st);
-        for (int n = 0; n < chunk; n++) CUDA_TRY(launch_b2_iteration(dfr, dtf, ntiles, b, st));
+        graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(launch_b2_iteration(dfr, dtf, ntiles, b, s2)); });
       }
       total += chunk;
       pull(act.data(), b.active, nq * sizeof(int));

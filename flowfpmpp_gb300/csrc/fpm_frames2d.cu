@@ -369,7 +369,11 @@ __global__ void k_b2_update(const Frame2* __restrict__ fr, const int* __restrict
     act[r] = b.active[t.f * kR + r];
     alpha[r] = (float)b.alpha[t.f * kR + r];
   }
-  if (!act[0] && !act[1]) return;
+  if (!act[0] && !act[1]) {
+    // no iteration for this frame: no direction update either
+    if (blockIdx.x == (unsigned)F.tile0 && lin_tid() == 0) b.dir[t.f * kR] = b.dir[t.f * kR + 1] = 0;
+    return;
+  }
   double s[kR] = {0.0, 0.0}, m[1] = {0.0};
   F2Pair acc[kR];
   if (t.live) {
@@ -390,15 +394,20 @@ __global__ void k_b2_update(const Frame2* __restrict__ fr, const int* __restrict
   if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0) {
     for (int r = 0; r < kR; r++) {
       const int q = t.f * kR + r;
-      if (!act[r]) continue;
+      if (!act[r]) {
+        b.dir[q] = 0;
+        continue;
+      }
       b.iters[q] += 1;
       const double rz_new = out[r];
       if (!(rz_new >= 0)) {
         b.active[q] = 0;
+        b.dir[q] = 0;
         continue;
       }
       b.beta[q] = rz_new / b.rz[q];
       b.rz[q] = rz_new;
+      b.dir[q] = 1;  // the direction update of this iteration still runs
       if (rz_new <= b.tol2 * b.rz0[q]) b.active[q] = 0;
     }
   }
@@ -410,7 +419,7 @@ __global__ void k_b2_direction(const Frame2* __restrict__ fr, const int* __restr
   int act[kR];
   float beta[kR];
   for (int r = 0; r < kR; r++) {
-    act[r] = b.active[t.f * kR + r];
+    act[r] = b.dir[t.f * kR + r];  // set by this iteration's update, even if it stopped the iteration
     beta[r] = (float)b.beta[t.f * kR + r];
   }
   if ((!act[0] && !act[1]) || !t.live) return;

@@ -132,6 +132,7 @@ struct MixedScale {
 struct MixedScalars {
   double rz[kMaxRhs], rz0[kMaxRhs], pq[kMaxRhs], alpha[kMaxRhs], beta[kMaxRhs], tol2[kMaxRhs];
   int active[kMaxRhs];
+  int dir[kMaxRhs];  // the update computed beta: the direction update runs (even if it stopped the iteration)
   int iters;
   int pad[3];
 };
@@ -174,6 +175,7 @@ struct Batch2 {
   // per (frame, direction) scalars, index 2*f + r
   double *corr, *res, *rmean, *scale, *pmul, *rz, *rz0, *alpha, *beta;
   int *in_set, *active, *iters;
+  int* dir;   // per (frame, direction): the update computed beta, so the direction update runs
   int* keep;  // per (frame, direction): 1 = save phi as the best iterate, 2 = restore it
   double tol2;
   double* partials;       // ntiles * 8
@@ -239,6 +241,8 @@ cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* 
                                 cudaStream_t st);
 cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src, const double* diag, const Coefs& c,
                                const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st);
+cudaError_t launch_energy(const Dims& d, const double* phi, const double* src, const double* diag, const Coefs& c,
+                          const Axes& ax, double* out2, const RedBuf& rb, cudaStream_t st);
 namespace net {
 // Network forward pass into out (FP32, one value per cell); returns an FPM_*
 // status and fills *err on failure.

@@ -9,9 +9,11 @@
 //
 // The network output y (FP32) is used as phi0 = gamma y_f, y_f = y on fluid
 // cells and 0 elsewhere, with gamma = (y_f . b) / (y_f . A y_f): the multiple
-// of y_f closest to the solution in the energy norm.  If phi0's max-norm
-// residual is not below that of the caller's initial guess, the guess is
-// discarded (a fallback) and the solve starts from the caller's phi.
+// of y_f closest to the solution in the energy norm.  The guess is kept only
+// if it is closer to the solution than the caller's phi in the norm CG
+// minimises, ||phi - phi*||_A, compared through the energy
+// E(phi) = phi.A phi / 2 - phi.b = ||phi - phi*||_A^2 / 2 + const; otherwise
+// it is discarded (a fallback) and the solve starts from the caller's phi.
 #include "fpm_internal.h"
 
 namespace fpm {
@@ -108,6 +110,32 @@ __global__ void k_learn_apply(Dims d, const float* __restrict__ y, const double*
   }
 }
 
+// phi.b and phi.(A phi) for a padded FP64 phi (zero in solid cells and the
+// physical halo), b = V src, A phi = V (diag phi - sum c phi_nb).
+__global__ void k_energy(Dims d, const double* __restrict__ phi, const double* __restrict__ src,
+                         const double* __restrict__ diag, Coefs cf, Axes ax, double* partials, unsigned int* ticket,
+                         double* out2) {
+  double s[2] = {0.0, 0.0}, m[1] = {0.0};
+  const long long n = d.ncell(), px = d.nx + 2, pl = d.plane();
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    if (!(diag[c] > 0)) continue;
+    const int i = (int)(c % d.nx) + 1, j = (int)((c / d.nx) % d.ny) + 1, k = (int)(c / ((long long)d.nx * d.ny)) + 1;
+    const long long p = d.ph(i, j, k);
+    const double vol = ax.dx[i - 1] * ax.dy[j - 1] * ax.dz[k - 1];
+    const double f = phi[p];
+    const double nb = cf.cw[i - 1] * phi[p - 1] + cf.ce[i - 1] * phi[p + 1] + cf.cs[j - 1] * phi[p - px] +
+                      cf.cn[j - 1] * phi[p + px] + cf.cb[k - 1] * phi[k > 1 ? p - pl : p] +
+                      cf.ct[k - 1] * phi[k < d.nz ? p + pl : p];
+    s[0] += f * vol * src[c];
+    s[1] += f * vol * (diag[c] * f - nb);
+  }
+  double o[2];
+  if (grid_reduce<2, 0>(s, m, partials, ticket, o) && lin_tid() == 0) {
+    out2[0] = o[0];
+    out2[1] = o[1];
+  }
+}
+
 unsigned blocks_for(long long n) {
   long long b = (n + 255) / 256;
   if (b > 152LL * 16) b = 152LL * 16;
@@ -137,6 +165,15 @@ cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src,
   k_learn_dots<<<nb, 256, 0, st>>>(d, y, src, diag, c, ax, rb.partials, rb.ticket, dots);
   note_launch();
   k_learn_apply<<<blocks_for(d.ncell()), 256, 0, st>>>(d, y, diag, dots, phi);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy(const Dims& d, const double* phi, const double* src, const double* diag, const Coefs& c,
+                          const Axes& ax, double* out2, const RedBuf& rb, cudaStream_t st) {
+  const unsigned nb = blocks_for(d.ncell());
+  if ((int)nb > rb.max_blocks) return cudaErrorInvalidValue;
+  k_energy<<<nb, 256, 0, st>>>(d, phi, src, diag, c, ax, rb.partials, rb.ticket, out2);
   note_launch();
   return cudaGetLastError();
 }

@@ -271,7 +271,11 @@ __global__ void __launch_bounds__(128) k_mx_update(MixedGrid G, MixedVecs v, Mix
     alpha[m] = (float)S->alpha[m];
     any = any || act[m];
   }
-  if (!any) return;
+  if (!any) {
+    if (lin_bid() == 0 && lin_tid() == 0)
+      for (int m = 0; m < kMaxRhs; m++) S->dir[m] = 0;
+    return;
+  }
   F2Acc acc[NR];
   const MxPos t = mx_pos(G);
   if (t.live) {
@@ -307,14 +311,19 @@ __global__ void __launch_bounds__(128) k_mx_update(MixedGrid G, MixedVecs v, Mix
   if (grid_reduce<kMaxRhs, 0>(s, mm, rb.partials, rb.ticket, out)) {
     if (lin_tid() == 0) {
       for (int m = 0; m < kMaxRhs; m++) {
-        if (!act[m]) continue;
+        if (!act[m]) {
+          S->dir[m] = 0;
+          continue;
+        }
         const double rz_new = out[m];
         if (!(rz_new >= 0)) {
           S->active[m] = 0;
+          S->dir[m] = 0;
           continue;
         }
         S->beta[m] = rz_new / S->rz[m];
         S->rz[m] = rz_new;
+        S->dir[m] = 1;  // the direction update of this iteration still runs
         if (rz_new <= S->tol2[m] * S->rz0[m]) S->active[m] = 0;
       }
     }
@@ -329,7 +338,7 @@ __global__ void __launch_bounds__(128) k_mx_direction(MixedGrid G, MixedVecs v, 
   bool any = false;
 #pragma unroll
   for (int m = 0; m < kMaxRhs; m++) {
-    act[m] = m < v.nrhs ? S->active[m] : 0;
+    act[m] = m < v.nrhs ? S->dir[m] : 0;
     beta[m] = (float)S->beta[m];
     any = any || act[m];
   }

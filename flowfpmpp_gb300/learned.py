@@ -142,7 +142,29 @@ def random_bodies(rng: np.random.Generator, ax, ay, az) -> np.ndarray:
             solid |= (np.abs(X - cen[0]) < h[0]) & (np.abs(Y - cen[1]) < h[1]) & (np.abs(Z - cen[2]) < h[2])
     if not solid.any():
         solid[nx // 2, ny // 2, nz // 2] = True
-    return solid
+    # fluid pockets enclosed by the body have no outer face: their Neumann
+    # problem is incompatible on its own, so they are blocked
+    from scipy import ndimage
+    lab, _ = ndimage.label(~solid)
+    outer = np.unique(np.concatenate([lab[0].ravel(), lab[-1].ravel(), lab[:, 0].ravel(), lab[:, -1].ravel(),
+                                      lab[:, :, 0].ravel(), lab[:, :, -1].ravel()]))
+    solid |= ~np.isin(lab, outer[outer > 0])
+    # the solver rejects fluid cells without a fluid neighbour (as the
+    # reference does): block them
+    while True:
+        fl = ~solid
+        nb = np.zeros(solid.shape, dtype=np.int8)
+        for axis in range(3):
+            for sh in (1, -1):
+                r = np.roll(fl, sh, axis=axis)
+                idx = [slice(None)] * 3
+                idx[axis] = 0 if sh == 1 else -1
+                r[tuple(idx)] = False
+                nb += r
+        lonely = fl & (nb == 0)
+        if not lonely.any():
+            return solid
+        solid |= lonely
 
 
 def frame_for(solid_interior: np.ndarray, ax, ay, az, axis: int):

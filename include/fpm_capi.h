@@ -340,9 +340,11 @@ int fpm_net_train_step_dev(void* net, int nx, int ny, int nz, const uint8_t* flu
                            double* loss, void* stream);
 /* fpm_solve_stairstep_multi_dev with the network's initial guess: for each
  * right-hand side, phi0 = gamma * net(...) (gamma from the A-norm projection)
- * replaces the caller's phi unless its max-norm residual is not lower, in
- * which case the caller's phi is kept and fallbacks[m] = 1 (fallbacks may be
- * NULL).  Any method; nx, ny, nz multiples of 8. */
+ * replaces the caller's phi unless it is not closer to the solution in the
+ * energy norm ||phi - phi*||_A (the norm CG minimises, compared through
+ * phi.A phi / 2 - phi.b), in which case the caller's phi is kept and
+ * fallbacks[m] = 1 (fallbacks may be NULL).  Any method; nx, ny, nz
+ * multiples of 8. */
 int fpm_solve_stairstep_learned_dev(void* net, int nrhs, double* const* phi, const double* const* rhs,
                                     const int32_t* solid, const double* body_grads, const double* const* faces,
                                     const double* xc, const double* yc, const double* zc, const double* dx,

@@ -58,12 +58,12 @@ def test_forward_and_gradients_match_oracle(gpu_lib):
     assert np.linalg.norm(y - y_o) <= 1e-2 * np.linalg.norm(y_o)
     assert abs(loss - loss_o) <= 2e-3, (loss, loss_o)
     for n, (sw, sb) in enumerate(_layers()):
+        # relative to the layer's whole gradient where a part is ~0 in exact
+        # arithmetic (the head bias: the loss is offset free)
+        scale = np.linalg.norm(g_o[sw.start:sb.stop])
         for sl, what in ((sw, "weights"), (sb, "bias")):
             ref = g_o[sl]
-            if np.linalg.norm(ref) == 0:
-                assert np.abs(g[sl]).max() == 0
-                continue
-            err = np.linalg.norm(g[sl] - ref) / np.linalg.norm(ref)
+            err = np.linalg.norm(g[sl] - ref) / max(np.linalg.norm(ref), 1e-2 * scale)
             assert err <= 3e-2, (n, what, err)
 
 
