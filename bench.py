@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, nargs=3, default=None,
+                    help="pcg_c3 only: a smaller grid of the same generator (profiling runs)")
     ap.add_argument("--workload", choices=["jacobi256", "pcg_c1", "pcg_c3", "frames_c4", "learned_c5"],
                     default="jacobi256",
                     help="jacobi256: the headline bandwidth benchmark; pcg_c1 / pcg_c3: three-potential PCG "
@@ -210,6 +212,9 @@ def run_pcg(args):
     if args.workload == "pcg_c1":
         f = workloads.sphere_c1()
         name = "C1 64x64x32 sphere, ratio 1.03"
+    elif args.grid:
+        f = workloads.ellipsoids_c3(*args.grid)
+        name = "C3 generator at %dx%dx%d, 3 ellipsoids, ratio 1.02" % tuple(args.grid)
     else:
         f = workloads.ellipsoids_c3()
         name = "C3 384x384x192, 3 ellipsoids, ratio 1.02"

@@ -263,6 +263,12 @@ class ChunkGraphs {
   }
   int kpi_;
   std::map<int, cudaGraphExec_t> exec_;
+
+ public:
+  void clear() {
+    for (auto& kv : exec_) cudaGraphExecDestroy(kv.second);
+    exec_.clear();
+  }
 };
 
 // PCG with the control flow of pcg_iterate (src/fpm_stairstep_mpi_3d.f90:235-293):
@@ -501,8 +507,10 @@ static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src,
 // residual at each update, exactly the reference's test; a right-hand side
 // also stops after kStallUpdates updates without a 1% improvement (the
 // reference's roundoff-floor rule, counted in updates).
-// An update whose true residual is not below kUpdateGain times the previous
-// one restarts the direction (p = rdiag r) instead of keeping it, and every
+// The direction is restarted (p = rdiag r) only after a breakdown or a
+// rolled-back update (kBlowup); slow progress keeps it, because a restart
+// throws the Krylov space away.  (FPM_MIXED_UPDATE_GAIN = g also restarts
+// when an update's residual is not below g times the previous one.)  Every
 // right-hand side finishes on its best iterate.
 // Tunables of the reliable updates (defaults; FPM_MIXED_UPDATE_DROP,
 // FPM_MIXED_UPDATE_MAX and FPM_MIXED_UPDATE_GAIN override them).
@@ -513,7 +521,7 @@ static double env_double(const char* name, double dflt) {
   return v > 0 ? v : dflt;
 }
 static const double kUpdateDrop = env_double("FPM_MIXED_UPDATE_DROP", 1e-3);
-static const double kUpdateGain = env_double("FPM_MIXED_UPDATE_GAIN", 0.5);
+static const double kUpdateGain = env_double("FPM_MIXED_UPDATE_GAIN", 1e300);
 static const int kUpdateMax = (int)env_double("FPM_MIXED_UPDATE_MAX", 1000);
 constexpr double kBlowup = 4.0;
 constexpr int kStallUpdates = 4;
@@ -1676,6 +1684,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     int* dtf = A.upload(tile_frame.data(), tile_frame.size());
     Batch2 b;
     std::memset(&b, 0, sizeof(b));
+    std::memset(&b, 0, sizeof(b));
     b.xc = A.upload(hxc.data(), hxc.size());
     b.dx = A.upload(hdx.data(), hdx.size());
     b.xf = A.upload(hxf.data(), hxf.size());
@@ -1777,12 +1786,37 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       CUDA_TRY(launch_k_b2_start(dfr, dtf, ntiles, b, st));
     };
     if (any) push_start();
+    // The iteration kernels run over the tiles of the frames that still have
+    // a live direction; the list is compacted whenever frames finish.
+    int* dtiles = A.get<int>(ntiles);
+    std::vector<int> act_tiles;
+    std::vector<char> frame_on(nframes, 0);
+    Batch2 bi = b;
+    bi.tiles = dtiles;
+    int nact = 0;
+    auto rebuild_tiles = [&]() {
+      bool changed = false;
+      for (int f = 0; f < nframes; f++) {
+        const char on = (live[2 * f] || live[2 * f + 1]) ? 1 : 0;
+        changed = changed || on != frame_on[f];
+        frame_on[f] = on;
+      }
+      if (!changed) return;
+      act_tiles.clear();
+      for (int f = 0; f < nframes; f++)
+        if (frame_on[f])
+          for (int t = 0; t < fr[f].ntiles; t++) act_tiles.push_back(fr[f].tile0 + t);
+      nact = (int)act_tiles.size();
+      if (nact) CUDA_TRY(cudaMemcpyAsync(dtiles, act_tiles.data(), nact * sizeof(int), cudaMemcpyHostToDevice, st));
+      graphs.clear();
+    };
+    rebuild_tiles();
     while (any && total < max_sweeps) {
       int chunk = chunk_len;
       if (chunk > max_sweeps - total) chunk = (int)(max_sweeps - total);
       {
         TimedRun t(FPM_TIMER_FRAMES_ITER, chunk, st);
-        graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(launch_b2_iteration(dfr, dtf, ntiles, b, s2)); });
+        graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(launch_b2_iteration(dfr, dtf, nact, bi, s2)); });
       }
       total += chunk;
       pull(act.data(), b.active, nq * sizeof(int));
@@ -1860,6 +1894,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         CUDA_TRY(launch_k_b2_keep(dfr, dtf, ntiles, b, st));
       }
       CUDA_TRY(cudaMemcpyAsync(b.active, act.data(), nq * sizeof(int), cudaMemcpyHostToDevice, st));
+      rebuild_tiles();
       bool refresh = false;
       for (size_t q = 0; q < nq; q++) refresh = refresh || set[q];
       if (refresh) push_start();

@@ -24,15 +24,19 @@ constexpr int kR = 2;  // right-hand sides per frame (phi_x, phi_y)
 constexpr double kCz = 4.0;
 
 struct TileRef {
-  int f, i, j;  // frame, 1-based cell indices of this thread's column
+  int tile, f, i, j;  // global tile id, frame, 1-based cell indices of this thread's column
   bool live;
 };
 
-__device__ __forceinline__ TileRef tile_ref(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame) {
+// Block -> tile: the identity, or an entry of a compacted list of the tiles of
+// the frames still iterating (all tiles of a frame are in it or none).
+__device__ __forceinline__ TileRef tile_ref(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame,
+                                            const int* __restrict__ tiles) {
   TileRef t;
-  t.f = tile_frame[blockIdx.x];
+  t.tile = tiles ? tiles[blockIdx.x] : (int)blockIdx.x;
+  t.f = tile_frame[t.tile];
   const Frame2& F = fr[t.f];
-  const int idx = blockIdx.x - F.tile0;
+  const int idx = t.tile - F.tile0;
   t.i = (idx % F.tiles_x) * 32 + threadIdx.x + 1;
   t.j = (idx / F.tiles_x) * 8 + threadIdx.y + 1;
   t.live = t.i <= F.nx && t.j <= F.ny;
@@ -53,16 +57,16 @@ __device__ __forceinline__ long long c2(const Frame2& F, int i, int j) {
 // Returns true in the last tile of the frame, with out[] holding the results.
 template <int NS, int NM>
 __device__ bool seg_reduce(double (&s)[NS > 0 ? NS : 1], double (&m)[NM > 0 ? NM : 1], const Frame2& F, int f,
-                           double* partials, unsigned int* tickets, double* out) {
+                           double* partials, unsigned int* tickets, double* out, int tile) {
   __shared__ bool am_last;
   constexpr int N = NS + NM;
   block_reduce<NS, NM>(s, m);
   const int tid = lin_tid();
   if (tid == 0) {
 #pragma unroll
-    for (int n = 0; n < NS; n++) partials[(size_t)blockIdx.x * N + n] = s[n];
+    for (int n = 0; n < NS; n++) partials[(size_t)tile * N + n] = s[n];
 #pragma unroll
-    for (int n = 0; n < NM; n++) partials[(size_t)blockIdx.x * N + NS + n] = m[n];
+    for (int n = 0; n < NM; n++) partials[(size_t)tile * N + NS + n] = m[n];
     __threadfence();
     const unsigned int t = atomicAdd(&tickets[f], 1u);
     am_last = (t == (unsigned int)F.ntiles - 1);
@@ -115,7 +119,7 @@ struct F2Pair {
 // rhs = 0 and zero outer data: correction = -(body flux) / (fluid outer area),
 // for body_grad = e_x (r = 0) and e_y (r = 1).
 __global__ void k_b2_compat(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   double s[3] = {0.0, 0.0, 0.0}, m[1] = {0.0};
   if (t.live) {
@@ -135,7 +139,7 @@ __global__ void k_b2_compat(const Frame2* __restrict__ fr, const int* __restrict
     }
   }
   double out[3];
-  if (seg_reduce<3, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0) {
+  if (seg_reduce<3, 0>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0) {
     const double area = out[2];
     for (int r = 0; r < kR; r++) b.corr[t.f * kR + r] = area > 0 ? -out[r] / area : 0.0;
     if (!(area > 0)) atomicExch(b.err, 2);
@@ -147,7 +151,7 @@ __global__ void k_b2_compat(const Frame2* __restrict__ fr, const int* __restrict
 // directions: outer faces carry +-corr (xlo = -c, xhi = +c, ...), body faces
 // body_grad; diag, rdiag = 1/(V diag) shared by both directions.
 __global__ void k_b2_build(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   if (!t.live) return;
   const Frame2& F = fr[t.f];
   const int i = t.i, j = t.j, nx = F.nx, ny = F.ny;
@@ -229,7 +233,7 @@ __device__ __forceinline__ ColCoef col_coef(const Frame2& F, const Batch2& b, in
 // rV = V t on diag > 0 (t = src + sum c phi - diag phi), res = max |t|, and
 // the sum and count for the projection; only directions in the set.
 __global__ void k_b2_tres(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   int set[kR];
   for (int r = 0; r < kR; r++) set[r] = b.in_set[t.f * kR + r];
@@ -256,7 +260,7 @@ __global__ void k_b2_tres(const Frame2* __restrict__ fr, const int* __restrict__
     }
   }
   double out[5];
-  if (seg_reduce<3, 2>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0) {
+  if (seg_reduce<3, 2>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0) {
     for (int r = 0; r < kR; r++) {
       if (!set[r]) continue;
       b.res[t.f * kR + r] = out[3 + r];
@@ -269,7 +273,7 @@ __global__ void k_b2_tres(const Frame2* __restrict__ fr, const int* __restrict__
 // Residual replacement (reliable update) for the (frame, direction) pairs in
 // the set: r = scale (rV - mean), e = 0, p = rdiag r (pmul == 0) or p *= pmul.
 __global__ void k_b2_start(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   int set[kR];
   for (int r = 0; r < kR; r++) set[r] = b.in_set[t.f * kR + r];
@@ -296,7 +300,7 @@ __global__ void k_b2_start(const Frame2* __restrict__ fr, const int* __restrict_
   }
   for (int r = 0; r < kR; r++) s[r] = acc[r].value();
   double out[kR];
-  if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0) {
+  if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0) {
     for (int r = 0; r < kR; r++) {
       if (!set[r]) continue;
       const int q = t.f * kR + r;
@@ -308,7 +312,7 @@ __global__ void k_b2_start(const Frame2* __restrict__ fr, const int* __restrict_
 }
 
 __global__ void k_b2_spmv(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   int act[kR];
   for (int r = 0; r < kR; r++) act[r] = b.active[t.f * kR + r];
@@ -346,7 +350,7 @@ __global__ void k_b2_spmv(const Frame2* __restrict__ fr, const int* __restrict__
   }
   for (int r = 0; r < kR; r++) s[r] = acc[r].value();
   double out[kR];
-  if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0) {
+  if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0) {
     for (int r = 0; r < kR; r++) {
       const int q = t.f * kR + r;
       if (!act[r]) continue;
@@ -361,7 +365,7 @@ __global__ void k_b2_spmv(const Frame2* __restrict__ fr, const int* __restrict__
 }
 
 __global__ void k_b2_update(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   int act[kR];
   float alpha[kR];
@@ -371,7 +375,7 @@ __global__ void k_b2_update(const Frame2* __restrict__ fr, const int* __restrict
   }
   if (!act[0] && !act[1]) {
     // no iteration for this frame: no direction update either
-    if (blockIdx.x == (unsigned)F.tile0 && lin_tid() == 0) b.dir[t.f * kR] = b.dir[t.f * kR + 1] = 0;
+    if (t.tile == F.tile0 && lin_tid() == 0) b.dir[t.f * kR] = b.dir[t.f * kR + 1] = 0;
     return;
   }
   double s[kR] = {0.0, 0.0}, m[1] = {0.0};
@@ -391,7 +395,7 @@ __global__ void k_b2_update(const Frame2* __restrict__ fr, const int* __restrict
   }
   for (int r = 0; r < kR; r++) s[r] = acc[r].value();
   double out[kR];
-  if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0) {
+  if (seg_reduce<kR, 0>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0) {
     for (int r = 0; r < kR; r++) {
       const int q = t.f * kR + r;
       if (!act[r]) {
@@ -414,7 +418,7 @@ __global__ void k_b2_update(const Frame2* __restrict__ fr, const int* __restrict
 }
 
 __global__ void k_b2_direction(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   int act[kR];
   float beta[kR];
@@ -432,7 +436,7 @@ __global__ void k_b2_direction(const Frame2* __restrict__ fr, const int* __restr
 }
 
 __global__ void k_b2_apply(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   if (!t.live) return;
   const Frame2& F = fr[t.f];
   for (int r = 0; r < kR; r++) {
@@ -445,7 +449,7 @@ __global__ void k_b2_apply(const Frame2* __restrict__ fr, const int* __restrict_
 
 // Best-iterate bookkeeping: copy phi to phi_best (keep = 1) or back (keep = 2).
 __global__ void k_b2_keep(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   if (!t.live) return;
   const Frame2& F = fr[t.f];
   for (int r = 0; r < kR; r++) {
@@ -462,7 +466,7 @@ __global__ void k_b2_keep(const Frame2* __restrict__ fr, const int* __restrict__
 // ---------------------------------------------------------------- gauge
 // src/fpm_stairstep_mpi_3d.f90:170-185 per frame and direction.
 __global__ void k_b2_gauge_sum(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   double s[3] = {0.0, 0.0, 0.0}, m[1] = {0.0};
   if (t.live) {
@@ -475,11 +479,11 @@ __global__ void k_b2_gauge_sum(const Frame2* __restrict__ fr, const int* __restr
     }
   }
   double out[3];
-  if (seg_reduce<3, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0)
+  if (seg_reduce<3, 0>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0)
     for (int r = 0; r < kR; r++) b.rmean[t.f * kR + r] = out[r] / out[2];
 }
 __global__ void k_b2_gauge_sub(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   if (!t.live) return;
   const Frame2& F = fr[t.f];
   for (int k = 1; k <= 2; k++) {
@@ -526,7 +530,7 @@ __device__ __forceinline__ Face2 face2(const Frame2& F, const Batch2& b, int i, 
 }
 
 __global__ void k_b2_part1(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   if (!t.live) return;
   const Frame2& F = fr[t.f];
   const int i = t.i, j = t.j;
@@ -577,7 +581,7 @@ __global__ void k_b2_part1(const Frame2* __restrict__ fr, const int* __restrict_
 }
 
 __global__ void k_b2_part2(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
-  const TileRef t = tile_ref(fr, tile_frame);
+  const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, m[1] = {0.0};  // [r*4 + term]
   const int i = t.i, j = t.j;
@@ -643,7 +647,7 @@ __global__ void k_b2_part2(const Frame2* __restrict__ fr, const int* __restrict_
     }
   }
   double out[8];
-  if (seg_reduce<8, 0>(s, m, F, t.f, b.partials, b.tickets, out) && lin_tid() == 0)
+  if (seg_reduce<8, 0>(s, m, F, t.f, b.partials, b.tickets, out, t.tile) && lin_tid() == 0)
     for (int n = 0; n < 8; n++) b.terms[t.f * 8 + n] = out[n];
 }
 

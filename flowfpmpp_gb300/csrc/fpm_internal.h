@@ -180,6 +180,7 @@ struct Batch2 {
   double tol2;
   double* partials;       // ntiles * 8
   unsigned int* tickets;  // one per frame
+  const int* tiles;       // compacted list of tile ids launched (NULL: block = tile)
   int* err;
 };
 #define B2_DECL(kern) \

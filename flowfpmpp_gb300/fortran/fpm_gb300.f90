@@ -156,6 +156,7 @@ contains
       case ('pcg'); m = 0
       case ('jacobi'); m = 1
       case ('jacobi_df'); m = 2
+      case ('pcg_mixed'); m = 3
       case default; error stop 'stair-step method must be pcg or jacobi'
       end select
     end if

@@ -111,10 +111,13 @@ class LearnedGuess:
 
 # ---------------------------------------------------------------- problems
 def training_grid(nx: int, ny: int, nz: int):
-    """Axes of the training / evaluation boxes: [-3,3]^2 x [-1.5,1.5], ratio 1.02."""
+    """Axes of the training / evaluation boxes: ratio 1.02 away from the centre
+    planes, at least [-3,3]^2 x [-1.5,1.5], smallest cell at least 0.01 (so
+    the FP64 rounding floor of the max-norm residual stays well below 1e-10)."""
     hx, hy, hz = TRAIN_DOMAIN
-    return (workloads.geometric_axis(nx, -hx, hx, TRAIN_RATIO), workloads.geometric_axis(ny, -hy, hy, TRAIN_RATIO),
-            workloads.geometric_axis(nz, -hz, hz, TRAIN_RATIO))
+    return (workloads.geometric_axis_w0(nx, 0.01, TRAIN_RATIO, hx),
+            workloads.geometric_axis_w0(ny, 0.01, TRAIN_RATIO, hy),
+            workloads.geometric_axis_w0(nz, 0.01, TRAIN_RATIO, hz))
 
 
 def random_bodies(rng: np.random.Generator, ax, ay, az) -> np.ndarray:
