@@ -535,10 +535,39 @@ static int mixed_kchunk() {
   return v;
 }
 
+static bool learned_refine() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("FPM_LEARNED_REFINE");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
 static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
-                        const double* rdiag, const double* coef64, const Axes& ax, const Coefs& c, double tol,
-                        int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st) {
+                        const double* rdiag, const int32_t* solid, const Axes& ax, const Coefs& c, double tol,
+                        int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st,
+                        void* net = nullptr) {
   const long long np = d.npad();
+  // Network correction steps inside the refinement (FPM_LEARNED_REFINE=1 with
+  // a network): at every residual replacement, phi += gamma net(r), gamma
+  // the energy-optimal step, then the FP32 iteration restarts from the new
+  // residual.
+  struct NetBufs {
+    uint8_t* fluid = nullptr;
+    float *mx = nullptr, *my = nullptr, *mz = nullptr, *b = nullptr, *y = nullptr;
+    double* sc = nullptr;
+  } nb;
+  const bool refine = net && learned_refine();
+  if (refine) {
+    nb.fluid = A.get<uint8_t>(d.ncell());
+    nb.mx = A.get<float>(d.nx);
+    nb.my = A.get<float>(d.ny);
+    nb.mz = A.get<float>(d.nz);
+    nb.b = A.get<float>(d.ncell());
+    nb.y = A.get<float>(d.ncell());
+    nb.sc = A.get<double>(4);
+  }
   const MixedGrid G = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk());
   MixedVecs v;
   std::memset(&v, 0, sizeof(v));
@@ -548,11 +577,11 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
     CUDA_TRY(cudaMemsetAsync(x, 0, G.size * sizeof(float), st));
     return x;
   };
-  float* diag32 = vec();
+  float* wall32 = vec();
   float* rdiag32 = vec();
-  CUDA_TRY(launch_mx_layout(G, diag, diag32, st));
+  CUDA_TRY(launch_mx_wall(G, d, solid, c, wall32, st));
   CUDA_TRY(launch_mx_layout(G, rdiag, rdiag32, st));
-  v.diag = diag32;
+  v.wall = wall32;
   v.rdiag = rdiag32;
   auto row = [&](const double* a) {
     float* x = A.get<float>(G.px);
@@ -617,7 +646,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
   } hf{hms};
 
   double res[kMaxRhs], best[kMaxRhs], prev[kMaxRhs], scale[kMaxRhs];
-  int stall[kMaxRhs] = {}, since[kMaxRhs] = {};
+  int stall[kMaxRhs] = {}, since[kMaxRhs] = {}, done_at[kMaxRhs] = {-1, -1, -1, -1};
   bool live[kMaxRhs] = {};
   MixedScale sc;
   std::memset(&sc, 0, sizeof(sc));
@@ -625,6 +654,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
   for (int m = 0; m < nrhs; m++) {
     res[m] = best[m] = prev[m] = true_res(m);
     live[m] = res[m] > tol && res[m] == res[m];
+    if (!live[m]) done_at[m] = 0;
     scale[m] = res[m] > 0 ? 1.0 / res[m] : 1.0;
     sc.in_set[m] = live[m];
     sc.scale[m] = scale[m];
@@ -675,6 +705,19 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
           res[m] = true_res(m);
           sc.pmul[m] = 0.0;
         }
+        if (refine && res[m] > tol) {
+          CUDA_TRY(launch_learn_inputs(d, r64.p[m], diag, ax, nb.fluid, nb.mx, nb.my, nb.mz, nb.b, nb.sc + 2, cm.rb,
+                                       st, 1));
+          std::string err;
+          const int rc = net::forward_into(net, d.nx, d.ny, d.nz, nb.fluid, nb.mx, nb.my, nb.mz, nb.b, nb.y, st, &err);
+          if (rc != FPM_OK) throw Error{rc, err};
+          CUDA_TRY(launch_learn_apply(d, nb.y, r64.p[m], diag, c, ax, phi[m], nb.sc, cm.rb, st, 1, 1));
+          const double before = res[m];
+          res[m] = true_res(m);
+          sc.pmul[m] = 0.0;
+          if (verbose())
+            std::fprintf(stderr, "fpm pcg_mixed: rhs %d network step residual %.3e -> %.3e\n", m, before, res[m]);
+        }
         stall[m] = res[m] < 0.99 * best[m] ? 0 : stall[m] + 1;
         if (res[m] < best[m]) {
           best[m] = res[m];
@@ -684,6 +727,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
         prev[m] = res[m];
         if (!(res[m] > tol) || !(res[m] == res[m]) || stall[m] >= kStallUpdates) {
           live[m] = false;
+          done_at[m] = total;
           sc.in_set[m] = 0;
           if (!(res[m] <= best[m]))  // finish on the best iterate
             CUDA_TRY(cudaMemcpyAsync(phi[m], best_phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -716,7 +760,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
       pend = true;
     }
   if (pend) CUDA_TRY(launch_mx_apply(G, v, phis, sc, st));
-  for (int m = 0; m < nrhs; m++) sweeps_out[m] = total;
+  for (int m = 0; m < nrhs; m++) sweeps_out[m] = done_at[m] >= 0 ? done_at[m] : total;
 }
 
 // solve_stairstep_poisson_3d (src/fpm_stairstep_mpi_3d.f90:106-330), device
@@ -803,7 +847,8 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
     if (a0.method == FPM_METHOD_PCG_MIXED) {
       double* phis[kMaxRhs] = {};
       for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
-      mixed_solve(d, nrhs, phis, src, diag, rdiag, coef, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps, st);
+      mixed_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps,
+                  st, net);
     } else {
       for (int m = 0; m < nrhs; m++) {
         const SolveArgs& a = args[m];
@@ -1719,6 +1764,11 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     b.rdiag = A.get<double>(nint);
     b.diag32 = A.get<float>(nint);
     b.rdiag32 = A.get<float>(nint);
+    b.wall32 = A.get<float>(nint);
+    b.cw32 = A.get<float>(npx);
+    b.ce32 = A.get<float>(npx);
+    b.cs32 = A.get<float>(npy);
+    b.cn32 = A.get<float>(npy);
     b.nxf = A.get<double>(n2);
     b.nyf = A.get<double>(n2);
     b.omega = A.get<double>(n2);

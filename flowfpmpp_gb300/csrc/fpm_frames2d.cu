@@ -162,9 +162,17 @@ __global__ void k_b2_build(const Frame2* __restrict__ fr, const int* __restrict_
   const double ce = i == nx ? 0.0 : ddiv(1.0, dmul(dxi, dsub(xc[i + 1], xc[i])));
   const double cs = j == 1 ? 0.0 : ddiv(1.0, dmul(dyj, dsub(yc[j], yc[j - 1])));
   const double cn = j == ny ? 0.0 : ddiv(1.0, dmul(dyj, dsub(yc[j + 1], yc[j])));
+  if (j == 1) {
+    b.cw32[F.ox + i - 1] = (float)cw;
+    b.ce32[F.ox + i - 1] = (float)ce;
+  }
+  if (i == 1) {
+    b.cs32[F.oy + j - 1] = (float)cs;
+    b.cn32[F.oy + j - 1] = (float)cn;
+  }
   for (int k = 1; k <= 2; k++) {
     const long long c = in(F, i, j, k);
-    double s[kR] = {0.0, 0.0}, d = 0.0;
+    double s[kR] = {0.0, 0.0}, d = 0.0, wall = -1.0;
     if (b.solid3[ph(F, i, j, k)] == 0) {
       const double bg[kR][2] = {{1.0, 0.0}, {0.0, 1.0}};
       for (int r = 0; r < kR; r++) {
@@ -187,7 +195,13 @@ __global__ void k_b2_build(const Frame2* __restrict__ fr, const int* __restrict_
       if (j > 1 && b.solid3[ph(F, i, j - 1, k)] == 0) d = dadd(d, cs);
       if (j < ny && b.solid3[ph(F, i, j + 1, k)] == 0) d = dadd(d, cn);
       d = dadd(d, kCz);  // the other z layer of a fluid column is fluid
+      wall = 0.0;        // coefficients towards solid neighbours (difference form of the FP32 stencil)
+      if (i > 1 && b.solid3[ph(F, i - 1, j, k)] != 0) wall += cw;
+      if (i < nx && b.solid3[ph(F, i + 1, j, k)] != 0) wall += ce;
+      if (j > 1 && b.solid3[ph(F, i, j - 1, k)] != 0) wall += cs;
+      if (j < ny && b.solid3[ph(F, i, j + 1, k)] != 0) wall += cn;
     }
+    b.wall32[c] = (float)wall;
     for (int r = 0; r < kR; r++) b.src[r][c] = s[r];
     b.diag[c] = d;
     const double rd = d > 0 ? ddiv(1.0, dmul(dmul(dmul(dxi, dyj), dzk), d)) : 0.0;
@@ -320,8 +334,9 @@ __global__ void k_b2_spmv(const Frame2* __restrict__ fr, const int* __restrict__
   double s[kR] = {0.0, 0.0}, m[1] = {0.0};
   F2Pair acc[kR];
   if (t.live) {
-    const ColCoef cc = col_coef(F, b, t.i, t.j);
-    const float cw = (float)cc.cw, ce = (float)cc.ce, cs = (float)cc.cs, cn = (float)cc.cn, cz = (float)kCz;
+    // difference form V (sum_nb c (p - p_nb) - wall p) of V (diag p - sum c p_nb)
+    const float cw = b.cw32[F.ox + t.i - 1], ce = b.ce32[F.ox + t.i - 1], cs = b.cs32[F.oy + t.j - 1],
+                cn = b.cn32[F.oy + t.j - 1], cz = (float)kCz;
     const float vol = (float)b.dx[F.ox + t.i - 1] * (float)b.dy[F.oy + t.j - 1] * 0.5f;
     const long long px = F.nx + 2, pl = (long long)(F.nx + 2) * (F.ny + 2);
     for (int r = 0; r < kR; r++) {
@@ -331,16 +346,16 @@ __global__ void k_b2_spmv(const Frame2* __restrict__ fr, const int* __restrict__
       const float a1 = pm[p1], a2 = pm[p2];
       for (int k = 1; k <= 2; k++) {
         const long long c = in(F, t.i, t.j, k), p = k == 1 ? p1 : p2;
-        const float dg = b.diag32[c];
+        const float wl = b.wall32[c];
         const float pc = k == 1 ? a1 : a2, pz = k == 1 ? a2 : a1;
         float q = 0.f;
-        if (dg > 0.f) {
-          float tt = dg * pc;
-          tt = fmaf(-cw, pm[p - 1], tt);
-          tt = fmaf(-ce, pm[p + 1], tt);
-          tt = fmaf(-cs, pm[p - px], tt);
-          tt = fmaf(-cn, pm[p + px], tt);
-          tt = fmaf(-cz, pz, tt);
+        if (wl >= 0.f) {
+          float tt = -wl * pc;
+          tt = fmaf(cw, pc - pm[p - 1], tt);
+          tt = fmaf(ce, pc - pm[p + 1], tt);
+          tt = fmaf(cs, pc - pm[p - px], tt);
+          tt = fmaf(cn, pc - pm[p + px], tt);
+          tt = fmaf(cz, pc - pz, tt);
           q = vol * tt;
         }
         b.q32[r][c] = q;

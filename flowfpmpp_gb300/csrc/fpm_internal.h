@@ -118,7 +118,8 @@ struct MixedGrid {
 MixedGrid mixed_grid(int nx, int ny, int nz, int kc);
 struct MixedVecs {
   int nrhs;
-  const float *diag, *rdiag;         // FP32 operator, MixedGrid layout
+  const float *wall, *rdiag;         // FP32 operator, MixedGrid layout: wall = sum of the
+                                     // coefficients towards solid neighbours (-1 in solid cells)
   const float *cw, *ce, *dx;         // x-axis: row layout (index 3 + i)
   const float *cs, *cn, *dy;         // y-axis: index j - 1
   const float *cb, *ct, *dz;         // z-axis: index k - 1
@@ -140,6 +141,8 @@ struct DPtr4 {
   double* p[kMaxRhs];
 };
 cudaError_t launch_mx_layout(const MixedGrid& G, const double* a, float* b, cudaStream_t st);
+cudaError_t launch_mx_wall(const MixedGrid& G, const Dims& d, const int32_t* solid, const Coefs& c, float* wall,
+                           cudaStream_t st);
 cudaError_t launch_mx_row(int n, int len, const double* a, float* b, cudaStream_t st);
 cudaError_t launch_mx_convert(const double* a, float* b, long long n, cudaStream_t st);
 cudaError_t launch_mx_start(const MixedGrid& G, const MixedVecs& v, const DPtr4& rv64, const MixedScale& sc,
@@ -170,6 +173,8 @@ struct Batch2 {
   // operator and solution (two directions)
   double *src[2], *diag, *rdiag, *phi[2], *phi_best[2], *r64[2];
   float *diag32, *rdiag32, *r32[2], *p32[2], *q32[2], *e32[2];
+  float *wall32;                      // per cell: sum of coefficients towards solid neighbours, -1 in solid
+  float *cw32, *ce32, *cs32, *cn32;   // FP32 axis coefficients (x pools at ox + i - 1, y pools at oy + j - 1)
   // partition
   double *nxf, *nyf, *omega, *gpx[2], *gpy[2], *vif[2], *terms;
   // per (frame, direction) scalars, index 2*f + r
@@ -237,11 +242,14 @@ int operator_residual_noalloc(const double* phi, const double* src, const double
 void note_launch();
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
+// weighted: src is already a volume-weighted vector (a residual b - A phi)
+// instead of the source; accumulate: phi += gamma y instead of phi = gamma y.
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,
                                 float* mx, float* my, float* mz, float* b, double* bmax, const RedBuf& rb,
-                                cudaStream_t st);
+                                cudaStream_t st, int weighted = 0);
 cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src, const double* diag, const Coefs& c,
-                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st);
+                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st,
+                               int weighted = 0, int accumulate = 0);
 cudaError_t launch_energy(const Dims& d, const double* phi, const double* src, const double* diag, const Coefs& c,
                           const Axes& ax, double* out2, const RedBuf& rb, cudaStream_t st);
 namespace net {

@@ -16,11 +16,14 @@
 // chunk of kc planes in k, keeping the planes k-1 and k of the search
 // direction in registers (the stencil's z neighbours); x neighbours across
 // groups come from the adjacent lane by shuffle.
+#include <cstdlib>
+
 #include "fpm_internal.h"
 
 namespace fpm {
 
-// Error-free f32 pair accumulator for dot products.
+// f32 pair accumulator for dot products: a per-thread running sum carried
+// with its rounding error (TwoSum), combined across the grid in FP64.
 struct F2Acc {
   float s = 0.f, e = 0.f;
   __device__ __forceinline__ void add_prod(float a, float b) {
@@ -31,11 +34,16 @@ struct F2Acc {
     e += ((s - (t - bb)) + (p - bb)) + pe;
     s = t;
   }
+  __device__ __forceinline__ void add(float p) {  // error-free s + p
+    const float t = s + p;
+    const float bb = t - s;
+    e += (s - (t - bb)) + (p - bb);
+    s = t;
+  }
+  // The four products of one float4 group are summed in FP32 (one rounding
+  // each, relative 1e-7 of the group) and the group sum is added error-free.
   __device__ __forceinline__ void add4(const float4& a, const float4& b) {
-    add_prod(a.x, b.x);
-    add_prod(a.y, b.y);
-    add_prod(a.z, b.z);
-    add_prod(a.w, b.w);
+    add(fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x))));
   }
   __device__ __forceinline__ double value() const { return (double)s + (double)e; }
 };
@@ -76,6 +84,43 @@ __global__ void k_mx_layout(MixedGrid G, const double* __restrict__ a, float* __
       vv[c] = i <= G.nx ? (float)a[(i - 1) + (long long)G.nx * ((t.j - 1) + (long long)G.ny * (k - 1))] : 0.f;
     }
     st4(b + base, v);
+  }
+}
+
+// wall = sum of the coefficients of the faces towards solid neighbours inside
+// the grid (exactly 0 for a cell with only fluid neighbours), -1 in solid
+// cells.  With it the stencil is evaluated in difference form,
+// V (sum_nb c (p - p_nb) - wall p), which equals V (diag p - sum_nb c p_nb)
+// (solid neighbours hold p = 0) but keeps FP32 rounding relative to the
+// result instead of to the diagonal term when p is smooth.
+__global__ void k_mx_wall(MixedGrid G, Dims d, const int32_t* __restrict__ solid, Coefs cf, float* __restrict__ w) {
+  const MxPos t = mx_pos(G);
+  if (!t.live) return;
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+    float4 v;
+    float* vv = &v.x;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int i = 4 * t.g + 1 + c, j = t.j;
+      float x = 0.f;
+      if (i <= G.nx) {
+        if (solid[d.ph(i, j, k)] != 0) {
+          x = -1.f;
+        } else {
+          double s = 0.0;
+          if (solid[d.ph(i - 1, j, k)] != 0) s += cf.cw[i - 1];
+          if (solid[d.ph(i + 1, j, k)] != 0) s += cf.ce[i - 1];
+          if (solid[d.ph(i, j - 1, k)] != 0) s += cf.cs[j - 1];
+          if (solid[d.ph(i, j + 1, k)] != 0) s += cf.cn[j - 1];
+          if (k > 1 && solid[d.ph(i, j, k - 1)] != 0) s += cf.cb[k - 1];
+          if (k < G.nz && solid[d.ph(i, j, k + 1)] != 0) s += cf.ct[k - 1];
+          x = (float)s;
+        }
+      }
+      vv[c] = x;
+    }
+    st4(w + base, v);
   }
 }
 
@@ -143,9 +188,8 @@ __global__ void __launch_bounds__(128) k_mx_start(MixedGrid G, MixedVecs v, DPtr
   }
 }
 
-// q = V (diag p - sum c p_nb) on diag > 0 (same FP32 operation order for
-// every cell: centre, west, east, south, north, bottom, top, then the volume),
-// pq = p.q, alpha = rz / pq.
+// q = V (sum_nb c (p - p_nb) - wall p) on fluid cells (the difference form of
+// V (diag p - sum c p_nb)), pq = p.q, alpha = rz / pq.
 template <int NR>
 __global__ void __launch_bounds__(128, 4) k_mx_spmv(MixedGrid G, MixedVecs v, MixedScalars* S, RedBuf rb) {
   int act[kMaxRhs];
@@ -186,9 +230,9 @@ __global__ void __launch_bounds__(128, 4) k_mx_spmv(MixedGrid G, MixedVecs v, Mi
     const float cb = __ldg(v.cb + k - 1), ct = __ldg(v.ct + k - 1), dz = __ldg(v.dz + k - 1);
     // Phase 1: every load of this plane (read-only path, no aliasing with the
     // q stores below), so they are all in flight together.
-    float4 dg = zero4(), pt[NR], ps[NR], pn[NR];
+    float4 dg = make_float4(-1.f, -1.f, -1.f, -1.f), pt[NR], ps[NR], pn[NR];
     float lft[NR], rgt[NR];
-    if (t.live) dg = ldg4(v.diag + base);
+    if (t.live) dg = ldg4(v.wall + base);
 #pragma unroll
     for (int m = 0; m < NR; m++) {
       pt[m] = pc[m];
@@ -222,14 +266,15 @@ __global__ void __launch_bounds__(128, 4) k_mx_spmv(MixedGrid G, MixedVecs v, Mi
       float q[4];
 #pragma unroll
       for (int n = 0; n < 4; n++) {
-        float u = dgv[n] * pcv[n];
-        u = fmaf(-cwv[n], pw[n], u);
-        u = fmaf(-cev[n], pe[n], u);
-        u = fmaf(-cs, psv[n], u);
-        u = fmaf(-cn, pnv[n], u);
-        u = fmaf(-cb, pbv[n], u);
-        u = fmaf(-ct, ptv[n], u);
-        q[n] = dgv[n] > 0.f ? vv[n] * u : 0.f;
+        const float x = pcv[n];
+        float u = -dgv[n] * x;
+        u = fmaf(cwv[n], x - pw[n], u);
+        u = fmaf(cev[n], x - pe[n], u);
+        u = fmaf(cs, x - psv[n], u);
+        u = fmaf(cn, x - pnv[n], u);
+        u = fmaf(cb, x - pbv[n], u);
+        u = fmaf(ct, x - ptv[n], u);
+        q[n] = dgv[n] >= 0.f ? vv[n] * u : 0.f;
       }
       const float4 q4 = make_float4(q[0], q[1], q[2], q[3]);
       if (t.live) {
@@ -249,6 +294,107 @@ __global__ void __launch_bounds__(128, 4) k_mx_spmv(MixedGrid G, MixedVecs v, Mi
         if (!act[m]) continue;
         S->pq[m] = out[m];
         if (!(out[m] > 0) || !(S->rz[m] > 0)) {  // breakdown: stop this right-hand side's inner solve
+          S->active[m] = 0;
+          S->alpha[m] = 0;
+        } else {
+          S->alpha[m] = S->rz[m] / out[m];
+        }
+      }
+    }
+  }
+}
+
+// The same product, one right-hand side at a time: each thread marches its
+// planes once per right-hand side, so it holds a third of the state and the
+// SM runs twice the warps (the wall and coefficients come from L1 after the
+// first pass).
+template <int NR>
+__global__ void __launch_bounds__(128, 8) k_mx_spmv_seq(MixedGrid G, MixedVecs v, MixedScalars* S, RedBuf rb) {
+  int act[kMaxRhs];
+  bool any = false;
+#pragma unroll
+  for (int m = 0; m < kMaxRhs; m++) {
+    act[m] = m < v.nrhs ? S->active[m] : 0;
+    any = any || act[m];
+  }
+  if (!any) return;
+  F2Acc acc[NR];
+  const MxPos t = mx_pos(G);
+  const int lane = threadIdx.x;
+  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
+  const long long px = G.px, pl = G.plane;
+#pragma unroll 1
+  for (int m = 0; m < NR; m++) {
+    if (!act[m]) continue;
+    const float* p = v.p[m];
+    float4 cw = zero4(), ce = zero4(), dx = zero4(), pb = zero4(), pc = zero4();
+    float cs = 0.f, cn = 0.f, dy = 0.f;
+    if (t.live) {
+      const int o = 4 * (t.g + 1);
+      cw = ldg4(v.cw + o);
+      ce = ldg4(v.ce + o);
+      dx = ldg4(v.dx + o);
+      cs = __ldg(v.cs + t.j - 1);
+      cn = __ldg(v.cn + t.j - 1);
+      dy = __ldg(v.dy + t.j - 1);
+      pc = ldg4(p + t.base);
+      pb = t.k0 > 1 ? ldg4(p + t.base - pl) : pc;
+    }
+    long long base = t.base;
+    for (int k = t.k0; k <= t.k1; k++, base += pl) {
+      const float cb = __ldg(v.cb + k - 1), ct = __ldg(v.ct + k - 1), dz = __ldg(v.dz + k - 1);
+      float4 dg = make_float4(-1.f, -1.f, -1.f, -1.f), pt = pc, ps = zero4(), pn = zero4();
+      float lft = 0.f, rgt = 0.f;
+      if (t.live) {
+        dg = ldg4(v.wall + base);
+        if (k < G.nz) pt = ldg4(p + base + pl);
+        ps = ldg4(p + base - px);
+        pn = ldg4(p + base + px);
+        if (lane == 0) lft = __ldg(p + base - 1);
+        if (fetch_right) rgt = __ldg(p + base + 4);
+      }
+      float left = __shfl_up_sync(0xffffffffu, pc.w, 1);
+      float right = __shfl_down_sync(0xffffffffu, pc.x, 1);
+      if (lane == 0) left = lft;
+      if (fetch_right) right = rgt;
+      const float dyz = dy * dz;
+      const float pw[4] = {left, pc.x, pc.y, pc.z}, pe[4] = {pc.y, pc.z, pc.w, right};
+      const float pcv[4] = {pc.x, pc.y, pc.z, pc.w}, psv[4] = {ps.x, ps.y, ps.z, ps.w},
+                  pnv[4] = {pn.x, pn.y, pn.z, pn.w}, pbv[4] = {pb.x, pb.y, pb.z, pb.w},
+                  ptv[4] = {pt.x, pt.y, pt.z, pt.w}, dgv[4] = {dg.x, dg.y, dg.z, dg.w},
+                  cwv[4] = {cw.x, cw.y, cw.z, cw.w}, cev[4] = {ce.x, ce.y, ce.z, ce.w},
+                  dxv[4] = {dx.x, dx.y, dx.z, dx.w};
+      float q[4];
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        const float x = pcv[n];
+        float u = -dgv[n] * x;
+        u = fmaf(cwv[n], x - pw[n], u);
+        u = fmaf(cev[n], x - pe[n], u);
+        u = fmaf(cs, x - psv[n], u);
+        u = fmaf(cn, x - pnv[n], u);
+        u = fmaf(cb, x - pbv[n], u);
+        u = fmaf(ct, x - ptv[n], u);
+        q[n] = dgv[n] >= 0.f ? (dxv[n] * dyz) * u : 0.f;
+      }
+      const float4 q4 = make_float4(q[0], q[1], q[2], q[3]);
+      if (t.live) {
+        st4(v.q[m] + base, q4);
+        acc[m].add4(pc, q4);
+      }
+      pb = pc;
+      pc = pt;
+    }
+  }
+  double s[kMaxRhs], mm[1] = {0.0}, out[kMaxRhs];
+#pragma unroll
+  for (int m = 0; m < kMaxRhs; m++) s[m] = m < NR ? acc[m < NR ? m : 0].value() : 0.0;
+  if (grid_reduce<kMaxRhs, 0>(s, mm, rb.partials, rb.ticket, out)) {
+    if (lin_tid() == 0) {
+      for (int m = 0; m < kMaxRhs; m++) {
+        if (!act[m]) continue;
+        S->pq[m] = out[m];
+        if (!(out[m] > 0) || !(S->rz[m] > 0)) {
           S->active[m] = 0;
           S->alpha[m] = 0;
         } else {
@@ -410,6 +556,11 @@ cudaError_t launch_mx_layout(const MixedGrid& G, const double* a, float* b, cuda
   k_mx_layout<<<mx_grid(G), dim3(32, 4), 0, st>>>(G, a, b); note_launch();
   return cudaGetLastError();
 }
+cudaError_t launch_mx_wall(const MixedGrid& G, const Dims& d, const int32_t* solid, const Coefs& c, float* wall,
+                           cudaStream_t st) {
+  k_mx_wall<<<mx_grid(G), dim3(32, 4), 0, st>>>(G, d, solid, c, wall); note_launch();
+  return cudaGetLastError();
+}
 cudaError_t launch_mx_row(int n, int len, const double* a, float* b, cudaStream_t st) {
   k_mx_row<<<(len + 255) / 256, 256, 0, st>>>(n, len, a, b); note_launch();
   return cudaGetLastError();
@@ -429,11 +580,24 @@ cudaError_t launch_mx_start(const MixedGrid& G, const MixedVecs& v, const DPtr4&
 cudaError_t launch_mx_iteration(const MixedGrid& G, const MixedVecs& v, MixedScalars* S, const RedBuf& rb,
                                 cudaStream_t st) {
   const dim3 g = mx_grid(G), b(32, 4);
-  switch (v.nrhs) {
-    case 1: k_mx_spmv<1><<<g, b, 0, st>>>(G, v, S, rb); break;
-    case 2: k_mx_spmv<2><<<g, b, 0, st>>>(G, v, S, rb); break;
-    case 3: k_mx_spmv<3><<<g, b, 0, st>>>(G, v, S, rb); break;
-    default: k_mx_spmv<4><<<g, b, 0, st>>>(G, v, S, rb); break;
+  static const int seq = [] {
+    const char* e = std::getenv("FPM_MIXED_SPMV");
+    return (e && e[0] == '1') ? 1 : 0;
+  }();
+  if (seq) {
+    switch (v.nrhs) {
+      case 1: k_mx_spmv_seq<1><<<g, b, 0, st>>>(G, v, S, rb); break;
+      case 2: k_mx_spmv_seq<2><<<g, b, 0, st>>>(G, v, S, rb); break;
+      case 3: k_mx_spmv_seq<3><<<g, b, 0, st>>>(G, v, S, rb); break;
+      default: k_mx_spmv_seq<4><<<g, b, 0, st>>>(G, v, S, rb); break;
+    }
+  } else {
+    switch (v.nrhs) {
+      case 1: k_mx_spmv<1><<<g, b, 0, st>>>(G, v, S, rb); break;
+      case 2: k_mx_spmv<2><<<g, b, 0, st>>>(G, v, S, rb); break;
+      case 3: k_mx_spmv<3><<<g, b, 0, st>>>(G, v, S, rb); break;
+      default: k_mx_spmv<4><<<g, b, 0, st>>>(G, v, S, rb); break;
+    }
   }
   note_launch();
   switch (v.nrhs) {
