@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -13,6 +14,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <utility>
 #include <vector>
@@ -525,6 +527,13 @@ static const double kUpdateGain = env_double("FPM_MIXED_UPDATE_GAIN", 1e300);
 static const int kUpdateMax = (int)env_double("FPM_MIXED_UPDATE_MAX", 1000);
 constexpr double kBlowup = 4.0;
 constexpr int kStallUpdates = 4;
+// FP32 stagnation: kSlowUpdates updates in a row that each gain less than
+// a factor kSlowGain hand the right-hand side to FP64 PCG from its current
+// phi (on strongly stretched grids the FP32 iteration cannot resolve the
+// remaining error: its rounding relative to the operator grows with the
+// condition number).
+constexpr double kSlowGain = 2.0;
+constexpr int kSlowUpdates = 2;
 // Planes per thread in the FP32 kernels (FPM_MIXED_KCHUNK overrides).
 static int mixed_kchunk() {
   static int v = -1;
@@ -535,39 +544,11 @@ static int mixed_kchunk() {
   return v;
 }
 
-static bool learned_refine() {
-  static int v = -1;
-  if (v < 0) {
-    const char* e = std::getenv("FPM_LEARNED_REFINE");
-    v = (e && e[0] == '1') ? 1 : 0;
-  }
-  return v == 1;
-}
-
 static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
                         const double* rdiag, const int32_t* solid, const Axes& ax, const Coefs& c, double tol,
                         int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st,
-                        void* net = nullptr) {
+                        int* to_fp64 = nullptr) {
   const long long np = d.npad();
-  // Network correction steps inside the refinement (FPM_LEARNED_REFINE=1 with
-  // a network): at every residual replacement, phi += gamma net(r), gamma
-  // the energy-optimal step, then the FP32 iteration restarts from the new
-  // residual.
-  struct NetBufs {
-    uint8_t* fluid = nullptr;
-    float *mx = nullptr, *my = nullptr, *mz = nullptr, *b = nullptr, *y = nullptr;
-    double* sc = nullptr;
-  } nb;
-  const bool refine = net && learned_refine();
-  if (refine) {
-    nb.fluid = A.get<uint8_t>(d.ncell());
-    nb.mx = A.get<float>(d.nx);
-    nb.my = A.get<float>(d.ny);
-    nb.mz = A.get<float>(d.nz);
-    nb.b = A.get<float>(d.ncell());
-    nb.y = A.get<float>(d.ncell());
-    nb.sc = A.get<double>(4);
-  }
   const MixedGrid G = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk());
   MixedVecs v;
   std::memset(&v, 0, sizeof(v));
@@ -646,7 +627,9 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
   } hf{hms};
 
   double res[kMaxRhs], best[kMaxRhs], prev[kMaxRhs], scale[kMaxRhs];
-  int stall[kMaxRhs] = {}, since[kMaxRhs] = {}, done_at[kMaxRhs] = {-1, -1, -1, -1};
+  int stall[kMaxRhs] = {}, since[kMaxRhs] = {}, done_at[kMaxRhs] = {-1, -1, -1, -1}, slow[kMaxRhs] = {};
+  if (to_fp64)
+    for (int m = 0; m < nrhs; m++) to_fp64[m] = 0;
   bool live[kMaxRhs] = {};
   MixedScale sc;
   std::memset(&sc, 0, sizeof(sc));
@@ -705,29 +688,19 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
           res[m] = true_res(m);
           sc.pmul[m] = 0.0;
         }
-        if (refine && res[m] > tol) {
-          CUDA_TRY(launch_learn_inputs(d, r64.p[m], diag, ax, nb.fluid, nb.mx, nb.my, nb.mz, nb.b, nb.sc + 2, cm.rb,
-                                       st, 1));
-          std::string err;
-          const int rc = net::forward_into(net, d.nx, d.ny, d.nz, nb.fluid, nb.mx, nb.my, nb.mz, nb.b, nb.y, st, &err);
-          if (rc != FPM_OK) throw Error{rc, err};
-          CUDA_TRY(launch_learn_apply(d, nb.y, r64.p[m], diag, c, ax, phi[m], nb.sc, cm.rb, st, 1, 1));
-          const double before = res[m];
-          res[m] = true_res(m);
-          sc.pmul[m] = 0.0;
-          if (verbose())
-            std::fprintf(stderr, "fpm pcg_mixed: rhs %d network step residual %.3e -> %.3e\n", m, before, res[m]);
-        }
         stall[m] = res[m] < 0.99 * best[m] ? 0 : stall[m] + 1;
         if (res[m] < best[m]) {
           best[m] = res[m];
           CUDA_TRY(cudaMemcpyAsync(best_phi[m], phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
         }
         const bool restart = !(res[m] < kUpdateGain * prev[m]);
+        slow[m] = res[m] * kSlowGain > prev[m] ? slow[m] + 1 : 0;
         prev[m] = res[m];
-        if (!(res[m] > tol) || !(res[m] == res[m]) || stall[m] >= kStallUpdates) {
+        const bool hand_over = to_fp64 && slow[m] >= kSlowUpdates && res[m] > tol;
+        if (!(res[m] > tol) || !(res[m] == res[m]) || stall[m] >= kStallUpdates || hand_over) {
           live[m] = false;
           done_at[m] = total;
+          if (hand_over) to_fp64[m] = 1;
           sc.in_set[m] = 0;
           if (!(res[m] <= best[m]))  // finish on the best iterate
             CUDA_TRY(cudaMemcpyAsync(phi[m], best_phi[m], np * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -847,8 +820,23 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
     if (a0.method == FPM_METHOD_PCG_MIXED) {
       double* phis[kMaxRhs] = {};
       for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
+      int to64[kMaxRhs] = {};
       mixed_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps,
-                  st, net);
+                  st, to64);
+      // right-hand sides whose FP32 iteration stagnated: FP64 PCG from the
+      // current phi (which the reference's PCG takes as its initial guess)
+      for (int m = 0; m < nrhs; m++) {
+        if (!to64[m]) continue;
+        SolveArgs a = args[m];
+        a.method = FPM_METHOD_PCG;
+        a.max_sweeps = a0.max_sweeps > sweeps[m] ? a0.max_sweeps - sweeps[m] : 1;
+        if (verbose()) std::fprintf(stderr, "fpm pcg_mixed: rhs %d hands over to FP64 PCG after %d iterations\n", m, sweeps[m]);
+        CUDA_TRY(launch_init_fields(d, a.solid, a.phi, next, st));
+        CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
+        int extra = 0;
+        pcg_loop(a, d, next, src[m], diag, rdiag, c, A, cm, &extra, st);
+        sweeps[m] += extra;
+      }
     } else {
       for (int m = 0; m < nrhs; m++) {
         const SolveArgs& a = args[m];
@@ -1821,7 +1809,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     long long total = 0;
     ChunkGraphs graphs(3);
     std::vector<double> best(res), prev(res), pmul(nq, 0.0), rz(nq), rz0(nq);
-    std::vector<int> live(nq), since(nq, 0), keepv(nq, 0);
+    std::vector<int> live(nq), since(nq, 0), keepv(nq, 0), slow(nq, 0), to64(nq, 0), extra_its(nq, 0);
     bool any = false;
     for (size_t q = 0; q < nq; q++) {
       live[q] = res[q] > tolerance && res[q] == res[q];
@@ -1924,11 +1912,14 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
           if (verbose_level() >= 2)
             std::fprintf(stderr, "fpm frames: q %zu iterations %lld residual %.3e previous %.3e %s%s\n", q, total,
                          res[q], prev[q], act[q] ? "" : "breakdown ", restart ? "restart" : "keep");
+          slow[q] = res[q] * kSlowGain > prev[q] ? slow[q] + 1 : 0;
           prev[q] = res[q];
-          if (!(res[q] > tolerance) || !(res[q] == res[q]) || stall[q] >= kStallUpdates) {
+          const bool hand_over = slow[q] >= kSlowUpdates && res[q] > tolerance;
+          if (!(res[q] > tolerance) || !(res[q] == res[q]) || stall[q] >= kStallUpdates || hand_over) {
             live[q] = 0;
             set[q] = 0;
             act[q] = 0;
+            if (hand_over) to64[q] = 1;
             if (!(res[q] <= best[q])) keepv[q] = 2;  // finish on the best iterate
           } else {
             const double ns = res[q] > 0 ? 1.0 / res[q] : 1.0;
@@ -1968,6 +1959,91 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       push_set();
       CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
     }
+    // (frame, direction) pairs whose FP32 iteration stagnated: FP64 PCG of
+    // that frame alone (the reference's 3-D solve with nz = 2), from its
+    // current phi, with the outer face data of its compatibility correction.
+    {
+      bool any64 = false;
+      for (size_t q = 0; q < nq; q++) any64 = any64 || to64[q];
+      if (any64) {
+        Trace t64("frames: FP64 PCG hand-over");
+        std::vector<double> hcorr(nq);
+        pull(hcorr.data(), b.corr, nq * sizeof(double));
+        const double zc2[2] = {0.25, 0.75}, dz2[2] = {0.5, 0.5};
+        double* dzc = A.upload(zc2, 2);
+        double* ddz = A.upload(dz2, 2);
+        std::vector<SolveArgs> jobs;
+        std::vector<size_t> job_q;
+        for (int f = 0; f < nframes; f++) {
+          for (int r = 0; r < 2; r++) {
+            const size_t q = 2 * (size_t)f + r;
+            if (!to64[q]) continue;
+            const Frame2& F = fr[f];
+            const int fnx = F.nx, fny = F.ny;
+            const double cr = hcorr[q];
+            std::vector<double> xl((size_t)fny * 2, -cr), xh((size_t)fny * 2, cr), yl((size_t)fnx * 2, -cr),
+                yh((size_t)fnx * 2, cr), zl((size_t)fnx * fny, -cr), zh((size_t)fnx * fny, cr);
+            SolveArgs a;
+            a.phi = b.phi[r] + F.opad;
+            double* zero_rhs = A.get<double>((size_t)fnx * fny * 2);
+            CUDA_TRY(cudaMemsetAsync(zero_rhs, 0, (size_t)fnx * fny * 2 * sizeof(double), st));
+            a.rhs = zero_rhs;
+            a.solid = b.solid3 + F.opad;
+            a.bg[0] = r == 0 ? 1.0 : 0.0;
+            a.bg[1] = r == 1 ? 1.0 : 0.0;
+            a.bg[2] = 0.0;
+            a.f = Faces{A.upload(xl.data(), xl.size()), A.upload(xh.data(), xh.size()), A.upload(yl.data(), yl.size()),
+                        A.upload(yh.data(), yh.size()), A.upload(zl.data(), zl.size()), A.upload(zh.data(), zh.size())};
+            a.ax = Axes{b.xc + F.ox, b.yc + F.oy, dzc, b.dx + F.ox, b.dy + F.oy, ddz};
+            a.nx = fnx;
+            a.ny = fny;
+            a.nz = 2;
+            a.tol = tolerance;
+            a.max_sweeps = max_sweeps;
+            a.ci = check_interval;
+            a.method = FPM_METHOD_PCG;
+            jobs.push_back(a);
+            job_q.push_back(q);
+          }
+        }
+        CUDA_TRY(cudaStreamSynchronize(st));
+        // The frames are small next to the GPU, so several of them are solved
+        // at once: host worker threads, one stream each.
+        int dev = 0;
+        CUDA_TRY(cudaGetDevice(&dev));
+        const int nworkers = (int)std::min<size_t>(jobs.size(), 12);
+        std::vector<int> sws(jobs.size(), 0);
+        std::vector<double> rrs(jobs.size(), 0.0);
+        std::vector<std::string> errs(nworkers);
+        std::vector<int> codes(nworkers, FPM_OK);
+        std::atomic<size_t> next_job{0};
+        std::vector<std::thread> pool;
+        for (int w = 0; w < nworkers; w++) {
+          pool.emplace_back([&, w] {
+            cudaStream_t ws = nullptr;
+            try {
+              CUDA_TRY(cudaSetDevice(dev));
+              CUDA_TRY(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking));
+              for (size_t j = next_job++; j < jobs.size(); j = next_job++)
+                solve_multi_dev(1, &jobs[j], &sws[j], &rrs[j], ws);
+            } catch (const Error& e) {
+              codes[w] = e.code;
+              errs[w] = e.msg;
+            }
+            if (ws) cudaStreamDestroy(ws);
+          });
+        }
+        for (auto& t : pool) t.join();
+        for (int w = 0; w < nworkers; w++)
+          if (codes[w] != FPM_OK) throw Error{codes[w], errs[w]};
+        for (size_t j = 0; j < jobs.size(); j++) {
+          extra_its[job_q[j]] = sws[j];
+          if (verbose())
+            std::fprintf(stderr, "fpm frames: frame %zu direction %zu FP64 PCG %d iterations, residual %.3e\n",
+                         job_q[j] / 2, job_q[j] % 2, sws[j], rrs[j]);
+        }
+      }
+    }
     Trace tg("frames: gauge and partition");
     CUDA_TRY(launch_k_b2_gauge_sum(dfr, dtf, ntiles, b, st));
     CUDA_TRY(launch_k_b2_gauge_sub(dfr, dtf, ntiles, b, st));
@@ -1978,6 +2054,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     CUDA_TRY(launch_k_b2_part2(dfr, dtf, ntiles, b, st));
     pull(residual, b.res, nq * sizeof(double));
     pull(sweeps, b.iters, nq * sizeof(int));
+    for (size_t q = 0; q < nq; q++) sweeps[q] += extra_its[q];
     pull(terms, b.terms, 8 * (size_t)nframes * sizeof(double));
     if (phi_out) {
       for (int f = 0; f < nframes; f++) {

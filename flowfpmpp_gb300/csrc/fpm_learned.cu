@@ -7,10 +7,6 @@
 // (w_min = smallest cell width of the grid), and b = V src (the PCG right-hand
 // side) divided by max |b|.
 //
-// (The same kernels take an already volume-weighted residual r = b - A phi
-// in place of V src, and can add gamma y to phi instead of replacing it: the
-// network as a correction step inside the refinement.)
-//
 // The network output y (FP32) is used as phi0 = gamma y_f, y_f = y on fluid
 // cells and 0 elsewhere, with gamma = (y_f . b) / (y_f . A y_f): the multiple
 // of y_f closest to the solution in the energy norm.  The guess is kept only
