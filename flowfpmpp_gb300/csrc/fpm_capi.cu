@@ -736,11 +736,125 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
   for (int m = 0; m < nrhs; m++) sweeps_out[m] = done_at[m] >= 0 ? done_at[m] : total;
 }
 
+// FP32 PCG preconditioned by the aggregation multigrid V-cycle of fpm_mg.cu,
+// in the same FP64 refinement as mixed_solve: each outer step loads the
+// projected FP64 true residual (scaled to unit max-norm), runs PCG until its
+// preconditioned residual norm r.z has dropped by kMgDrop^2 (or kMgInnerMax
+// iterations), adds the correction to phi in FP64 and recomputes the true
+// residual; convergence is the reference's max-norm test.  The right-hand
+// sides are solved one after the other.
+constexpr double kMgDrop = 1e-4;
+constexpr int kMgInnerMax = 400;
+
+static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
+                     const double* rdiag, const int32_t* solid, const Axes& ax, const Coefs& c, double tol,
+                     int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st) {
+  Trace tr("multigrid setup");
+  MgHierarchy H;
+  std::memset(&H, 0, sizeof(H));
+  H.nu = (int)env_double("FPM_MG_NU", 1);
+  H.omega = (float)env_double("FPM_MG_OMEGA", 0.7);
+  H.coarse_sweeps = (int)env_double("FPM_MG_COARSE_SWEEPS", 30);
+  int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (;;) {
+    MgLevel& L = H.lv[H.nlev];
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = nz;
+    const long long n = L.n();
+    L.te = A.get<float>(n);
+    L.tn = A.get<float>(n);
+    L.tt = A.get<float>(n);
+    L.dinv = A.get<float>(n);
+    L.x = A.get<float>(n);
+    L.b = A.get<float>(n);
+    L.r = A.get<float>(n);
+    L.t = A.get<float>(n);
+    H.nlev++;
+    if (n <= 1024 || H.nlev == kMgMaxLevels) break;
+    nx = (nx + 1) / 2;
+    ny = (ny + 1) / 2;
+    nz = (nz + 1) / 2;
+  }
+  if (H.lv[H.nlev - 1].n() > 1024) throw Error{FPM_E_LIMIT, "grid too large for the multigrid hierarchy"};
+  CUDA_TRY(mg_setup(H, d, solid, ax, st));
+  const long long n0 = H.lv[0].n();
+  MgVecs v;
+  v.r = A.get<float>(n0);
+  v.z = A.get<float>(n0);
+  v.p = A.get<float>(n0);
+  v.q = A.get<float>(n0);
+  v.e = A.get<float>(n0);
+  RedBuf rb;
+  rb.max_blocks = mg_grid_blocks(H.lv[0]);
+  rb.partials = A.get<double>((size_t)rb.max_blocks);
+  rb.ticket = A.get<unsigned int>(1);
+  CUDA_TRY(cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned int), st));
+  MgScalars* S = A.get<MgScalars>(1);
+  double* r64 = A.get<double>(d.ncell());
+  SolveScalars* S64 = A.get<SolveScalars>(1);
+  CUDA_TRY(cudaMemsetAsync(S64, 0, sizeof(SolveScalars), st));
+  MgScalars* hS = nullptr;
+  CUDA_TRY(cudaMallocHost(&hS, sizeof(MgScalars)));
+  struct HostFree {
+    void* p;
+    ~HostFree() { cudaFreeHost(p); }
+  } hf{hS};
+  const int chunk_len = ci < 1 ? 1 : (ci > 50 ? 50 : ci);
+  for (int m = 0; m < nrhs; m++) {
+    Trace ti("multigrid PCG");
+    auto true_res = [&]() {
+      CUDA_TRY(launch_true_residual(d, phi[m], src[m], diag, rdiag, r64, nullptr, c, ax, 0, S64, cm.rb, st));
+      return read_scalars(S64, st).res;
+    };
+    double res = true_res(), best = res;
+    int total = 0, stall = 0;
+    ChunkGraphs graphs(4 + (H.nlev - 1) * (2 * H.nu + 3) + 1);
+    while (res > tol && res == res && total < max_sweeps) {
+      const double scale = res > 0 ? 1.0 / res : 1.0;
+      MgScalars h0;
+      std::memset(&h0, 0, sizeof(h0));
+      h0.tol2 = kMgDrop * kMgDrop;
+      CUDA_TRY(cudaMemcpyAsync(S, &h0, sizeof(MgScalars), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(mg_pcg_start(H, r64, scale, v, S, rb, st));
+      int inner = 0;
+      for (;;) {
+        int chunk = chunk_len;
+        if (chunk > max_sweeps - total) chunk = max_sweeps - total;
+        if (chunk <= 0) break;
+        {
+          TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
+          graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
+        }
+        CUDA_TRY(cudaMemcpyAsync(hS, S, sizeof(MgScalars), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        inner = hS->iters;
+        if (!hS->active || inner >= kMgInnerMax) break;
+      }
+      total += inner;
+      CUDA_TRY(mg_pcg_apply(H, d, v, scale, phi[m], st));
+      const double prev = res;
+      res = true_res();
+      if (verbose())
+        std::fprintf(stderr, "fpm pcg_mg: rhs %d inner %d total %d residual %.3e\n", m, inner, total, res);
+      if (res < 0.99 * best) {
+        best = res;
+        stall = 0;
+      } else if (++stall >= kStallUpdates) {
+        break;
+      }
+      if (inner == 0 && !(res < prev)) break;  // no progress possible
+    }
+    sweeps_out[m] = total;
+  }
+}
+
 // solve_stairstep_poisson_3d (src/fpm_stairstep_mpi_3d.f90:106-330), device
 // arrays, for nrhs right-hand sides that share solid and axes.  FP64 methods
 // solve them one after the other; FPM_METHOD_PCG_MIXED solves them together.
 static bool valid_method(int m) {
-  return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED;
+  return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED ||
+         m == FPM_METHOD_PCG_MG;
 }
 
 // Learned initial guess for every right-hand side (see fpm_learned.cu): the
@@ -805,7 +919,7 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
   double* next = A.get<double>(d.npad());
   double* diag = A.get<double>(d.ncell());
   double* rdiag = A.get<double>(d.ncell());
-  const bool for_pcg = a0.method == FPM_METHOD_PCG || a0.method == FPM_METHOD_PCG_MIXED;
+  const bool for_pcg = a0.method == FPM_METHOD_PCG || a0.method == FPM_METHOD_PCG_MIXED || a0.method == FPM_METHOD_PCG_MG;
   double* src[kMaxRhs] = {};
   for (int m = 0; m < nrhs; m++) {
     src[m] = A.get<double>(d.ncell());
@@ -817,7 +931,11 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
   if (net) learned_guess(net, d, nrhs, args, src, diag, rdiag, c, A, cm, fallbacks, st);
   {
     Trace t1("stair-step iterations");
-    if (a0.method == FPM_METHOD_PCG_MIXED) {
+    if (a0.method == FPM_METHOD_PCG_MG) {
+      double* phis[kMaxRhs] = {};
+      for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
+      mg_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps, st);
+    } else if (a0.method == FPM_METHOD_PCG_MIXED) {
       double* phis[kMaxRhs] = {};
       for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
       int to64[kMaxRhs] = {};

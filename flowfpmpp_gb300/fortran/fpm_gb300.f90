@@ -157,6 +157,7 @@ contains
       case ('jacobi'); m = 1
       case ('jacobi_df'); m = 2
       case ('pcg_mixed'); m = 3
+      case ('pcg_mg'); m = 4
       case default; error stop 'stair-step method must be pcg or jacobi'
       end select
     end if

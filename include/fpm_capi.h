@@ -60,6 +60,8 @@ extern "C" {
                                    arithmetic with FP64 residual checks: same iteration, HBM-bound on GB300 */
 #define FPM_METHOD_PCG_MIXED 3  /* FP64 iterative refinement (true residual, max-norm test, phi update in FP64)
                                    around FP32 diagonal PCG; max_sweeps caps the FP32 iterations */
+#define FPM_METHOD_PCG_MG 4     /* the refinement of FPM_METHOD_PCG_MIXED around FP32 PCG preconditioned by an
+                                   aggregation multigrid V-cycle (no reference counterpart) */
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char* fpm_last_error(void);

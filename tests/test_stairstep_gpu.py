@@ -240,26 +240,29 @@ def test_df_tma_tile_shapes_match_fp64(gpu_lib, monkeypatch, shape, dims, kchunk
     assert np.array_equal(rdf[0], a[0]) and np.array_equal(rdf[:, 0], a[:, 0])  # halos untouched
 
 
-def test_pcg_mixed_matches_fp64_oracle(gpu_lib):
-    """FP32 PCG inside FP64 refinement reaches the same residual tolerance and
-    potentials within 1e-9 relative max-norm of the FP64 oracle."""
+@pytest.mark.parametrize("method", ["pcg_mixed", "pcg_mg"])
+def test_pcg_mixed_matches_fp64_oracle(gpu_lib, method):
+    """FP32 PCG (diagonal or multigrid preconditioner) inside FP64 refinement
+    reaches the same residual tolerance and potentials within 1e-9 relative
+    max-norm of the FP64 oracle."""
     c = stairstep_case_exact(False)
-    g = gpu_run(c, "pcg_mixed", 1e-11, 100000)
+    g = gpu_run(c, method, 1e-11, 100000)
     o = cpu_run(c, "pcg", 1e-11, 100000)
     assert g["res"] <= 2e-11
     assert rel_linf(g["phi"], o["phi"]) <= 1e-9
     assert np.abs(g["terms"][5] - o["terms"][5]).max() < 1e-8
     e = stairstep_case_exact(True)
-    ge = gpu_run(e, "pcg_mixed", 1e-10, 100000)
+    ge = gpu_run(e, method, 1e-10, 100000)
     gx, gy, gz, vortex, adv, totals = ge["terms"]
     errors, ierr = exact_expectations(e, ge["phi"], gx, gy, gz, vortex, totals)
     assert ge["res"] <= 2e-10 and errors[0] < 1e-9 and errors[1] < 1e-9 and errors[3] == 0 and ierr < 1e-10
 
 
-@pytest.mark.parametrize("method", [0, 3])
+@pytest.mark.parametrize("method", [0, 3, 4])
 def test_multi_rhs_three_influence_fields(gpu_lib, method):
     """phi_x, phi_y, phi_z of a stretched-grid sphere in one call (FP64 one
-    after the other, or mixed precision batched) against the FP64 oracle."""
+    after the other, mixed precision batched, or multigrid-preconditioned FP32)
+    against the FP64 oracle."""
     import torch
     from flowfpmpp_gb300 import stairstep as ss
     from flowfpmpp_gb300 import workloads
