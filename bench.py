@@ -21,6 +21,15 @@ C, OpenMP over z-planes, every host core) on a bounded sample of the same
 workload: the oracle is the reference arm because the reference itself is
 Fortran/OpenACC and no Fortran compiler is available.
 
+Other workloads (one GPU, a JSON line each):
+  pcg_c1, pcg_c3  phi_x, phi_y, phi_z to a 1e-10 max-norm residual with plain
+                  FP64 PCG, FP32 PCG in FP64 refinement (diagonal and multigrid
+                  preconditioners) and the learned initial guess; value is the
+                  multigrid arm's solve time
+  frames_c4       256 uneven 2-D foil frames, two potentials and the four
+                  partition terms each
+  learned_c5      the trained network as initial guess on unseen bodies
+
 Multi-GPU: replicas only (each rank solves its own copy; no collective on the
 data path); value is the sum over ranks divided by the slowest rank's time.
 """
@@ -200,8 +209,10 @@ def run_reference(args):
 # ---------------------------------------------------------------- PCG time to solution
 def run_pcg(args):
     """Three influence potentials (phi_x, phi_y, phi_z) to a 1e-10 max-norm
-    residual: plain FP64 PCG (one after the other, the reference's method) and
-    FP32 PCG in FP64 refinement batched over the three right-hand sides."""
+    residual: plain FP64 PCG (one after the other, the reference's method),
+    FP32 PCG in FP64 refinement batched over the three right-hand sides
+    (diagonal preconditioner), the same refinement with the multigrid
+    preconditioner, and both with the learned initial guess."""
     import torch
     from flowfpmpp_gb300 import build as fbuild
     fbuild.build()

@@ -748,45 +748,70 @@ constexpr int kMgInnerMax = 400;
 
 static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
                      const double* rdiag, const int32_t* solid, const Axes& ax, const Coefs& c, double tol,
-                     int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st) {
+                     int max_sweeps, int ci, Scratch& A, Common& cm, int* sweeps_out, cudaStream_t st,
+                     int* to_fp64) {
+  if (d.ncell() <= 1024) {  // too small for a coarse level: the diagonal preconditioner
+    int to64[kMaxRhs] = {};
+    mixed_solve(d, nrhs, phi, src, diag, rdiag, solid, ax, c, tol, max_sweeps, ci, A, cm, sweeps_out, st, to64);
+    for (int m = 0; m < nrhs; m++) to_fp64[m] = to64[m];
+    return;
+  }
   Trace tr("multigrid setup");
   MgHierarchy H;
   std::memset(&H, 0, sizeof(H));
   H.nu = (int)env_double("FPM_MG_NU", 1);
-  H.omega = (float)env_double("FPM_MG_OMEGA", 0.7);
-  H.coarse_sweeps = (int)env_double("FPM_MG_COARSE_SWEEPS", 30);
+  H.omega = (float)env_double("FPM_MG_OMEGA", 0.8);
+  H.coarse_sweeps = (int)env_double("FPM_MG_COARSE_SWEEPS", 40);
+  // level 0 in the mixed solver's FP32 layout (zero halo), coarse levels compact
+  H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk());
+  auto zeros = [&](long long n) {
+    float* x = A.get<float>(n);
+    CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(float), st));
+    return x;
+  };
   int nx = d.nx, ny = d.ny, nz = d.nz;
   for (;;) {
     MgLevel& L = H.lv[H.nlev];
     L.nx = nx;
     L.ny = ny;
     L.nz = nz;
-    const long long n = L.n();
-    L.te = A.get<float>(n);
-    L.tn = A.get<float>(n);
-    L.tt = A.get<float>(n);
-    L.dinv = A.get<float>(n);
-    L.x = A.get<float>(n);
-    L.b = A.get<float>(n);
-    L.r = A.get<float>(n);
-    L.t = A.get<float>(n);
+    if (H.nlev == 0) {
+      L.off = 4 + H.g0.px;
+      L.sy = H.g0.px;
+      L.sz = H.g0.plane;
+      L.alloc = H.g0.size;
+    } else {
+      L.off = 0;
+      L.sy = nx;
+      L.sz = (long long)nx * ny;
+      L.alloc = L.n();
+    }
+    L.te = zeros(L.alloc);
+    L.tn = zeros(L.alloc);
+    L.tt = zeros(L.alloc);
+    L.dinv = zeros(L.alloc);
+    L.t = zeros(L.alloc);
+    L.x = H.nlev == 0 ? nullptr : zeros(L.alloc);
+    L.b = H.nlev == 0 ? nullptr : zeros(L.alloc);
     H.nlev++;
-    if (n <= 1024 || H.nlev == kMgMaxLevels) break;
+    if (L.n() <= 1024 || H.nlev == kMgMaxLevels) break;
     nx = (nx + 1) / 2;
     ny = (ny + 1) / 2;
     nz = (nz + 1) / 2;
   }
-  if (H.lv[H.nlev - 1].n() > 1024) throw Error{FPM_E_LIMIT, "grid too large for the multigrid hierarchy"};
+  if (H.nlev < 2 || H.lv[H.nlev - 1].n() > 1024)
+    throw Error{FPM_E_LIMIT, "grid too small or too large for the multigrid hierarchy"};
+  if (H.nu != 1) throw Error{FPM_E_ARG, "the multigrid cycle uses one smoothing sweep on level 0"};
   CUDA_TRY(mg_setup(H, d, solid, ax, st));
-  const long long n0 = H.lv[0].n();
+  const long long n0 = H.lv[0].alloc;
   MgVecs v;
-  v.r = A.get<float>(n0);
-  v.z = A.get<float>(n0);
-  v.p = A.get<float>(n0);
-  v.q = A.get<float>(n0);
-  v.e = A.get<float>(n0);
+  v.r = zeros(n0);
+  v.z = zeros(n0);
+  v.p = zeros(n0);
+  v.q = zeros(n0);
+  v.e = zeros(n0);
   RedBuf rb;
-  rb.max_blocks = mg_grid_blocks(H.lv[0]);
+  rb.max_blocks = mg_grid_blocks(H.g0);
   rb.partials = A.get<double>((size_t)rb.max_blocks);
   rb.ticket = A.get<unsigned int>(1);
   CUDA_TRY(cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned int), st));
@@ -809,12 +834,16 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     };
     double res = true_res(), best = res;
     int total = 0, stall = 0;
-    ChunkGraphs graphs(4 + (H.nlev - 1) * (2 * H.nu + 3) + 1);
+    ChunkGraphs graphs(5 + (H.nlev - 2) * (2 * H.nu + 1) + 1);
     while (res > tol && res == res && total < max_sweeps) {
       const double scale = res > 0 ? 1.0 / res : 1.0;
       MgScalars h0;
       std::memset(&h0, 0, sizeof(h0));
-      h0.tol2 = kMgDrop * kMgDrop;
+      // drop by kMgDrop, or just far enough for the tolerance (with a margin
+      // of 30 for the max-norm versus the preconditioned norm)
+      const double need = tol / (30.0 * res);
+      const double drop = need > kMgDrop ? (need < 0.5 ? need : 0.5) : kMgDrop;
+      h0.tol2 = drop * drop;
       CUDA_TRY(cudaMemcpyAsync(S, &h0, sizeof(MgScalars), cudaMemcpyHostToDevice, st));
       CUDA_TRY(mg_pcg_start(H, r64, scale, v, S, rb, st));
       int inner = 0;
@@ -846,6 +875,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
       if (inner == 0 && !(res < prev)) break;  // no progress possible
     }
     sweeps_out[m] = total;
+    // stopped above the tolerance (FP32 can no longer resolve the error at
+    // the FP64 rounding floor of the residual): FP64 PCG finishes
+    to_fp64[m] = res > tol ? 1 : 0;
   }
 }
 
@@ -931,30 +963,37 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
   if (net) learned_guess(net, d, nrhs, args, src, diag, rdiag, c, A, cm, fallbacks, st);
   {
     Trace t1("stair-step iterations");
-    if (a0.method == FPM_METHOD_PCG_MG) {
-      double* phis[kMaxRhs] = {};
-      for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
-      mg_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps, st);
-    } else if (a0.method == FPM_METHOD_PCG_MIXED) {
-      double* phis[kMaxRhs] = {};
-      for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
-      int to64[kMaxRhs] = {};
-      mixed_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps,
-                  st, to64);
-      // right-hand sides whose FP32 iteration stagnated: FP64 PCG from the
-      // current phi (which the reference's PCG takes as its initial guess)
+    // right-hand sides whose FP32 iteration stagnated: FP64 PCG from the
+    // current phi (which the reference's PCG takes as its initial guess)
+    auto finish_fp64 = [&](const int* to64) {
       for (int m = 0; m < nrhs; m++) {
         if (!to64[m]) continue;
         SolveArgs a = args[m];
         a.method = FPM_METHOD_PCG;
         a.max_sweeps = a0.max_sweeps > sweeps[m] ? a0.max_sweeps - sweeps[m] : 1;
-        if (verbose()) std::fprintf(stderr, "fpm pcg_mixed: rhs %d hands over to FP64 PCG after %d iterations\n", m, sweeps[m]);
+        if (verbose())
+          std::fprintf(stderr, "fpm: rhs %d hands over to FP64 PCG after %d FP32 iterations\n", m, sweeps[m]);
         CUDA_TRY(launch_init_fields(d, a.solid, a.phi, next, st));
         CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
         int extra = 0;
         pcg_loop(a, d, next, src[m], diag, rdiag, c, A, cm, &extra, st);
         sweeps[m] += extra;
       }
+    };
+    if (a0.method == FPM_METHOD_PCG_MG) {
+      double* phis[kMaxRhs] = {};
+      for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
+      int to64[kMaxRhs] = {};
+      mg_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps, st,
+               to64);
+      finish_fp64(to64);
+    } else if (a0.method == FPM_METHOD_PCG_MIXED) {
+      double* phis[kMaxRhs] = {};
+      for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
+      int to64[kMaxRhs] = {};
+      mixed_solve(d, nrhs, phis, src, diag, rdiag, a0.solid, a0.ax, c, a0.tol, a0.max_sweeps, a0.ci, A, cm, sweeps,
+                  st, to64);
+      finish_fp64(to64);
     } else {
       for (int m = 0; m < nrhs; m++) {
         const SolveArgs& a = args[m];
@@ -1935,6 +1974,22 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       scale[q] = res[q] > 0 ? 1.0 / res[q] : 1.0;
       any = any || live[q];
     }
+    // Frame method: the batched FP32 diagonal PCG above, or (multigrid)
+    // every (frame, direction) solved on its own by the multigrid-
+    // preconditioned refinement, several at once on worker streams.
+    const int frames_mg = [] {
+      const char* e = std::getenv("FPM_FRAMES_METHOD");
+      return (e && std::strcmp(e, "batched") == 0) ? 0 : 1;
+    }();
+    int individual_method = FPM_METHOD_PCG;
+    if (frames_mg) {
+      for (size_t q = 0; q < nq; q++) {
+        to64[q] = live[q];
+        live[q] = 0;
+      }
+      any = false;
+      individual_method = FPM_METHOD_PCG_MG;
+    }
     auto push_start = [&] {
       push_set();
       CUDA_TRY(cudaMemcpyAsync(b.scale, scale.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -2077,14 +2132,16 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       push_set();
       CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
     }
-    // (frame, direction) pairs whose FP32 iteration stagnated: FP64 PCG of
-    // that frame alone (the reference's 3-D solve with nz = 2), from its
-    // current phi, with the outer face data of its compatibility correction.
+    // (frame, direction) pairs solved on their own: with the multigrid frame
+    // method all of them; otherwise those whose FP32 iteration stagnated
+    // (FP64 PCG from their current phi).  Each is the reference's 3-D solve of
+    // that frame with nz = 2 and the outer face data of its compatibility
+    // correction.
     {
       bool any64 = false;
       for (size_t q = 0; q < nq; q++) any64 = any64 || to64[q];
       if (any64) {
-        Trace t64("frames: FP64 PCG hand-over");
+        Trace t64("frames: individual solves");
         std::vector<double> hcorr(nq);
         pull(hcorr.data(), b.corr, nq * sizeof(double));
         const double zc2[2] = {0.25, 0.75}, dz2[2] = {0.5, 0.5};
@@ -2119,7 +2176,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
             a.tol = tolerance;
             a.max_sweeps = max_sweeps;
             a.ci = check_interval;
-            a.method = FPM_METHOD_PCG;
+            a.method = individual_method;
             jobs.push_back(a);
             job_q.push_back(q);
           }

@@ -244,14 +244,17 @@ void note_launch();
 // ---- aggregation multigrid preconditioner (fpm_mg.cu) ---------------------
 struct MgLevel {
   int nx, ny, nz;
+  long long off, sy, sz;       // cell (i, j, k) (0-based) at off + i + sy j + sz k
+  long long alloc;             // elements per array
   float *te, *tn, *tt, *dinv;  // face transmissibilities, inverse diagonal
-  float *x, *b, *r, *t;        // solution, right-hand side, residual, smoothing scratch
+  float *x, *b, *t;            // solution, right-hand side, smoothing scratch
   __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
 };
 constexpr int kMgMaxLevels = 16;
 struct MgHierarchy {
   int nlev;
   MgLevel lv[kMgMaxLevels];
+  MixedGrid g0;       // level 0 uses the FP32 layout of the mixed solver (float4 groups, zero halo)
   int nu;             // pre- and post-smoothing sweeps
   int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block)
   float omega;        // Jacobi weight
@@ -264,13 +267,12 @@ struct MgScalars {
   int active, dir, iters, pad;
 };
 cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const Axes& ax, cudaStream_t st);
-cudaError_t mg_vcycle(const MgHierarchy& H, const float* r, float* z, cudaStream_t st);
 cudaError_t mg_pcg_start(const MgHierarchy& H, const double* rv, double scale, MgVecs& v, MgScalars* S,
                          const RedBuf& rb, cudaStream_t st);
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, cudaStream_t st);
 cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, double scale, double* phi,
                          cudaStream_t st);
-int mg_grid_blocks(const MgLevel& L);
+int mg_grid_blocks(const MixedGrid& G);
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
 // weighted: src is already a volume-weighted vector (a residual b - A phi)

@@ -15,7 +15,9 @@
 // = P^T, a fixed number of Jacobi sweeps on the coarsest level), so it is a
 // valid preconditioner for CG.
 //
-// Vectors are FP32 in the compact cell order (x fastest) of each level.
+// Level 0 uses the FP32 layout of the mixed solver (16-byte aligned rows,
+// zero x-y halo, see MixedGrid) and float4 kernels that march through k; the
+// coarse levels are compact (x fastest) and use one thread per cell.
 #include "fpm_internal.h"
 
 namespace fpm {
@@ -23,7 +25,7 @@ namespace fpm {
 namespace {
 
 __device__ __forceinline__ long long ix(const MgLevel& L, int i, int j, int k) {
-  return i + (long long)L.nx * (j + (long long)L.ny * k);
+  return L.off + i + L.sy * j + L.sz * k;
 }
 
 #define MG_CELLS(L)                                                                       \
@@ -72,8 +74,8 @@ __global__ void k_mg_coarsen(MgLevel F, MgLevel C) {
 __device__ __forceinline__ float face_sum(const MgLevel& L, int i, int j, int k, long long c) {
   float d = L.te[c] + L.tn[c] + L.tt[c];
   if (i > 0) d += L.te[c - 1];
-  if (j > 0) d += L.tn[c - L.nx];
-  if (k > 0) d += L.tt[c - (long long)L.nx * L.ny];
+  if (j > 0) d += L.tn[c - L.sy];
+  if (k > 0) d += L.tt[c - L.sz];
   return d;
 }
 
@@ -88,15 +90,15 @@ __global__ void k_mg_dinv(MgLevel L) {
 // (A x)_c in face form.
 __device__ __forceinline__ float apply_a(const MgLevel& L, const float* __restrict__ x, int i, int j, int k,
                                         long long c) {
-  const long long pl = (long long)L.nx * L.ny;
+  const long long sy = L.sy, sz = L.sz;
   const float xc = x[c];
   float u = 0.f;
   if (i + 1 < L.nx) u = fmaf(L.te[c], xc - x[c + 1], u);
   if (i > 0) u = fmaf(L.te[c - 1], xc - x[c - 1], u);
-  if (j + 1 < L.ny) u = fmaf(L.tn[c], xc - x[c + L.nx], u);
-  if (j > 0) u = fmaf(L.tn[c - L.nx], xc - x[c - L.nx], u);
-  if (k + 1 < L.nz) u = fmaf(L.tt[c], xc - x[c + pl], u);
-  if (k > 0) u = fmaf(L.tt[c - pl], xc - x[c - pl], u);
+  if (j + 1 < L.ny) u = fmaf(L.tn[c], xc - x[c + sy], u);
+  if (j > 0) u = fmaf(L.tn[c - sy], xc - x[c - sy], u);
+  if (k + 1 < L.nz) u = fmaf(L.tt[c], xc - x[c + sz], u);
+  if (k > 0) u = fmaf(L.tt[c - sz], xc - x[c - sz], u);
   return u;
 }
 
@@ -110,30 +112,42 @@ __global__ void k_mg_smooth(MgLevel L, const float* __restrict__ x, const float*
   }
 }
 
-// r = b - A x
-__global__ void k_mg_residual(MgLevel L, const float* __restrict__ x, const float* __restrict__ b,
-                              float* __restrict__ r) {
-  MG_CELLS(L) {
-    const long long c = ix(L, i, j, k);
-    r[c] = b[c] - apply_a(L, x, i, j, k, c);
-  }
-}
-
-// bc = sum of the fine residuals of each aggregate
-__global__ void k_mg_restrict(MgLevel F, MgLevel C, const float* __restrict__ rf, float* __restrict__ bc) {
+// bc = restriction of b - A x: one thread per coarse cell sums the residuals
+// of its (up to 8) fine cells (k_mg_residual + k_mg_restrict in one pass).
+__global__ void k_mg_resrestrict(MgLevel F, MgLevel C, const float* __restrict__ x, const float* __restrict__ b,
+                                 float* __restrict__ bc) {
   MG_CELLS(C) {
     float s = 0.f;
     for (int o = 0; o < 8; o++) {
       const int fi = 2 * i + (o & 1), fj = 2 * j + ((o >> 1) & 1), fk = 2 * k + (o >> 2);
-      if (fi < F.nx && fj < F.ny && fk < F.nz) s += rf[ix(F, fi, fj, fk)];
+      if (fi < F.nx && fj < F.ny && fk < F.nz) {
+        const long long c = ix(F, fi, fj, fk);
+        s += b[c] - apply_a(F, x, fi, fj, fk, c);
+      }
     }
     bc[ix(C, i, j, k)] = s;
   }
 }
 
-// xf += xc(parent)
-__global__ void k_mg_prolong(MgLevel F, MgLevel C, const float* __restrict__ xc, float* __restrict__ xf) {
-  MG_CELLS(F) { xf[ix(F, i, j, k)] += xc[ix(C, i >> 1, j >> 1, k >> 1)]; }
+// xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
+// added on the fly, also at the neighbours): k_mg_prolong and the first
+// post-smoothing sweep in one pass.
+__global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, const float* __restrict__ x,
+                                    const float* __restrict__ xcrs, const float* __restrict__ b,
+                                    float* __restrict__ xo, float omega) {
+  const long long sy = F.sy, sz = F.sz, cy = C.sy, cz = C.sz;
+  MG_CELLS(F) {
+    const long long c = ix(F, i, j, k), pc = ix(C, i >> 1, j >> 1, k >> 1);
+    const float yc = x[c] + xcrs[pc];
+    float u = 0.f;
+    if (i + 1 < F.nx) u = fmaf(F.te[c], yc - (x[c + 1] + xcrs[(i & 1) ? pc + 1 : pc]), u);
+    if (i > 0) u = fmaf(F.te[c - 1], yc - (x[c - 1] + xcrs[(i & 1) ? pc : pc - 1]), u);
+    if (j + 1 < F.ny) u = fmaf(F.tn[c], yc - (x[c + sy] + xcrs[(j & 1) ? pc + cy : pc]), u);
+    if (j > 0) u = fmaf(F.tn[c - sy], yc - (x[c - sy] + xcrs[(j & 1) ? pc : pc - cy]), u);
+    if (k + 1 < F.nz) u = fmaf(F.tt[c], yc - (x[c + sz] + xcrs[(k & 1) ? pc + cz : pc]), u);
+    if (k > 0) u = fmaf(F.tt[c - sz], yc - (x[c - sz] + xcrs[(k & 1) ? pc : pc - cz]), u);
+    xo[c] = fmaf(omega * F.dinv[c], b[c] - u, yc);
+  }
 }
 
 // Coarsest level: nsweeps weighted Jacobi sweeps from 0 in one block
@@ -207,16 +221,19 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const float* b, float* x,
     cur = oth;
     oth = t;
   }
-  k_mg_residual<<<g, blk, 0, st>>>(L, cur, b, L.r);
-  note_launch();
   const MgLevel& C = H.lv[l + 1];
-  k_mg_restrict<<<mg_grid(C), blk, 0, st>>>(L, C, L.r, C.b);
+  k_mg_resrestrict<<<mg_grid(C), blk, 0, st>>>(L, C, cur, b, C.b);
   note_launch();
   cudaError_t e = vcycle(H, l + 1, C.b, C.x, st);
   if (e != cudaSuccess) return e;
-  k_mg_prolong<<<g, blk, 0, st>>>(L, C, C.x, cur);
+  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, C.x, b, oth, H.omega);
   note_launch();
-  for (int s = 0; s < H.nu; s++) {
+  {
+    float* t = cur;
+    cur = oth;
+    oth = t;
+  }
+  for (int s = 1; s < H.nu; s++) {
     k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0);
     note_launch();
     float* t = cur;
@@ -226,27 +243,117 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const float* b, float* x,
   return cudaGetLastError();
 }
 
-cudaError_t mg_vcycle(const MgHierarchy& H, const float* r, float* z, cudaStream_t st) { return vcycle(H, 0, r, z, st); }
-
-// ---------------------------------------------------------------- PCG pieces (level-0 layout)
+// ---------------------------------------------------------------- level 0: float4 kernels
 namespace {
 
-// q = A p, pq = p.q, alpha = rz / pq
-__global__ void k_mgp_spmv(MgLevel L, const float* __restrict__ p, float* __restrict__ q, MgScalars* S, RedBuf rb) {
-  if (!S->active) return;
-  double s[1] = {0.0}, m[1] = {0.0};
-  float acc = 0.f, err = 0.f;
-  MG_CELLS(L) {
-    const long long c = ix(L, i, j, k);
-    const float v = apply_a(L, p, i, j, k, c);
-    q[c] = v;
-    const float prod = p[c] * v;
-    const float t = acc + prod, bb = t - acc;
-    err += (acc - (t - bb)) + (prod - bb);
-    acc = t;
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 zero4() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ float el(const float4& v, int n) { return n == 0 ? v.x : (n == 1 ? v.y : (n == 2 ? v.z : v.w)); }
+
+// f32 running sum with its rounding error (TwoSum)
+struct Acc2 {
+  float s = 0.f, e = 0.f;
+  __device__ __forceinline__ void add(float p) {
+    const float t = s + p, bb = t - s;
+    e += (s - (t - bb)) + (p - bb);
+    s = t;
   }
-  s[0] = (double)acc + (double)err;
-  double out[1];
+  __device__ __forceinline__ void add4(const float4& a, const float4& b) {
+    add(fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x))));
+  }
+};
+
+// Thread position on level 0: group g (cells 4g .. 4g+3, 0-based) of row j
+// (1-based), planes k0..k1 (1-based), as in the mixed solver's kernels.
+struct P0 {
+  int g, j, k0, k1;
+  bool live;
+  long long base;
+};
+__device__ __forceinline__ P0 p0_pos(const MixedGrid& G) {
+  P0 t;
+  t.g = blockIdx.x * 32 + threadIdx.x;
+  t.j = blockIdx.y * 4 + threadIdx.y + 1;
+  t.live = t.g < G.ng && t.j <= G.ny;
+  t.k0 = blockIdx.z * G.kc + 1;
+  t.k1 = min(G.nz, t.k0 + G.kc - 1);
+  t.base = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (t.k0 - 1));
+  return t;
+}
+
+// u = (A v) for the four cells of a group from the loaded neighbourhood.
+__device__ __forceinline__ float4 face_apply(const float4& c, float left, float right, const float4& s,
+                                             const float4& n, const float4& b, const float4& t, const float4& te,
+                                             float te_left, const float4& tn, const float4& tns, const float4& tt,
+                                             const float4& ttb) {
+  float u[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const float x = el(c, q);
+    const float xw = q == 0 ? left : el(c, q - 1), xe = q == 3 ? right : el(c, q + 1);
+    const float tw = q == 0 ? te_left : el(te, q - 1);
+    float v = el(te, q) * (x - xe);
+    v = fmaf(tw, x - xw, v);
+    v = fmaf(el(tn, q), x - el(n, q), v);
+    v = fmaf(el(tns, q), x - el(s, q), v);
+    v = fmaf(el(tt, q), x - el(t, q), v);
+    v = fmaf(el(ttb, q), x - el(b, q), v);
+    u[q] = v;
+  }
+  return make_float4(u[0], u[1], u[2], u[3]);
+}
+
+// q = A p, pq = p.q, alpha = rz / pq
+__global__ void __launch_bounds__(128) k_mg0_spmv(MixedGrid G, MgLevel L, const float* __restrict__ p,
+                                                  float* __restrict__ q, MgScalars* S, RedBuf rb) {
+  if (!S->active) return;
+  const P0 t = p0_pos(G);
+  const int lane = threadIdx.x;
+  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
+  const long long px = G.px, pl = G.plane;
+  Acc2 acc;
+  float4 pc = zero4(), pb = zero4(), ttb = zero4();
+  if (t.live) {
+    pc = ld4(p + t.base);
+    pb = t.k0 > 1 ? ld4(p + t.base - pl) : pc;
+    if (t.k0 > 1) ttb = ld4(L.tt + t.base - pl);
+  }
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += pl) {
+    float4 pt = pc, ps = zero4(), pn = zero4(), te = zero4(), tn = zero4(), tns = zero4(), tt = zero4();
+    float lft = 0.f, tlft = 0.f, rgt = 0.f;
+    if (t.live) {
+      if (k < G.nz) pt = ld4(p + base + pl);
+      ps = ld4(p + base - px);
+      pn = ld4(p + base + px);
+      te = ld4(L.te + base);
+      tn = ld4(L.tn + base);
+      tns = ld4(L.tn + base - px);
+      tt = ld4(L.tt + base);
+      if (lane == 0) {
+        lft = __ldg(p + base - 1);
+        tlft = __ldg(L.te + base - 1);
+      }
+      if (fetch_right) rgt = __ldg(p + base + 4);
+    }
+    float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
+    float te_left = __shfl_up_sync(0xffffffffu, te.w, 1);
+    if (lane == 0) {
+      left = lft;
+      te_left = tlft;
+    }
+    if (fetch_right) right = rgt;
+    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, te, te_left, tn, tns, tt, ttb);
+    if (t.live) {
+      st4(q + base, u);
+      acc.add4(pc, u);
+    }
+    pb = pc;
+    pc = pt;
+    ttb = tt;
+  }
+  double s[1] = {(double)acc.s + (double)acc.e}, m[1] = {0.0}, out[1];
   if (grid_reduce<1, 0>(s, m, rb.partials, rb.ticket, out) && lin_tid() == 0) {
     S->pq = out[0];
     if (!(out[0] > 0) || !(S->rz > 0)) {
@@ -258,33 +365,107 @@ __global__ void k_mgp_spmv(MgLevel L, const float* __restrict__ p, float* __rest
   }
 }
 
-// e += alpha p; r -= alpha q
-__global__ void k_mgp_update(MgLevel L, const float* __restrict__ p, const float* __restrict__ q, float* __restrict__ e,
-                             float* __restrict__ r, const MgScalars* S) {
+// e += alpha p; r -= alpha q; t = omega dinv r (the V-cycle's first
+// pre-smoothing sweep from zero)
+__global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, const float* __restrict__ p,
+                                                    const float* __restrict__ q, float* __restrict__ e,
+                                                    float* __restrict__ r, float omega, const MgScalars* S) {
   if (!S->active) return;
   const float a = (float)S->alpha;
-  MG_CELLS(L) {
-    const long long c = ix(L, i, j, k);
-    e[c] = fmaf(a, p[c], e[c]);
-    r[c] = fmaf(-a, q[c], r[c]);
+  const P0 t = p0_pos(G);
+  if (!t.live) return;
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+    const float4 pp = ld4(p + base), qq = ld4(q + base), dv = ld4(L.dinv + base);
+    float4 ee = *reinterpret_cast<const float4*>(e + base), rr = *reinterpret_cast<const float4*>(r + base);
+    ee = make_float4(fmaf(a, pp.x, ee.x), fmaf(a, pp.y, ee.y), fmaf(a, pp.z, ee.z), fmaf(a, pp.w, ee.w));
+    rr = make_float4(fmaf(-a, qq.x, rr.x), fmaf(-a, qq.y, rr.y), fmaf(-a, qq.z, rr.z), fmaf(-a, qq.w, rr.w));
+    st4(e + base, ee);
+    st4(r + base, rr);
+    st4(L.t + base, make_float4(omega * dv.x * rr.x, omega * dv.y * rr.y, omega * dv.z * rr.z, omega * dv.w * rr.w));
   }
 }
 
-// rz_new = r.z; beta; stop at the drop
-__global__ void k_mgp_rz(MgLevel L, const float* __restrict__ r, const float* __restrict__ z, MgScalars* S, RedBuf rb,
-                         int start) {
+// z = y + omega dinv (r - A y), y = t + P xc (the coarse correction added to
+// the pre-smoothed level-0 iterate, also at the neighbours), and r.z with the
+// PCG scalar updates (start: rz = rz0; otherwise beta and the stop test).
+__global__ void __launch_bounds__(128) k_mg0_prolong_smooth(MixedGrid G, MgLevel L, MgLevel C,
+                                                            const float* __restrict__ r, float* __restrict__ z,
+                                                            float omega, MgScalars* S, RedBuf rb, int start) {
   if (!start && !S->active) return;
-  double s[1] = {0.0}, m[1] = {0.0};
-  float acc = 0.f, err = 0.f;
-  MG_CELLS(L) {
-    const long long c = ix(L, i, j, k);
-    const float prod = r[c] * z[c];
-    const float t = acc + prod, bb = t - acc;
-    err += (acc - (t - bb)) + (prod - bb);
-    acc = t;
+  const P0 t = p0_pos(G);
+  const int lane = threadIdx.x;
+  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
+  const long long px = G.px, pl = G.plane;
+  const float* __restrict__ tv = L.t;
+  const float* __restrict__ xc = C.x;
+  const int jj = t.j - 1, i0 = 4 * t.g;  // 0-based row and first cell
+  // coarse value at (ci, cj, ck) or 0 outside
+  auto cval = [&](int ci, int cj, int ck) -> float {
+    if (ci < 0 || ci >= C.nx || cj < 0 || cj >= C.ny || ck < 0 || ck >= C.nz) return 0.f;
+    return __ldg(xc + ci + C.sy * cj + C.sz * ck);
+  };
+  // P xc for the four cells of the group in fine row jr, fine plane kr
+  auto prol4 = [&](int jr, int kr) -> float4 {
+    if (jr < 0 || jr >= L.ny || kr < 0 || kr >= L.nz) return zero4();
+    const float a = cval(i0 >> 1, jr >> 1, kr >> 1), b = cval((i0 >> 1) + 1, jr >> 1, kr >> 1);
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) v[q] = i0 + q < L.nx ? (q < 2 ? a : b) : 0.f;
+    return make_float4(v[0], v[1], v[2], v[3]);
+  };
+  auto add4 = [](const float4& a, const float4& b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); };
+  Acc2 acc;
+  float4 yc = zero4(), yb = zero4(), ttb = zero4();
+  if (t.live) {
+    yc = add4(ld4(tv + t.base), prol4(jj, t.k0 - 1));
+    yb = t.k0 > 1 ? add4(ld4(tv + t.base - pl), prol4(jj, t.k0 - 2)) : yc;
+    if (t.k0 > 1) ttb = ld4(L.tt + t.base - pl);
   }
-  s[0] = (double)acc + (double)err;
-  double out[1];
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += pl) {
+    const int kk = k - 1;
+    float4 yt = yc, ys = zero4(), yn = zero4(), te = zero4(), tn = zero4(), tns = zero4(), tt = zero4(),
+           dv = zero4(), rr = zero4();
+    float lft = 0.f, tlft = 0.f, rgt = 0.f;
+    if (t.live) {
+      if (k < G.nz) yt = add4(ld4(tv + base + pl), prol4(jj, kk + 1));
+      ys = add4(ld4(tv + base - px), prol4(jj - 1, kk));
+      yn = add4(ld4(tv + base + px), prol4(jj + 1, kk));
+      te = ld4(L.te + base);
+      tn = ld4(L.tn + base);
+      tns = ld4(L.tn + base - px);
+      tt = ld4(L.tt + base);
+      dv = ld4(L.dinv + base);
+      rr = ld4(r + base);
+      if (lane == 0) {
+        lft = i0 > 0 ? __ldg(tv + base - 1) + cval((i0 - 1) >> 1, jj >> 1, kk >> 1) : 0.f;
+        tlft = __ldg(L.te + base - 1);
+      }
+      if (fetch_right) rgt = i0 + 4 < L.nx ? __ldg(tv + base + 4) + cval((i0 + 4) >> 1, jj >> 1, kk >> 1) : 0.f;
+    }
+    float left = __shfl_up_sync(0xffffffffu, yc.w, 1), right = __shfl_down_sync(0xffffffffu, yc.x, 1);
+    float te_left = __shfl_up_sync(0xffffffffu, te.w, 1);
+    if (lane == 0) {
+      left = lft;
+      te_left = tlft;
+    }
+    if (fetch_right) right = rgt;
+    const float4 u = face_apply(yc, left, right, ys, yn, yb, yt, te, te_left, tn, tns, tt, ttb);
+    float zz[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      zz[q] = (t.live && i0 + q < L.nx) ? fmaf(omega * el(dv, q), el(rr, q) - el(u, q), el(yc, q)) : 0.f;
+    const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
+    if (t.live) {
+      st4(z + base, z4);
+      acc.add4(rr, z4);
+    }
+    yb = yc;
+    yc = yt;
+    ttb = tt;
+  }
+  double s[1] = {(double)acc.s + (double)acc.e}, m[1] = {0.0}, out[1];
   if (grid_reduce<1, 0>(s, m, rb.partials, rb.ticket, out) && lin_tid() == 0) {
     const double rz = out[0];
     if (start) {
@@ -308,23 +489,30 @@ __global__ void k_mgp_rz(MgLevel L, const float* __restrict__ r, const float* __
   }
 }
 
-// p = z + beta p  (start: p = z)
-__global__ void k_mgp_direction(MgLevel L, const float* __restrict__ z, float* __restrict__ p, const MgScalars* S,
-                                int start) {
+// p = z + beta p (start: p = z)
+__global__ void __launch_bounds__(128) k_mg0_direction(MixedGrid G, const float* __restrict__ z, float* __restrict__ p,
+                                                       const MgScalars* S, int start) {
   if (!start && !S->dir) return;
   const float b = start ? 0.f : (float)S->beta;
-  MG_CELLS(L) {
-    const long long c = ix(L, i, j, k);
-    p[c] = start ? z[c] : fmaf(b, p[c], z[c]);
+  const P0 t = p0_pos(G);
+  if (!t.live) return;
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
+    const float4 zz = ld4(z + base);
+    const float4 pp = *reinterpret_cast<const float4*>(p + base);
+    st4(p + base, start ? zz
+                        : make_float4(fmaf(b, pp.x, zz.x), fmaf(b, pp.y, zz.y), fmaf(b, pp.z, zz.z),
+                                      fmaf(b, pp.w, zz.w)));
   }
 }
 
-// r32 = scale * rV (compact FP64 projected residual) on fluid cells, e = 0
+// r = scale * rV (compact FP64 projected residual) on fluid cells, e = 0
 __global__ void k_mgp_load(MgLevel L, const double* __restrict__ rv, double scale, float* __restrict__ r,
                            float* __restrict__ e) {
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
-    r[c] = L.dinv[c] > 0.f ? (float)(rv[c] * scale) : 0.f;
+    const long long cc = i + (long long)L.nx * (j + (long long)L.ny * k);
+    r[c] = L.dinv[c] > 0.f ? (float)(rv[cc] * scale) : 0.f;
     e[c] = 0.f;
   }
 }
@@ -337,7 +525,28 @@ __global__ void k_mgp_apply(MgLevel L, Dims d, const float* __restrict__ e, doub
   }
 }
 
+dim3 g0_grid(const MixedGrid& G) {
+  return dim3((unsigned)((G.ng + 31) / 32), (unsigned)((G.ny + 3) / 4), (unsigned)((G.nz + G.kc - 1) / G.kc));
+}
+
 }  // namespace
+
+// Level-0 V-cycle tail shared by start and iteration: restriction of
+// r - A t, the coarse cycle, and the prolongation + post-smoothing + r.z pass.
+static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, int start,
+                               cudaStream_t st) {
+  const MgLevel& L = H.lv[0];
+  const MgLevel& C = H.lv[1];
+  k_mg_resrestrict<<<mg_grid(C), dim3(32, 8), 0, st>>>(L, C, L.t, v.r, C.b);
+  note_launch();
+  cudaError_t e = vcycle(H, 1, C.b, C.x, st);
+  if (e != cudaSuccess) return e;
+  k_mg0_prolong_smooth<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, C, v.r, v.z, H.omega, S, rb, start);
+  note_launch();
+  k_mg0_direction<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, v.z, v.p, S, start);
+  note_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t mg_pcg_start(const MgHierarchy& H, const double* rv, double scale, MgVecs& v, MgScalars* S, const RedBuf& rb,
                          cudaStream_t st) {
@@ -345,29 +554,18 @@ cudaError_t mg_pcg_start(const MgHierarchy& H, const double* rv, double scale, M
   const dim3 blk(32, 8), g = mg_grid(L);
   k_mgp_load<<<g, blk, 0, st>>>(L, rv, scale, v.r, v.e);
   note_launch();
-  cudaError_t e = mg_vcycle(H, v.r, v.z, st);
-  if (e != cudaSuccess) return e;
-  k_mgp_rz<<<g, blk, 0, st>>>(L, v.r, v.z, S, rb, 1);
+  k_mg_smooth<<<g, blk, 0, st>>>(L, L.t, v.r, L.t, H.omega, 1);
   note_launch();
-  k_mgp_direction<<<g, blk, 0, st>>>(L, v.z, v.p, S, 1);
-  note_launch();
-  return cudaGetLastError();
+  return level0_tail(H, v, S, rb, 1, st);
 }
 
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
-  const dim3 blk(32, 8), g = mg_grid(L);
-  k_mgp_spmv<<<g, blk, 0, st>>>(L, v.p, v.q, S, rb);
+  k_mg0_spmv<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.p, v.q, S, rb);
   note_launch();
-  k_mgp_update<<<g, blk, 0, st>>>(L, v.p, v.q, v.e, v.r, S);
+  k_mg0_update<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.p, v.q, v.e, v.r, H.omega, S);
   note_launch();
-  cudaError_t e = mg_vcycle(H, v.r, v.z, st);
-  if (e != cudaSuccess) return e;
-  k_mgp_rz<<<g, blk, 0, st>>>(L, v.r, v.z, S, rb, 0);
-  note_launch();
-  k_mgp_direction<<<g, blk, 0, st>>>(L, v.z, v.p, S, 0);
-  note_launch();
-  return cudaGetLastError();
+  return level0_tail(H, v, S, rb, 0, st);
 }
 
 cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, double scale, double* phi,
@@ -378,8 +576,8 @@ cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, d
   return cudaGetLastError();
 }
 
-int mg_grid_blocks(const MgLevel& L) {
-  const dim3 g = mg_grid(L);
+int mg_grid_blocks(const MixedGrid& G) {
+  const dim3 g = g0_grid(G);
   return (int)(g.x * g.y * g.z);
 }
 
