@@ -760,8 +760,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   MgHierarchy H;
   std::memset(&H, 0, sizeof(H));
   H.nu = (int)env_double("FPM_MG_NU", 1);
-  H.omega = (float)env_double("FPM_MG_OMEGA", 0.8);
+  H.omega = (float)env_double("FPM_MG_OMEGA", 0.9);
   H.coarse_sweeps = (int)env_double("FPM_MG_COARSE_SWEEPS", 40);
+  H.cscale = (float)env_double("FPM_MG_CSCALE", 1.0);
   // level 0 in the mixed solver's FP32 layout (zero halo), coarse levels compact
   H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk());
   auto zeros = [&](long long n) {
@@ -792,7 +793,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     L.dinv = zeros(L.alloc);
     L.t = zeros(L.alloc);
     L.x = H.nlev == 0 ? nullptr : zeros(L.alloc);
-    L.b = H.nlev == 0 ? nullptr : zeros(L.alloc);
+    L.b = zeros(L.alloc);  // level 0: the residual of the pre-smoothed iterate
     H.nlev++;
     if (L.n() <= 1024 || H.nlev == kMgMaxLevels) break;
     nx = (nx + 1) / 2;
@@ -834,7 +835,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     };
     double res = true_res(), best = res;
     int total = 0, stall = 0;
-    ChunkGraphs graphs(5 + (H.nlev - 2) * (2 * H.nu + 1) + 1);
+    ChunkGraphs graphs(6 + (H.nlev - 2) * (2 * H.nu + 1) + 1);
     while (res > tol && res == res && total < max_sweeps) {
       const double scale = res > 0 ? 1.0 / res : 1.0;
       MgScalars h0;
@@ -2186,7 +2187,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         // at once: host worker threads, one stream each.
         int dev = 0;
         CUDA_TRY(cudaGetDevice(&dev));
-        const int nworkers = (int)std::min<size_t>(jobs.size(), 12);
+        const int nworkers = (int)std::min<size_t>(jobs.size(), (size_t)env_double("FPM_FRAMES_WORKERS", 12));
         std::vector<int> sws(jobs.size(), 0);
         std::vector<double> rrs(jobs.size(), 0.0);
         std::vector<std::string> errs(nworkers);
@@ -2220,6 +2221,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       }
     }
     Trace tg("frames: gauge and partition");
+    for (size_t q = 0; q < nq; q++) set[q] = to64[q] ? 0 : 1;  // individually solved ones are gauged
+    push_set();
     CUDA_TRY(launch_k_b2_gauge_sum(dfr, dtf, ntiles, b, st));
     CUDA_TRY(launch_k_b2_gauge_sub(dfr, dtf, ntiles, b, st));
     std::fill(set.begin(), set.end(), 1);

@@ -479,7 +479,9 @@ __global__ void k_b2_keep(const Frame2* __restrict__ fr, const int* __restrict__
 }
 
 // ---------------------------------------------------------------- gauge
-// src/fpm_stairstep_mpi_3d.f90:170-185 per frame and direction.
+// src/fpm_stairstep_mpi_3d.f90:170-185 per frame and direction (the
+// subtraction only for the directions in the set: the others were solved on
+// their own and are gauged already).
 __global__ void k_b2_gauge_sum(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b) {
   const TileRef t = tile_ref(fr, tile_frame, b.tiles);
   const Frame2& F = fr[t.f];
@@ -504,7 +506,8 @@ __global__ void k_b2_gauge_sub(const Frame2* __restrict__ fr, const int* __restr
   for (int k = 1; k <= 2; k++) {
     const long long p = ph(F, t.i, t.j, k);
     if (b.solid3[p] != 0) continue;
-    for (int r = 0; r < kR; r++) b.phi[r][p] = dsub(b.phi[r][p], b.rmean[t.f * kR + r]);
+    for (int r = 0; r < kR; r++)
+      if (b.in_set[t.f * kR + r]) b.phi[r][p] = dsub(b.phi[r][p], b.rmean[t.f * kR + r]);
   }
 }
 

@@ -258,6 +258,7 @@ struct MgHierarchy {
   int nu;             // pre- and post-smoothing sweeps
   int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block)
   float omega;        // Jacobi weight
+  float cscale;       // coarse-correction scale (1 = plain Galerkin correction)
 };
 struct MgVecs {
   float *r, *z, *p, *q, *e;

@@ -112,10 +112,11 @@ __global__ void k_mg_smooth(MgLevel L, const float* __restrict__ x, const float*
   }
 }
 
-// bc = restriction of b - A x: one thread per coarse cell sums the residuals
-// of its (up to 8) fine cells (k_mg_residual + k_mg_restrict in one pass).
+// bc = scale x restriction of b - A x: one thread per coarse cell sums the
+// residuals of its (up to 8) fine cells.  scale > 1 over-corrects with the
+// coarse solution (the cycle stays linear and symmetric).
 __global__ void k_mg_resrestrict(MgLevel F, MgLevel C, const float* __restrict__ x, const float* __restrict__ b,
-                                 float* __restrict__ bc) {
+                                 float* __restrict__ bc, float scale) {
   MG_CELLS(C) {
     float s = 0.f;
     for (int o = 0; o < 8; o++) {
@@ -125,7 +126,19 @@ __global__ void k_mg_resrestrict(MgLevel F, MgLevel C, const float* __restrict__
         s += b[c] - apply_a(F, x, fi, fj, fk, c);
       }
     }
-    bc[ix(C, i, j, k)] = s;
+    bc[ix(C, i, j, k)] = scale * s;
+  }
+}
+
+// bc = scale x the sum of the fine residuals rf of each aggregate.
+__global__ void k_mg_restrict(MgLevel F, MgLevel C, const float* __restrict__ rf, float* __restrict__ bc, float scale) {
+  MG_CELLS(C) {
+    float s = 0.f;
+    for (int o = 0; o < 8; o++) {
+      const int fi = 2 * i + (o & 1), fj = 2 * j + ((o >> 1) & 1), fk = 2 * k + (o >> 2);
+      if (fi < F.nx && fj < F.ny && fk < F.nz) s += rf[ix(F, fi, fj, fk)];
+    }
+    bc[ix(C, i, j, k)] = scale * s;
   }
 }
 
@@ -150,28 +163,48 @@ __global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, const float* __restric
   }
 }
 
-// Coarsest level: nsweeps weighted Jacobi sweeps from 0 in one block
-// (the level has at most 1024 cells); ping-pong in global scratch.
-__global__ void k_mg_coarse(MgLevel L, const float* __restrict__ b, float* __restrict__ x, float* __restrict__ tmp,
-                            float omega, int nsweeps) {
+// Coarsest level (at most 1024 cells, compact layout): nsweeps weighted
+// Jacobi sweeps from 0 in one block, with the level's operator, right-hand
+// side and iterate in shared memory.
+__global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, const float* __restrict__ b, float* __restrict__ x,
+                                                    float omega, int nsweeps) {
+  __shared__ float te[1024], tn[1024], tt[1024], wd[1024], bb[1024], xa[1024], xb[1024];
   const int n = (int)L.n();
-  for (int c = threadIdx.x; c < n; c += blockDim.x) x[c] = omega * L.dinv[c] * b[c];
+  const int c = threadIdx.x;
+  const int sy = (int)L.sy, sz = (int)L.sz;
+  int i = 0, j = 0, k = 0;
+  if (c < n) {
+    te[c] = L.te[c];
+    tn[c] = L.tn[c];
+    tt[c] = L.tt[c];
+    wd[c] = omega * L.dinv[c];
+    bb[c] = b[c];
+    xa[c] = wd[c] * bb[c];
+    i = c % L.nx;
+    j = (c / L.nx) % L.ny;
+    k = c / (L.nx * L.ny);
+  }
   __syncthreads();
-  float* a = x;
-  float* o = tmp;
+  float* a = xa;
+  float* o = xb;
   for (int s = 1; s < nsweeps; s++) {
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      const int i = c % L.nx, j = (c / L.nx) % L.ny, k = c / (L.nx * L.ny);
-      o[c] = fmaf(omega * L.dinv[c], b[c] - apply_a(L, a, i, j, k, c), a[c]);
+    if (c < n) {
+      const float xc = a[c];
+      float u = 0.f;
+      if (i + 1 < L.nx) u = fmaf(te[c], xc - a[c + 1], u);
+      if (i > 0) u = fmaf(te[c - 1], xc - a[c - 1], u);
+      if (j + 1 < L.ny) u = fmaf(tn[c], xc - a[c + sy], u);
+      if (j > 0) u = fmaf(tn[c - sy], xc - a[c - sy], u);
+      if (k + 1 < L.nz) u = fmaf(tt[c], xc - a[c + sz], u);
+      if (k > 0) u = fmaf(tt[c - sz], xc - a[c - sz], u);
+      o[c] = fmaf(wd[c], bb[c] - u, xc);
     }
     __syncthreads();
     float* t = a;
     a = o;
     o = t;
   }
-  if (a != x) {
-    for (int c = threadIdx.x; c < n; c += blockDim.x) x[c] = a[c];
-  }
+  if (c < n) x[c] = a[c];
 }
 
 dim3 mg_grid(const MgLevel& L) {
@@ -206,7 +239,7 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const float* b, float* x,
   const MgLevel& L = H.lv[l];
   const dim3 blk(32, 8), g = mg_grid(L);
   if (l == H.nlev - 1) {
-    k_mg_coarse<<<1, 1024, 0, st>>>(L, b, x, L.t, H.omega, H.coarse_sweeps);
+    k_mg_coarse<<<1, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps);
     note_launch();
     return cudaGetLastError();
   }
@@ -222,7 +255,7 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const float* b, float* x,
     oth = t;
   }
   const MgLevel& C = H.lv[l + 1];
-  k_mg_resrestrict<<<mg_grid(C), blk, 0, st>>>(L, C, cur, b, C.b);
+  k_mg_resrestrict<<<mg_grid(C), blk, 0, st>>>(L, C, cur, b, C.b, H.cscale);
   note_launch();
   cudaError_t e = vcycle(H, l + 1, C.b, C.x, st);
   if (e != cudaSuccess) return e;
@@ -362,6 +395,55 @@ __global__ void __launch_bounds__(128) k_mg0_spmv(MixedGrid G, MgLevel L, const 
     } else {
       S->alpha = S->rz / out[0];
     }
+  }
+}
+
+// res = r - A t on level 0 (the residual of the pre-smoothed iterate)
+__global__ void __launch_bounds__(128) k_mg0_residual(MixedGrid G, MgLevel L, const float* __restrict__ r,
+                                                      float* __restrict__ res, const MgScalars* S, int start) {
+  if (!start && !S->active) return;
+  const P0 t = p0_pos(G);
+  const int lane = threadIdx.x;
+  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
+  const long long px = G.px, pl = G.plane;
+  const float* __restrict__ x = L.t;
+  float4 pc = zero4(), pb = zero4(), ttb = zero4();
+  if (t.live) {
+    pc = ld4(x + t.base);
+    pb = t.k0 > 1 ? ld4(x + t.base - pl) : pc;
+    if (t.k0 > 1) ttb = ld4(L.tt + t.base - pl);
+  }
+  long long base = t.base;
+  for (int k = t.k0; k <= t.k1; k++, base += pl) {
+    float4 pt = pc, ps = zero4(), pn = zero4(), te = zero4(), tn = zero4(), tns = zero4(), tt = zero4(), rr = zero4();
+    float lft = 0.f, tlft = 0.f, rgt = 0.f;
+    if (t.live) {
+      if (k < G.nz) pt = ld4(x + base + pl);
+      ps = ld4(x + base - px);
+      pn = ld4(x + base + px);
+      te = ld4(L.te + base);
+      tn = ld4(L.tn + base);
+      tns = ld4(L.tn + base - px);
+      tt = ld4(L.tt + base);
+      rr = ld4(r + base);
+      if (lane == 0) {
+        lft = __ldg(x + base - 1);
+        tlft = __ldg(L.te + base - 1);
+      }
+      if (fetch_right) rgt = __ldg(x + base + 4);
+    }
+    float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
+    float te_left = __shfl_up_sync(0xffffffffu, te.w, 1);
+    if (lane == 0) {
+      left = lft;
+      te_left = tlft;
+    }
+    if (fetch_right) right = rgt;
+    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, te, te_left, tn, tns, tt, ttb);
+    if (t.live) st4(res + base, make_float4(rr.x - u.x, rr.y - u.y, rr.z - u.z, rr.w - u.w));
+    pb = pc;
+    pc = pt;
+    ttb = tt;
   }
 }
 
@@ -537,7 +619,9 @@ static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, co
                                cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const MgLevel& C = H.lv[1];
-  k_mg_resrestrict<<<mg_grid(C), dim3(32, 8), 0, st>>>(L, C, L.t, v.r, C.b);
+  k_mg0_residual<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.r, L.b, S, start);
+  note_launch();
+  k_mg_restrict<<<mg_grid(C), dim3(32, 8), 0, st>>>(L, C, L.b, C.b, H.cscale);
   note_launch();
   cudaError_t e = vcycle(H, 1, C.b, C.x, st);
   if (e != cudaSuccess) return e;
