@@ -803,6 +803,14 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   if (H.nlev < 2 || H.lv[H.nlev - 1].n() > 1024)
     throw Error{FPM_E_LIMIT, "grid too small or too large for the multigrid hierarchy"};
   if (H.nu != 1) throw Error{FPM_E_ARG, "the multigrid cycle uses one smoothing sweep on level 0"};
+  H.fb0 = A.get<uint8_t>(H.g0.size);
+  CUDA_TRY(cudaMemsetAsync(H.fb0, 0, H.g0.size, st));
+  H.aex = zeros(H.g0.px);
+  H.dxr = zeros(H.g0.px);
+  H.dy = zeros(d.ny);
+  H.ayn = zeros(d.ny);
+  H.dz = zeros(d.nz);
+  H.azt = zeros(d.nz);
   CUDA_TRY(mg_setup(H, d, solid, ax, st));
   const long long n0 = H.lv[0].alloc;
   MgVecs v;

@@ -255,6 +255,13 @@ struct MgHierarchy {
   int nlev;
   MgLevel lv[kMgMaxLevels];
   MixedGrid g0;       // level 0 uses the FP32 layout of the mixed solver (float4 groups, zero halo)
+  // level 0 operator for the float4 kernels: open-face bits per cell (1 east,
+  // 2 north, 4 top) and 1-D FP32 axis factors; T_east = dy dz / (xc_{i+1} - xc_i)
+  // etc. are rebuilt from them in registers
+  uint8_t* fb0;
+  float *aex, *dxr;   // row layout (index 3 + i, i 1-based), zero outside
+  float *dy, *ayn;    // index j - 1
+  float *dz, *azt;    // index k - 1
   int nu;             // pre- and post-smoothing sweeps
   int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block)
   float omega;        // Jacobi weight
@@ -276,14 +283,11 @@ cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, d
 int mg_grid_blocks(const MixedGrid& G);
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
-// weighted: src is already a volume-weighted vector (a residual b - A phi)
-// instead of the source; accumulate: phi += gamma y instead of phi = gamma y.
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,
                                 float* mx, float* my, float* mz, float* b, double* bmax, const RedBuf& rb,
-                                cudaStream_t st, int weighted = 0);
+                                cudaStream_t st);
 cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src, const double* diag, const Coefs& c,
-                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st,
-                               int weighted = 0, int accumulate = 0);
+                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st);
 cudaError_t launch_energy(const Dims& d, const double* phi, const double* src, const double* diag, const Coefs& c,
                           const Axes& ax, double* out2, const RedBuf& rb, cudaStream_t st);
 namespace net {

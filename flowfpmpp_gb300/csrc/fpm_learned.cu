@@ -20,7 +20,7 @@ namespace fpm {
 
 namespace {
 
-__global__ void k_learn_prep(Dims d, const double* __restrict__ src, int weighted, const double* __restrict__ diag,
+__global__ void k_learn_prep(Dims d, const double* __restrict__ src, const double* __restrict__ diag,
                              const double* __restrict__ dx, const double* __restrict__ dy,
                              const double* __restrict__ dz, uint8_t* __restrict__ fluid, float* __restrict__ b,
                              double* partials, unsigned int* ticket, double* bmax) {
@@ -29,7 +29,7 @@ __global__ void k_learn_prep(Dims d, const double* __restrict__ src, int weighte
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(c % d.nx) + 1, j = (int)((c / d.nx) % d.ny) + 1, k = (int)(c / ((long long)d.nx * d.ny)) + 1;
     const bool fl = diag[c] > 0;
-    const double v = fl ? (weighted ? src[c] : dx[i - 1] * dy[j - 1] * dz[k - 1] * src[c]) : 0.0;
+    const double v = fl ? dx[i - 1] * dy[j - 1] * dz[k - 1] * src[c] : 0.0;
     fluid[c] = fl ? 1 : 0;
     b[c] = (float)v;
     m[0] = fmax(m[0], fabs(v));
@@ -71,7 +71,7 @@ __global__ void k_learn_metric(int nx, int ny, int nz, const double* __restrict_
 }
 
 // y.b and y.(A y) over fluid cells, A y = V (diag y - sum c y_nb).
-__global__ void k_learn_dots(Dims d, const float* __restrict__ y, const double* __restrict__ src, int weighted,
+__global__ void k_learn_dots(Dims d, const float* __restrict__ y, const double* __restrict__ src,
                              const double* __restrict__ diag, Coefs cf, Axes ax, double* partials,
                              unsigned int* ticket, double* out2) {
   double s[2] = {0.0, 0.0}, m[1] = {0.0};
@@ -88,7 +88,7 @@ __global__ void k_learn_dots(Dims d, const float* __restrict__ y, const double* 
     const double yc = y[c];
     const double nb = cf.cw[i - 1] * yv(i - 1, j, k) + cf.ce[i - 1] * yv(i + 1, j, k) + cf.cs[j - 1] * yv(i, j - 1, k) +
                       cf.cn[j - 1] * yv(i, j + 1, k) + cf.cb[k - 1] * yv(i, j, k - 1) + cf.ct[k - 1] * yv(i, j, k + 1);
-    s[0] += weighted ? yc * src[c] : yc * vol * src[c];
+    s[0] += yc * vol * src[c];
     s[1] += yc * vol * (diag[c] * yc - nb);
   }
   double o[2];
@@ -100,15 +100,13 @@ __global__ void k_learn_dots(Dims d, const float* __restrict__ y, const double* 
 
 // phi(interior) = gamma y on fluid cells, 0 on solid cells (gamma = yb / yAy).
 __global__ void k_learn_apply(Dims d, const float* __restrict__ y, const double* __restrict__ diag,
-                              const double* __restrict__ dots, double* __restrict__ phi, int accumulate) {
+                              const double* __restrict__ dots, double* __restrict__ phi) {
   const double yb = dots[0], yay = dots[1];
   const double g = yay > 0 ? yb / yay : 0.0;
   const long long n = d.ncell();
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(c % d.nx) + 1, j = (int)((c / d.nx) % d.ny) + 1, k = (int)(c / ((long long)d.nx * d.ny)) + 1;
-    const double v = diag[c] > 0 ? g * (double)y[c] : 0.0;
-    if (accumulate) phi[d.ph(i, j, k)] += v;
-    else phi[d.ph(i, j, k)] = v;
+    phi[d.ph(i, j, k)] = diag[c] > 0 ? g * (double)y[c] : 0.0;
   }
 }
 
@@ -148,11 +146,10 @@ unsigned blocks_for(long long n) {
 
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,
                                 float* mx, float* my, float* mz, float* b, double* bmax, const RedBuf& rb,
-                                cudaStream_t st, int weighted) {
+                                cudaStream_t st) {
   const unsigned nb = blocks_for(d.ncell());
   if ((int)nb > rb.max_blocks) return cudaErrorInvalidValue;
-  k_learn_prep<<<nb, 256, 0, st>>>(d, src, weighted, diag, ax.dx, ax.dy, ax.dz, fluid, b, rb.partials, rb.ticket,
-                                   bmax);
+  k_learn_prep<<<nb, 256, 0, st>>>(d, src, diag, ax.dx, ax.dy, ax.dz, fluid, b, rb.partials, rb.ticket, bmax);
   note_launch();
   k_learn_scale<<<blocks_for(d.ncell()), 256, 0, st>>>(d.ncell(), b, bmax);
   note_launch();
@@ -162,13 +159,12 @@ cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* 
 }
 
 cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src, const double* diag, const Coefs& c,
-                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st,
-                               int weighted, int accumulate) {
+                               const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st) {
   const unsigned nb = blocks_for(d.ncell());
   if ((int)nb > rb.max_blocks) return cudaErrorInvalidValue;
-  k_learn_dots<<<nb, 256, 0, st>>>(d, y, src, weighted, diag, c, ax, rb.partials, rb.ticket, dots);
+  k_learn_dots<<<nb, 256, 0, st>>>(d, y, src, diag, c, ax, rb.partials, rb.ticket, dots);
   note_launch();
-  k_learn_apply<<<blocks_for(d.ncell()), 256, 0, st>>>(d, y, diag, dots, phi, accumulate);
+  k_learn_apply<<<blocks_for(d.ncell()), 256, 0, st>>>(d, y, diag, dots, phi);
   note_launch();
   return cudaGetLastError();
 }

@@ -33,8 +33,9 @@ __device__ __forceinline__ long long ix(const MgLevel& L, int i, int j, int k) {
     for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < (L).ny; j += gridDim.y * blockDim.y) \
       for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (L).nx; i += gridDim.x * blockDim.x)
 
-// Level 0 from the solid flags (padded (0:nx+1, 0:ny+1, nz)) and the axes.
-__global__ void k_mg_level0(MgLevel L, Dims d, const int32_t* __restrict__ solid, Axes ax) {
+// Level 0 from the solid flags (padded (0:nx+1, 0:ny+1, nz)) and the axes;
+// also the open-face bits of the float4 kernels.
+__global__ void k_mg_level0(MgLevel L, Dims d, const int32_t* __restrict__ solid, Axes ax, uint8_t* __restrict__ fb) {
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const bool fl = solid[d.ph(i + 1, j + 1, k + 1)] == 0;
@@ -48,6 +49,27 @@ __global__ void k_mg_level0(MgLevel L, Dims d, const int32_t* __restrict__ solid
     L.te[c] = (float)te;
     L.tn[c] = (float)tn;
     L.tt[c] = (float)tt;
+    fb[c] = (uint8_t)((te > 0.0 ? 1 : 0) | (tn > 0.0 ? 2 : 0) | (tt > 0.0 ? 4 : 0));
+  }
+}
+
+// 1-D FP32 factors of the level-0 faces (see MgHierarchy).
+__global__ void k_mg_axes0(MixedGrid G, Axes ax, float* aex, float* dxr, float* dy, float* ayn, float* dz, float* azt) {
+  const int n = max(G.px, max(G.ny, G.nz));
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+    if (m < G.px) {
+      const int i = m - 3;  // 1-based cell
+      aex[m] = (i >= 1 && i + 1 <= G.nx) ? (float)(1.0 / (ax.xc[i + 1] - ax.xc[i])) : 0.f;
+      dxr[m] = (i >= 1 && i <= G.nx) ? (float)ax.dx[i - 1] : 0.f;
+    }
+    if (m < G.ny) {
+      dy[m] = (float)ax.dy[m];
+      ayn[m] = m + 1 < G.ny ? (float)(1.0 / (ax.yc[m + 2] - ax.yc[m + 1])) : 0.f;
+    }
+    if (m < G.nz) {
+      dz[m] = (float)ax.dz[m];
+      azt[m] = m + 1 < G.nz ? (float)(1.0 / (ax.zc[m + 1] - ax.zc[m])) : 0.f;
+    }
   }
 }
 
@@ -219,7 +241,9 @@ dim3 mg_grid(const MgLevel& L) {
 
 cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const Axes& ax, cudaStream_t st) {
   const dim3 blk(32, 8);
-  k_mg_level0<<<mg_grid(H.lv[0]), blk, 0, st>>>(H.lv[0], d, solid, ax);
+  k_mg_level0<<<mg_grid(H.lv[0]), blk, 0, st>>>(H.lv[0], d, solid, ax, H.fb0);
+  note_launch();
+  k_mg_axes0<<<8, 256, 0, st>>>(H.g0, ax, H.aex, H.dxr, H.dy, H.ayn, H.dz, H.azt);
   note_launch();
   for (int l = 0; l + 1 < H.nlev; l++) {
     k_mg_coarsen<<<mg_grid(H.lv[l + 1]), blk, 0, st>>>(H.lv[l], H.lv[l + 1]);
@@ -337,8 +361,64 @@ __device__ __forceinline__ float4 face_apply(const float4& c, float left, float 
   return make_float4(u[0], u[1], u[2], u[3]);
 }
 
+// Level-0 faces rebuilt from the open-face bits and the 1-D factors.
+struct Ops0 {
+  const uint8_t* fb;
+  const float *aex, *dxr, *dy, *ayn, *dz, *azt;
+};
+struct Row0 {  // per-thread constants of a group's row
+  float4 aex, dx;
+  float dy, ayn, ayn_s, aex_w;
+};
+__device__ __forceinline__ Row0 row0(const Ops0& O, const P0& t) {
+  Row0 r;
+  r.aex = r.dx = zero4();
+  r.dy = r.ayn = r.ayn_s = r.aex_w = 0.f;
+  if (t.live) {
+    const int o = 4 * (t.g + 1);
+    r.aex = ld4(O.aex + o);
+    r.dx = ld4(O.dxr + o);
+    r.dy = __ldg(O.dy + t.j - 1);
+    r.ayn = __ldg(O.ayn + t.j - 1);
+    r.ayn_s = t.j > 1 ? __ldg(O.ayn + t.j - 2) : 0.f;
+    r.aex_w = __ldg(O.aex + o - 1);
+  }
+  return r;
+}
+__device__ __forceinline__ uchar4 ldb4(const uint8_t* p) { return *reinterpret_cast<const uchar4*>(p); }
+__device__ __forceinline__ int bt(const uchar4& v, int n) { return n == 0 ? v.x : (n == 1 ? v.y : (n == 2 ? v.z : v.w)); }
+// Faces of plane k (1-based): f = bits of the group, fs = bits of the row
+// below, fb = bits of the plane below, fw = bits of the west cell.
+struct Faces0 {
+  float4 te, tn, tns, tt, ttb;
+  float te_w;
+};
+__device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, const uchar4& f, const uchar4& fs,
+                                         const uchar4& fbel, int fw) {
+  const float dz = __ldg(O.dz + k - 1), azt = __ldg(O.azt + k - 1), aztb = k > 1 ? __ldg(O.azt + k - 2) : 0.f;
+  const float ex = R.dy * dz, ny = dz * R.ayn, nys = dz * R.ayn_s, tz = R.dy * azt, tzb = R.dy * aztb;
+  float te[4], tn[4], tns[4], tt[4], ttb[4];
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    const float dxn = el(R.dx, n);
+    te[n] = (bt(f, n) & 1) ? el(R.aex, n) * ex : 0.f;
+    tn[n] = (bt(f, n) & 2) ? dxn * ny : 0.f;
+    tns[n] = (bt(fs, n) & 2) ? dxn * nys : 0.f;
+    tt[n] = (bt(f, n) & 4) ? dxn * tz : 0.f;
+    ttb[n] = (bt(fbel, n) & 4) ? dxn * tzb : 0.f;
+  }
+  Faces0 F;
+  F.te = make_float4(te[0], te[1], te[2], te[3]);
+  F.tn = make_float4(tn[0], tn[1], tn[2], tn[3]);
+  F.tns = make_float4(tns[0], tns[1], tns[2], tns[3]);
+  F.tt = make_float4(tt[0], tt[1], tt[2], tt[3]);
+  F.ttb = make_float4(ttb[0], ttb[1], ttb[2], ttb[3]);
+  F.te_w = (fw & 1) ? R.aex_w * ex : 0.f;
+  return F;
+}
+
 // q = A p, pq = p.q, alpha = rz / pq
-__global__ void __launch_bounds__(128) k_mg0_spmv(MixedGrid G, MgLevel L, const float* __restrict__ p,
+__global__ void __launch_bounds__(128, 6) k_mg0_spmv(MixedGrid G, MgLevel L, Ops0 O, const float* __restrict__ p,
                                                   float* __restrict__ q, MgScalars* S, RedBuf rb) {
   if (!S->active) return;
   const P0 t = p0_pos(G);
@@ -346,45 +426,48 @@ __global__ void __launch_bounds__(128) k_mg0_spmv(MixedGrid G, MgLevel L, const 
   const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
   const long long px = G.px, pl = G.plane;
   Acc2 acc;
-  float4 pc = zero4(), pb = zero4(), ttb = zero4();
+  float4 pc = zero4(), pb = zero4();
+  uchar4 fbel = make_uchar4(0, 0, 0, 0);
+  const Row0 R = row0(O, t);
   if (t.live) {
     pc = ld4(p + t.base);
     pb = t.k0 > 1 ? ld4(p + t.base - pl) : pc;
-    if (t.k0 > 1) ttb = ld4(L.tt + t.base - pl);
+    if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
   }
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += pl) {
-    float4 pt = pc, ps = zero4(), pn = zero4(), te = zero4(), tn = zero4(), tns = zero4(), tt = zero4();
-    float lft = 0.f, tlft = 0.f, rgt = 0.f;
+    float4 pt = pc, ps = zero4(), pn = zero4();
+    float lft = 0.f, rgt = 0.f;
+    uchar4 f4 = make_uchar4(0, 0, 0, 0), fs4 = f4;
+    int fw = 0;
     if (t.live) {
       if (k < G.nz) pt = ld4(p + base + pl);
       ps = ld4(p + base - px);
       pn = ld4(p + base + px);
-      te = ld4(L.te + base);
-      tn = ld4(L.tn + base);
-      tns = ld4(L.tn + base - px);
-      tt = ld4(L.tt + base);
+      f4 = ldb4(O.fb + base);
+      fs4 = ldb4(O.fb + base - px);
       if (lane == 0) {
         lft = __ldg(p + base - 1);
-        tlft = __ldg(L.te + base - 1);
+        fw = O.fb[base - 1];
       }
       if (fetch_right) rgt = __ldg(p + base + 4);
     }
     float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
-    float te_left = __shfl_up_sync(0xffffffffu, te.w, 1);
+    const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, fw);
+    float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
     if (lane == 0) {
       left = lft;
-      te_left = tlft;
+      te_left = Fc.te_w;
     }
     if (fetch_right) right = rgt;
-    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, te, te_left, tn, tns, tt, ttb);
+    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
     if (t.live) {
       st4(q + base, u);
       acc.add4(pc, u);
     }
     pb = pc;
     pc = pt;
-    ttb = tt;
+    fbel = f4;
   }
   double s[1] = {(double)acc.s + (double)acc.e}, m[1] = {0.0}, out[1];
   if (grid_reduce<1, 0>(s, m, rb.partials, rb.ticket, out) && lin_tid() == 0) {
@@ -399,7 +482,7 @@ __global__ void __launch_bounds__(128) k_mg0_spmv(MixedGrid G, MgLevel L, const 
 }
 
 // res = r - A t on level 0 (the residual of the pre-smoothed iterate)
-__global__ void __launch_bounds__(128) k_mg0_residual(MixedGrid G, MgLevel L, const float* __restrict__ r,
+__global__ void __launch_bounds__(128, 6) k_mg0_residual(MixedGrid G, MgLevel L, Ops0 O, const float* __restrict__ r,
                                                       float* __restrict__ res, const MgScalars* S, int start) {
   if (!start && !S->active) return;
   const P0 t = p0_pos(G);
@@ -407,43 +490,46 @@ __global__ void __launch_bounds__(128) k_mg0_residual(MixedGrid G, MgLevel L, co
   const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
   const long long px = G.px, pl = G.plane;
   const float* __restrict__ x = L.t;
-  float4 pc = zero4(), pb = zero4(), ttb = zero4();
+  float4 pc = zero4(), pb = zero4();
+  uchar4 fbel = make_uchar4(0, 0, 0, 0);
+  const Row0 R = row0(O, t);
   if (t.live) {
     pc = ld4(x + t.base);
     pb = t.k0 > 1 ? ld4(x + t.base - pl) : pc;
-    if (t.k0 > 1) ttb = ld4(L.tt + t.base - pl);
+    if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
   }
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += pl) {
-    float4 pt = pc, ps = zero4(), pn = zero4(), te = zero4(), tn = zero4(), tns = zero4(), tt = zero4(), rr = zero4();
-    float lft = 0.f, tlft = 0.f, rgt = 0.f;
+    float4 pt = pc, ps = zero4(), pn = zero4(), rr = zero4();
+    float lft = 0.f, rgt = 0.f;
+    uchar4 f4 = make_uchar4(0, 0, 0, 0), fs4 = f4;
+    int fw = 0;
     if (t.live) {
       if (k < G.nz) pt = ld4(x + base + pl);
       ps = ld4(x + base - px);
       pn = ld4(x + base + px);
-      te = ld4(L.te + base);
-      tn = ld4(L.tn + base);
-      tns = ld4(L.tn + base - px);
-      tt = ld4(L.tt + base);
+      f4 = ldb4(O.fb + base);
+      fs4 = ldb4(O.fb + base - px);
       rr = ld4(r + base);
       if (lane == 0) {
         lft = __ldg(x + base - 1);
-        tlft = __ldg(L.te + base - 1);
+        fw = O.fb[base - 1];
       }
       if (fetch_right) rgt = __ldg(x + base + 4);
     }
     float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
-    float te_left = __shfl_up_sync(0xffffffffu, te.w, 1);
+    const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, fw);
+    float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
     if (lane == 0) {
       left = lft;
-      te_left = tlft;
+      te_left = Fc.te_w;
     }
     if (fetch_right) right = rgt;
-    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, te, te_left, tn, tns, tt, ttb);
+    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
     if (t.live) st4(res + base, make_float4(rr.x - u.x, rr.y - u.y, rr.z - u.z, rr.w - u.w));
     pb = pc;
     pc = pt;
-    ttb = tt;
+    fbel = f4;
   }
 }
 
@@ -471,7 +557,7 @@ __global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, cons
 // z = y + omega dinv (r - A y), y = t + P xc (the coarse correction added to
 // the pre-smoothed level-0 iterate, also at the neighbours), and r.z with the
 // PCG scalar updates (start: rz = rz0; otherwise beta and the stop test).
-__global__ void __launch_bounds__(128) k_mg0_prolong_smooth(MixedGrid G, MgLevel L, MgLevel C,
+__global__ void __launch_bounds__(128, 6) k_mg0_prolong_smooth(MixedGrid G, MgLevel L, Ops0 O, MgLevel C,
                                                             const float* __restrict__ r, float* __restrict__ z,
                                                             float omega, MgScalars* S, RedBuf rb, int start) {
   if (!start && !S->active) return;
@@ -498,42 +584,45 @@ __global__ void __launch_bounds__(128) k_mg0_prolong_smooth(MixedGrid G, MgLevel
   };
   auto add4 = [](const float4& a, const float4& b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); };
   Acc2 acc;
-  float4 yc = zero4(), yb = zero4(), ttb = zero4();
+  float4 yc = zero4(), yb = zero4();
+  uchar4 fbel = make_uchar4(0, 0, 0, 0);
+  const Row0 R = row0(O, t);
   if (t.live) {
     yc = add4(ld4(tv + t.base), prol4(jj, t.k0 - 1));
     yb = t.k0 > 1 ? add4(ld4(tv + t.base - pl), prol4(jj, t.k0 - 2)) : yc;
-    if (t.k0 > 1) ttb = ld4(L.tt + t.base - pl);
+    if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
   }
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += pl) {
     const int kk = k - 1;
-    float4 yt = yc, ys = zero4(), yn = zero4(), te = zero4(), tn = zero4(), tns = zero4(), tt = zero4(),
+    float4 yt = yc, ys = zero4(), yn = zero4(),
            dv = zero4(), rr = zero4();
-    float lft = 0.f, tlft = 0.f, rgt = 0.f;
+    float lft = 0.f, rgt = 0.f;
+    uchar4 f4 = make_uchar4(0, 0, 0, 0), fs4 = f4;
+    int fw = 0;
     if (t.live) {
       if (k < G.nz) yt = add4(ld4(tv + base + pl), prol4(jj, kk + 1));
       ys = add4(ld4(tv + base - px), prol4(jj - 1, kk));
       yn = add4(ld4(tv + base + px), prol4(jj + 1, kk));
-      te = ld4(L.te + base);
-      tn = ld4(L.tn + base);
-      tns = ld4(L.tn + base - px);
-      tt = ld4(L.tt + base);
+      f4 = ldb4(O.fb + base);
+      fs4 = ldb4(O.fb + base - px);
       dv = ld4(L.dinv + base);
       rr = ld4(r + base);
       if (lane == 0) {
         lft = i0 > 0 ? __ldg(tv + base - 1) + cval((i0 - 1) >> 1, jj >> 1, kk >> 1) : 0.f;
-        tlft = __ldg(L.te + base - 1);
+        fw = O.fb[base - 1];
       }
       if (fetch_right) rgt = i0 + 4 < L.nx ? __ldg(tv + base + 4) + cval((i0 + 4) >> 1, jj >> 1, kk >> 1) : 0.f;
     }
     float left = __shfl_up_sync(0xffffffffu, yc.w, 1), right = __shfl_down_sync(0xffffffffu, yc.x, 1);
-    float te_left = __shfl_up_sync(0xffffffffu, te.w, 1);
+    const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, fw);
+    float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
     if (lane == 0) {
       left = lft;
-      te_left = tlft;
+      te_left = Fc.te_w;
     }
     if (fetch_right) right = rgt;
-    const float4 u = face_apply(yc, left, right, ys, yn, yb, yt, te, te_left, tn, tns, tt, ttb);
+    const float4 u = face_apply(yc, left, right, ys, yn, yb, yt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
     float zz[4];
 #pragma unroll
     for (int q = 0; q < 4; q++)
@@ -545,7 +634,7 @@ __global__ void __launch_bounds__(128) k_mg0_prolong_smooth(MixedGrid G, MgLevel
     }
     yb = yc;
     yc = yt;
-    ttb = tt;
+    fbel = f4;
   }
   double s[1] = {(double)acc.s + (double)acc.e}, m[1] = {0.0}, out[1];
   if (grid_reduce<1, 0>(s, m, rb.partials, rb.ticket, out) && lin_tid() == 0) {
@@ -607,6 +696,18 @@ __global__ void k_mgp_apply(MgLevel L, Dims d, const float* __restrict__ e, doub
   }
 }
 
+Ops0 ops0(const MgHierarchy& H) {
+  Ops0 O;
+  O.fb = H.fb0;
+  O.aex = H.aex;
+  O.dxr = H.dxr;
+  O.dy = H.dy;
+  O.ayn = H.ayn;
+  O.dz = H.dz;
+  O.azt = H.azt;
+  return O;
+}
+
 dim3 g0_grid(const MixedGrid& G) {
   return dim3((unsigned)((G.ng + 31) / 32), (unsigned)((G.ny + 3) / 4), (unsigned)((G.nz + G.kc - 1) / G.kc));
 }
@@ -619,13 +720,14 @@ static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, co
                                cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const MgLevel& C = H.lv[1];
-  k_mg0_residual<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.r, L.b, S, start);
+  k_mg0_residual<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, ops0(H), v.r, L.b, S, start);
   note_launch();
   k_mg_restrict<<<mg_grid(C), dim3(32, 8), 0, st>>>(L, C, L.b, C.b, H.cscale);
   note_launch();
   cudaError_t e = vcycle(H, 1, C.b, C.x, st);
   if (e != cudaSuccess) return e;
-  k_mg0_prolong_smooth<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, C, v.r, v.z, H.omega, S, rb, start);
+  k_mg0_prolong_smooth<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, ops0(H), C, v.r, v.z, H.omega, S, rb,
+                                                             start);
   note_launch();
   k_mg0_direction<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, v.z, v.p, S, start);
   note_launch();
@@ -645,7 +747,7 @@ cudaError_t mg_pcg_start(const MgHierarchy& H, const double* rv, double scale, M
 
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
-  k_mg0_spmv<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.p, v.q, S, rb);
+  k_mg0_spmv<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, ops0(H), v.p, v.q, S, rb);
   note_launch();
   k_mg0_update<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.p, v.q, v.e, v.r, H.omega, S);
   note_launch();
