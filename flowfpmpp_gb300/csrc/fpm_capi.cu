@@ -737,12 +737,13 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
 }
 
 // FP32 PCG preconditioned by the aggregation multigrid V-cycle of fpm_mg.cu,
-// in the same FP64 refinement as mixed_solve: each outer step loads the
-// projected FP64 true residual (scaled to unit max-norm), runs PCG until its
-// preconditioned residual norm r.z has dropped by kMgDrop^2 (or kMgInnerMax
-// iterations), adds the correction to phi in FP64 and recomputes the true
-// residual; convergence is the reference's max-norm test.  The right-hand
-// sides are solved one after the other.
+// in the same FP64 refinement as mixed_solve: each outer step of a
+// right-hand side loads its projected FP64 true residual (scaled to unit
+// max-norm), runs PCG until the preconditioned residual norm r.z has dropped
+// by kMgDrop^2 (or kMgInnerMax iterations), adds the correction to phi in
+// FP64 and recomputes the true residual; convergence is the reference's
+// max-norm test.  All right-hand sides iterate in the same launches; each
+// has its own outer steps.
 constexpr double kMgDrop = 1e-4;
 constexpr int kMgInnerMax = 400;
 
@@ -759,6 +760,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   Trace tr("multigrid setup");
   MgHierarchy H;
   std::memset(&H, 0, sizeof(H));
+  H.nrhs = nrhs;
   H.nu = (int)env_double("FPM_MG_NU", 1);
   H.omega = (float)env_double("FPM_MG_OMEGA", 0.9);
   H.coarse_sweeps = (int)env_double("FPM_MG_COARSE_SWEEPS", 40);
@@ -776,6 +778,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     L.nx = nx;
     L.ny = ny;
     L.nz = nz;
+    L.zc = mg_zchunks(nx, ny, nz, nrhs);
     if (H.nlev == 0) {
       L.off = 4 + H.g0.px;
       L.sy = H.g0.px;
@@ -791,9 +794,11 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     L.tn = zeros(L.alloc);
     L.tt = zeros(L.alloc);
     L.dinv = zeros(L.alloc);
-    L.t = zeros(L.alloc);
-    L.x = H.nlev == 0 ? nullptr : zeros(L.alloc);
-    L.b = zeros(L.alloc);  // level 0: the residual of the pre-smoothed iterate
+    for (int m = 0; m < nrhs; m++) {
+      L.t[m] = zeros(L.alloc);
+      L.x[m] = H.nlev == 0 ? nullptr : zeros(L.alloc);
+      L.b[m] = zeros(L.alloc);  // level 0: the residual of the pre-smoothed iterate
+    }
     H.nlev++;
     if (L.n() <= 1024 || H.nlev == kMgMaxLevels) break;
     nx = (nx + 1) / 2;
@@ -814,79 +819,119 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   CUDA_TRY(mg_setup(H, d, solid, ax, st));
   const long long n0 = H.lv[0].alloc;
   MgVecs v;
-  v.r = zeros(n0);
-  v.z = zeros(n0);
-  v.p = zeros(n0);
-  v.q = zeros(n0);
-  v.e = zeros(n0);
-  RedBuf rb;
-  rb.max_blocks = mg_grid_blocks(H.g0);
-  rb.partials = A.get<double>((size_t)rb.max_blocks);
-  rb.ticket = A.get<unsigned int>(1);
-  CUDA_TRY(cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned int), st));
-  MgScalars* S = A.get<MgScalars>(1);
-  double* r64 = A.get<double>(d.ncell());
-  SolveScalars* S64 = A.get<SolveScalars>(1);
-  CUDA_TRY(cudaMemsetAsync(S64, 0, sizeof(SolveScalars), st));
+  std::memset(&v, 0, sizeof(v));
+  DPtr4 r64{}, phis{};
+  SolveScalars* S64[kMaxRhs] = {};
+  for (int m = 0; m < nrhs; m++) {
+    v.r[m] = zeros(n0);
+    v.z[m] = zeros(n0);
+    v.p[m] = zeros(n0);
+    v.q[m] = zeros(n0);
+    v.e[m] = zeros(n0);
+    r64.p[m] = A.get<double>(d.ncell());
+    phis.p[m] = phi[m];
+    S64[m] = A.get<SolveScalars>(1);
+    CUDA_TRY(cudaMemsetAsync(S64[m], 0, sizeof(SolveScalars), st));
+  }
+  MgRed rb;
+  rb.partials = A.get<double>((size_t)mg_red_partials(H.g0));
+  rb.tickets = A.get<unsigned int>(kMaxRhs);
+  CUDA_TRY(cudaMemsetAsync(rb.tickets, 0, kMaxRhs * sizeof(unsigned int), st));
+  MgScalars* S = A.get<MgScalars>(kMaxRhs);
+  CUDA_TRY(cudaMemsetAsync(S, 0, kMaxRhs * sizeof(MgScalars), st));
   MgScalars* hS = nullptr;
-  CUDA_TRY(cudaMallocHost(&hS, sizeof(MgScalars)));
+  CUDA_TRY(cudaMallocHost(&hS, kMaxRhs * sizeof(MgScalars)));
   struct HostFree {
     void* p;
     ~HostFree() { cudaFreeHost(p); }
   } hf{hS};
-  const int chunk_len = ci < 1 ? 1 : (ci > 50 ? 50 : ci);
-  for (int m = 0; m < nrhs; m++) {
-    Trace ti("multigrid PCG");
-    auto true_res = [&]() {
-      CUDA_TRY(launch_true_residual(d, phi[m], src[m], diag, rdiag, r64, nullptr, c, ax, 0, S64, cm.rb, st));
-      return read_scalars(S64, st).res;
-    };
-    double res = true_res(), best = res;
-    int total = 0, stall = 0;
-    ChunkGraphs graphs(6 + (H.nlev - 2) * (2 * H.nu + 1) + 1);
-    while (res > tol && res == res && total < max_sweeps) {
-      const double scale = res > 0 ? 1.0 / res : 1.0;
+  Trace ti("multigrid PCG");
+  auto true_res = [&](int m) {
+    CUDA_TRY(launch_true_residual(d, phi[m], src[m], diag, rdiag, r64.p[m], nullptr, c, ax, 0, S64[m], cm.rb, st));
+    return read_scalars(S64[m], st).res;
+  };
+  double res[kMaxRhs] = {}, best[kMaxRhs] = {}, scale[kMaxRhs] = {};
+  int stall[kMaxRhs] = {}, iters[kMaxRhs] = {};
+  bool live[kMaxRhs] = {};
+  // (Re)start the inner PCG of the right-hand sides in set from their
+  // current true residuals: drop by kMgDrop, or just far enough for the
+  // tolerance (with a margin of 30 for the max-norm versus the
+  // preconditioned norm).
+  auto start = [&](unsigned set) {
+    for (int m = 0; m < nrhs; m++) {
+      if (!((set >> m) & 1u)) continue;
+      scale[m] = res[m] > 0 ? 1.0 / res[m] : 1.0;
+      const double need = tol / (30.0 * res[m]);
+      const double drop = need > kMgDrop ? (need < 0.5 ? need : 0.5) : kMgDrop;
       MgScalars h0;
       std::memset(&h0, 0, sizeof(h0));
-      // drop by kMgDrop, or just far enough for the tolerance (with a margin
-      // of 30 for the max-norm versus the preconditioned norm)
-      const double need = tol / (30.0 * res);
-      const double drop = need > kMgDrop ? (need < 0.5 ? need : 0.5) : kMgDrop;
       h0.tol2 = drop * drop;
-      CUDA_TRY(cudaMemcpyAsync(S, &h0, sizeof(MgScalars), cudaMemcpyHostToDevice, st));
-      CUDA_TRY(mg_pcg_start(H, r64, scale, v, S, rb, st));
-      int inner = 0;
-      for (;;) {
-        int chunk = chunk_len;
-        if (chunk > max_sweeps - total) chunk = max_sweeps - total;
-        if (chunk <= 0) break;
-        {
-          TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
-          graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
-        }
-        CUDA_TRY(cudaMemcpyAsync(hS, S, sizeof(MgScalars), cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        inner = hS->iters;
-        if (!hS->active || inner >= kMgInnerMax) break;
-      }
-      total += inner;
-      CUDA_TRY(mg_pcg_apply(H, d, v, scale, phi[m], st));
-      const double prev = res;
-      res = true_res();
-      if (verbose())
-        std::fprintf(stderr, "fpm pcg_mg: rhs %d inner %d total %d residual %.3e\n", m, inner, total, res);
-      if (res < 0.99 * best) {
-        best = res;
-        stall = 0;
-      } else if (++stall >= kStallUpdates) {
-        break;
-      }
-      if (inner == 0 && !(res < prev)) break;  // no progress possible
+      h0.active = 1;
+      CUDA_TRY(cudaMemcpyAsync(S + m, &h0, sizeof(MgScalars), cudaMemcpyHostToDevice, st));
     }
-    sweeps_out[m] = total;
+    CUDA_TRY(mg_pcg_start(H, r64, scale, set, v, S, rb, st));
+  };
+  unsigned set = 0;
+  for (int m = 0; m < nrhs; m++) {
+    res[m] = best[m] = true_res(m);
+    live[m] = res[m] > tol && res[m] == res[m];
+    if (live[m]) set |= 1u << m;
+  }
+  if (set) start(set);
+  const int chunk_len = ci < 1 ? 1 : (ci > 50 ? 50 : ci);
+  int total = 0;
+  ChunkGraphs graphs(6 + (H.nlev - 2) * (2 * H.nu + 1) + 1);
+  while (set && total < max_sweeps) {
+    int chunk = chunk_len;
+    if (chunk > max_sweeps - total) chunk = max_sweeps - total;
+    {
+      TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
+      graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
+    }
+    total += chunk;
+    CUDA_TRY(cudaMemcpyAsync(hS, S, kMaxRhs * sizeof(MgScalars), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    // Which right-hand sides have finished an outer step?
+    unsigned upd = 0;
+    for (int m = 0; m < nrhs; m++)
+      if (live[m] && (!hS[m].active || hS[m].iters >= kMgInnerMax || total >= max_sweeps)) upd |= 1u << m;
+    if (!upd) continue;
+    static_assert(offsetof(MgScalars, dir) == offsetof(MgScalars, active) + sizeof(int), "active, dir adjacent");
+    const int zero[2] = {0, 0};
+    for (int m = 0; m < nrhs; m++)  // park them until their restart (active and dir cleared)
+      if ((upd >> m) & 1u) CUDA_TRY(cudaMemcpyAsync(&S[m].active, zero, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(mg_pcg_apply(H, d, v, scale, upd, phis, st));
+    unsigned restart = 0;
+    for (int m = 0; m < nrhs; m++) {
+      if (!((upd >> m) & 1u)) continue;
+      const int inner = hS[m].iters;
+      iters[m] += inner;
+      const double prev = res[m];
+      res[m] = true_res(m);
+      if (verbose())
+        std::fprintf(stderr, "fpm pcg_mg: rhs %d inner %d total %d residual %.3e\n", m, inner, iters[m], res[m]);
+      if (res[m] < 0.99 * best[m]) {
+        best[m] = res[m];
+        stall[m] = 0;
+      } else {
+        stall[m]++;
+      }
+      const bool stop = !(res[m] > tol) || !(res[m] == res[m]) || stall[m] >= kStallUpdates ||
+                        (inner == 0 && !(res[m] < prev));  // no progress possible
+      if (stop) {
+        live[m] = false;
+        set &= ~(1u << m);
+      } else {
+        restart |= 1u << m;
+      }
+    }
+    if (restart && total < max_sweeps) start(restart);
+  }
+  for (int m = 0; m < nrhs; m++) {
+    sweeps_out[m] = iters[m];
     // stopped above the tolerance (FP32 can no longer resolve the error at
     // the FP64 rounding floor of the residual): FP64 PCG finishes
-    to_fp64[m] = res > tol ? 1 : 0;
+    to_fp64[m] = res[m] > tol ? 1 : 0;
   }
 }
 
@@ -2156,9 +2201,12 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         const double zc2[2] = {0.25, 0.75}, dz2[2] = {0.5, 0.5};
         double* dzc = A.upload(zc2, 2);
         double* ddz = A.upload(dz2, 2);
+        // jobs[job_first[n] .. job_first[n + 1]) are the directions of one
+        // frame, solved together (they share the solid flags and the axes)
         std::vector<SolveArgs> jobs;
-        std::vector<size_t> job_q;
+        std::vector<size_t> job_q, job_first;
         for (int f = 0; f < nframes; f++) {
+          if (to64[2 * (size_t)f] || to64[2 * (size_t)f + 1]) job_first.push_back(jobs.size());
           for (int r = 0; r < 2; r++) {
             const size_t q = 2 * (size_t)f + r;
             if (!to64[q]) continue;
@@ -2190,12 +2238,14 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
             job_q.push_back(q);
           }
         }
+        job_first.push_back(jobs.size());
+        const size_t ngroups = job_first.size() - 1;
         CUDA_TRY(cudaStreamSynchronize(st));
         // The frames are small next to the GPU, so several of them are solved
         // at once: host worker threads, one stream each.
         int dev = 0;
         CUDA_TRY(cudaGetDevice(&dev));
-        const int nworkers = (int)std::min<size_t>(jobs.size(), (size_t)env_double("FPM_FRAMES_WORKERS", 12));
+        const int nworkers = (int)std::min<size_t>(ngroups, (size_t)env_double("FPM_FRAMES_WORKERS", 12));
         std::vector<int> sws(jobs.size(), 0);
         std::vector<double> rrs(jobs.size(), 0.0);
         std::vector<std::string> errs(nworkers);
@@ -2208,8 +2258,10 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
             try {
               CUDA_TRY(cudaSetDevice(dev));
               CUDA_TRY(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking));
-              for (size_t j = next_job++; j < jobs.size(); j = next_job++)
-                solve_multi_dev(1, &jobs[j], &sws[j], &rrs[j], ws);
+              for (size_t n = next_job++; n < ngroups; n = next_job++) {
+                const size_t j = job_first[n];
+                solve_multi_dev((int)(job_first[n + 1] - j), &jobs[j], &sws[j], &rrs[j], ws);
+              }
             } catch (const Error& e) {
               codes[w] = e.code;
               errs[w] = e.msg;
@@ -2223,7 +2275,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         for (size_t j = 0; j < jobs.size(); j++) {
           extra_its[job_q[j]] = sws[j];
           if (verbose())
-            std::fprintf(stderr, "fpm frames: frame %zu direction %zu FP64 PCG %d iterations, residual %.3e\n",
+            std::fprintf(stderr, "fpm frames: frame %zu direction %zu solved alone: %d iterations, residual %.3e\n",
                          job_q[j] / 2, job_q[j] % 2, sws[j], rrs[j]);
         }
       }

@@ -242,17 +242,20 @@ int operator_residual_noalloc(const double* phi, const double* src, const double
 void note_launch();
 
 // ---- aggregation multigrid preconditioner (fpm_mg.cu) ---------------------
+// Every right-hand side has its own vectors on every level; the kernels of a
+// V-cycle cover all of them in one launch (blockIdx.z = chunk + chunks x rhs).
 struct MgLevel {
   int nx, ny, nz;
+  int zc;                      // chunks of planes per right-hand side (one-thread-per-cell kernels)
   long long off, sy, sz;       // cell (i, j, k) (0-based) at off + i + sy j + sz k
   long long alloc;             // elements per array
   float *te, *tn, *tt, *dinv;  // face transmissibilities, inverse diagonal
-  float *x, *b, *t;            // solution, right-hand side, smoothing scratch
+  float *x[kMaxRhs], *b[kMaxRhs], *t[kMaxRhs];  // per right-hand side: solution, right-hand side, scratch
   __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
 };
 constexpr int kMgMaxLevels = 16;
 struct MgHierarchy {
-  int nlev;
+  int nlev, nrhs;
   MgLevel lv[kMgMaxLevels];
   MixedGrid g0;       // level 0 uses the FP32 layout of the mixed solver (float4 groups, zero halo)
   // level 0 operator for the float4 kernels: open-face bits per cell (1 east,
@@ -263,24 +266,34 @@ struct MgHierarchy {
   float *dy, *ayn;    // index j - 1
   float *dz, *azt;    // index k - 1
   int nu;             // pre- and post-smoothing sweeps
-  int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block)
+  int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block per right-hand side)
   float omega;        // Jacobi weight
   float cscale;       // coarse-correction scale (1 = plain Galerkin correction)
 };
-struct MgVecs {
-  float *r, *z, *p, *q, *e;
+struct MgVecs {  // level-0 PCG vectors per right-hand side
+  float *r[kMaxRhs], *z[kMaxRhs], *p[kMaxRhs], *q[kMaxRhs], *e[kMaxRhs];
 };
-struct MgScalars {
+struct MgScalars {  // one per right-hand side
   double rz, rz0, pq, alpha, beta, tol2;
   int active, dir, iters, pad;
 };
+// Per-right-hand-side grid reductions: partials holds kMaxRhs x (level-0
+// blocks per right-hand side) doubles, tickets kMaxRhs counters (zero between
+// launches).
+struct MgRed {
+  double* partials;
+  unsigned int* tickets;
+};
+long long mg_red_partials(const MixedGrid& G);
+// A launch covers the right-hand sides whose bit is set in mask and whose
+// MgScalars::active is set.
 cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const Axes& ax, cudaStream_t st);
-cudaError_t mg_pcg_start(const MgHierarchy& H, const double* rv, double scale, MgVecs& v, MgScalars* S,
-                         const RedBuf& rb, cudaStream_t st);
-cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, cudaStream_t st);
-cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, double scale, double* phi,
-                         cudaStream_t st);
-int mg_grid_blocks(const MixedGrid& G);
+cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* scale, unsigned mask, MgVecs& v,
+                         MgScalars* S, const MgRed& rb, cudaStream_t st);
+cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, cudaStream_t st);
+cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const double* scale, unsigned mask,
+                         const DPtr4& phi, cudaStream_t st);
+int mg_zchunks(int nx, int ny, int nz, int nrhs);
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,

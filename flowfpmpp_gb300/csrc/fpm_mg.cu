@@ -28,8 +28,18 @@ __device__ __forceinline__ long long ix(const MgLevel& L, int i, int j, int k) {
   return L.off + i + L.sy * j + L.sz * k;
 }
 
+// Grids of the one-thread-per-cell kernels: (x, y) tiles and L.zc strided
+// chunks of planes per right-hand side; blockIdx.z = chunk + zc * rhs.
+#define MG_RHS(L) const int mrhs = (int)blockIdx.z / (L).zc
+#define MG_SKIP(m) \
+  if (!(((mask >> (m)) & 1u) && S[m].active)) return
+
+// Pointers of one vector per right-hand side.
+struct Vec4 {
+  float* p[kMaxRhs];
+};
 #define MG_CELLS(L)                                                                       \
-  for (int k = blockIdx.z; k < (L).nz; k += gridDim.z)                                    \
+  for (int k = (int)blockIdx.z % (L).zc; k < (L).nz; k += (L).zc)                         \
     for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < (L).ny; j += gridDim.y * blockDim.y) \
       for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (L).nx; i += gridDim.x * blockDim.x)
 
@@ -125,8 +135,13 @@ __device__ __forceinline__ float apply_a(const MgLevel& L, const float* __restri
 }
 
 // xo = (first ? 0 : x) + omega dinv (b - A x)   (first: x is taken as 0)
-__global__ void k_mg_smooth(MgLevel L, const float* __restrict__ x, const float* __restrict__ b,
-                            float* __restrict__ xo, float omega, int first) {
+__global__ void k_mg_smooth(MgLevel L, Vec4 xv, Vec4 bv, Vec4 xov, float omega, int first, const MgScalars* S,
+                            unsigned mask) {
+  MG_RHS(L);
+  MG_SKIP(mrhs);
+  const float* __restrict__ x = xv.p[mrhs];
+  const float* __restrict__ b = bv.p[mrhs];
+  float* __restrict__ xo = xov.p[mrhs];
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const float w = omega * L.dinv[c];
@@ -137,8 +152,13 @@ __global__ void k_mg_smooth(MgLevel L, const float* __restrict__ x, const float*
 // bc = scale x restriction of b - A x: one thread per coarse cell sums the
 // residuals of its (up to 8) fine cells.  scale > 1 over-corrects with the
 // coarse solution (the cycle stays linear and symmetric).
-__global__ void k_mg_resrestrict(MgLevel F, MgLevel C, const float* __restrict__ x, const float* __restrict__ b,
-                                 float* __restrict__ bc, float scale) {
+__global__ void k_mg_resrestrict(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bcv, float scale, const MgScalars* S,
+                                 unsigned mask) {
+  MG_RHS(C);
+  MG_SKIP(mrhs);
+  const float* __restrict__ x = xv.p[mrhs];
+  const float* __restrict__ b = bv.p[mrhs];
+  float* __restrict__ bc = bcv.p[mrhs];
   MG_CELLS(C) {
     float s = 0.f;
     for (int o = 0; o < 8; o++) {
@@ -153,7 +173,12 @@ __global__ void k_mg_resrestrict(MgLevel F, MgLevel C, const float* __restrict__
 }
 
 // bc = scale x the sum of the fine residuals rf of each aggregate.
-__global__ void k_mg_restrict(MgLevel F, MgLevel C, const float* __restrict__ rf, float* __restrict__ bc, float scale) {
+__global__ void k_mg_restrict(MgLevel F, MgLevel C, Vec4 rfv, Vec4 bcv, float scale, const MgScalars* S,
+                              unsigned mask) {
+  MG_RHS(C);
+  MG_SKIP(mrhs);
+  const float* __restrict__ rf = rfv.p[mrhs];
+  float* __restrict__ bc = bcv.p[mrhs];
   MG_CELLS(C) {
     float s = 0.f;
     for (int o = 0; o < 8; o++) {
@@ -165,11 +190,16 @@ __global__ void k_mg_restrict(MgLevel F, MgLevel C, const float* __restrict__ rf
 }
 
 // xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
-// added on the fly, also at the neighbours): k_mg_prolong and the first
+// added on the fly, also at the neighbours): prolongation and the first
 // post-smoothing sweep in one pass.
-__global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, const float* __restrict__ x,
-                                    const float* __restrict__ xcrs, const float* __restrict__ b,
-                                    float* __restrict__ xo, float omega) {
+__global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv, Vec4 xov, float omega,
+                                    const MgScalars* S, unsigned mask) {
+  MG_RHS(F);
+  MG_SKIP(mrhs);
+  const float* __restrict__ x = xv.p[mrhs];
+  const float* __restrict__ xcrs = xcv.p[mrhs];
+  const float* __restrict__ b = bv.p[mrhs];
+  float* __restrict__ xo = xov.p[mrhs];
   const long long sy = F.sy, sz = F.sz, cy = C.sy, cz = C.sz;
   MG_CELLS(F) {
     const long long c = ix(F, i, j, k), pc = ix(C, i >> 1, j >> 1, k >> 1);
@@ -186,10 +216,14 @@ __global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, const float* __restric
 }
 
 // Coarsest level (at most 1024 cells, compact layout): nsweeps weighted
-// Jacobi sweeps from 0 in one block, with the level's operator, right-hand
-// side and iterate in shared memory.
-__global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, const float* __restrict__ b, float* __restrict__ x,
-                                                    float omega, int nsweeps) {
+// Jacobi sweeps from 0 in one block per right-hand side, with the level's
+// operator, right-hand side and iterate in shared memory.
+__global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, Vec4 bv, Vec4 xv, float omega, int nsweeps,
+                                                    const MgScalars* S, unsigned mask) {
+  const int mrhs = blockIdx.x;
+  MG_SKIP(mrhs);
+  const float* __restrict__ b = bv.p[mrhs];
+  float* __restrict__ x = xv.p[mrhs];
   __shared__ float te[1024], tn[1024], tt[1024], wd[1024], bb[1024], xa[1024], xb[1024];
   const int n = (int)L.n();
   const int c = threadIdx.x;
@@ -229,12 +263,12 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, const float* __re
   if (c < n) x[c] = a[c];
 }
 
-dim3 mg_grid(const MgLevel& L) {
-  const int gx = (L.nx + 31) / 32, gy = (L.ny + 7) / 8;
-  long long gz = (152LL * 16 + (long long)gx * gy - 1) / ((long long)gx * gy);
-  if (gz > L.nz) gz = L.nz;
-  if (gz < 1) gz = 1;
-  return dim3(gx, gy, (unsigned)gz);
+dim3 mg_grid(const MgLevel& L) { return dim3((L.nx + 31) / 32, (L.ny + 7) / 8, (unsigned)L.zc); }
+dim3 rhs_grid(const MgLevel& L, int nrhs) { return dim3((L.nx + 31) / 32, (L.ny + 7) / 8, (unsigned)(L.zc * nrhs)); }
+Vec4 vec4(float* const (&p)[kMaxRhs]) {
+  Vec4 v;
+  for (int m = 0; m < kMaxRhs; m++) v.p[m] = p[m];
+  return v;
 }
 
 }  // namespace
@@ -256,46 +290,38 @@ cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const 
   return cudaGetLastError();
 }
 
-// x = V-cycle(b) on level l.  Smoothing alternates between x and the level's
-// scratch t; the first write goes to t, and 2 nu - 1 sweeps later the result
-// is in x.
-static cudaError_t vcycle(const MgHierarchy& H, int l, const float* b, float* x, cudaStream_t st) {
+// x = V-cycle(b) on level l >= 1 for every right-hand side at once.
+// Smoothing alternates between x and the level's scratch t; the first write
+// goes to t, and 2 nu - 1 sweeps later the result is in x.
+static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsigned mask, cudaStream_t st) {
   const MgLevel& L = H.lv[l];
-  const dim3 blk(32, 8), g = mg_grid(L);
+  const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
+  const Vec4 b = vec4(L.b), x = vec4(L.x), t = vec4(L.t);
   if (l == H.nlev - 1) {
-    k_mg_coarse<<<1, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps);
+    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask);
     note_launch();
     return cudaGetLastError();
   }
-  float* cur = L.t;
-  float* oth = x;
-  k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, cur, H.omega, 1);
+  Vec4 cur = t, oth = x;
+  k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, cur, H.omega, 1, S, mask);
   note_launch();
   for (int s = 1; s < H.nu; s++) {
-    k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0);
+    k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
     note_launch();
-    float* t = cur;
-    cur = oth;
-    oth = t;
+    std::swap(cur, oth);
   }
   const MgLevel& C = H.lv[l + 1];
-  k_mg_resrestrict<<<mg_grid(C), blk, 0, st>>>(L, C, cur, b, C.b, H.cscale);
+  k_mg_resrestrict<<<rhs_grid(C, H.nrhs), blk, 0, st>>>(L, C, cur, b, vec4(C.b), H.cscale, S, mask);
   note_launch();
-  cudaError_t e = vcycle(H, l + 1, C.b, C.x, st);
+  cudaError_t e = vcycle(H, l + 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, C.x, b, oth, H.omega);
+  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask);
   note_launch();
-  {
-    float* t = cur;
-    cur = oth;
-    oth = t;
-  }
+  std::swap(cur, oth);
   for (int s = 1; s < H.nu; s++) {
-    k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0);
+    k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
     note_launch();
-    float* t = cur;
-    cur = oth;
-    oth = t;
+    std::swap(cur, oth);
   }
   return cudaGetLastError();
 }
@@ -323,20 +349,53 @@ struct Acc2 {
 
 // Thread position on level 0: group g (cells 4g .. 4g+3, 0-based) of row j
 // (1-based), planes k0..k1 (1-based), as in the mixed solver's kernels.
+// blockIdx.z = chunk of kc planes + zc x right-hand side m.
 struct P0 {
-  int g, j, k0, k1;
+  int g, j, k0, k1, m, zc;
   bool live;
   long long base;
 };
 __device__ __forceinline__ P0 p0_pos(const MixedGrid& G) {
   P0 t;
+  t.zc = (G.nz + G.kc - 1) / G.kc;
+  t.m = (int)blockIdx.z / t.zc;
   t.g = blockIdx.x * 32 + threadIdx.x;
   t.j = blockIdx.y * 4 + threadIdx.y + 1;
   t.live = t.g < G.ng && t.j <= G.ny;
-  t.k0 = blockIdx.z * G.kc + 1;
+  t.k0 = ((int)blockIdx.z - t.m * t.zc) * G.kc + 1;
   t.k1 = min(G.nz, t.k0 + G.kc - 1);
   t.base = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (t.k0 - 1));
   return t;
+}
+
+// Sum of s over the blocks of right-hand side m (the zc chunks of its
+// blockIdx.z range); true in the last of them, with *out set in thread 0.
+__device__ bool rhs_reduce(double s, int m, int zc, const MgRed& rb, double* out) {
+  __shared__ bool am_last;
+  double a[1] = {s}, mm[1] = {0.0};
+  block_reduce<1, 0>(a, mm);
+  const int nb = (int)(gridDim.x * gridDim.y) * zc;
+  const int bid = (int)blockIdx.x + (int)gridDim.x * ((int)blockIdx.y + (int)gridDim.y * ((int)blockIdx.z - m * zc));
+  double* part = rb.partials + (size_t)m * nb;
+  const int tid = lin_tid();
+  if (tid == 0) {
+    part[bid] = a[0];
+    __threadfence();
+    am_last = atomicAdd(rb.tickets + m, 1u) == (unsigned int)nb - 1;
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  a[0] = 0.0;
+  for (int b = tid; b < nb; b += lin_nthreads()) a[0] += __ldcg(part + b);
+  block_reduce<1, 0>(a, mm);
+  if (tid == 0) {
+    *out = a[0];
+    rb.tickets[m] = 0u;
+    __threadfence();
+  }
+  __syncthreads();
+  return true;
 }
 
 // u = (A v) for the four cells of a group from the loaded neighbourhood.
@@ -418,10 +477,12 @@ __device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, co
 }
 
 // q = A p, pq = p.q, alpha = rz / pq
-__global__ void __launch_bounds__(128, 6) k_mg0_spmv(MixedGrid G, MgLevel L, Ops0 O, const float* __restrict__ p,
-                                                  float* __restrict__ q, MgScalars* S, RedBuf rb) {
-  if (!S->active) return;
+__global__ void __launch_bounds__(128, 6) k_mg0_spmv(MixedGrid G, Ops0 O, MgVecs v, MgScalars* S, MgRed rb,
+                                                  unsigned mask) {
   const P0 t = p0_pos(G);
+  MG_SKIP(t.m);
+  const float* __restrict__ p = v.p[t.m];
+  float* __restrict__ q = v.q[t.m];
   const int lane = threadIdx.x;
   const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
   const long long px = G.px, pl = G.plane;
@@ -469,27 +530,30 @@ __global__ void __launch_bounds__(128, 6) k_mg0_spmv(MixedGrid G, MgLevel L, Ops
     pc = pt;
     fbel = f4;
   }
-  double s[1] = {(double)acc.s + (double)acc.e}, m[1] = {0.0}, out[1];
-  if (grid_reduce<1, 0>(s, m, rb.partials, rb.ticket, out) && lin_tid() == 0) {
-    S->pq = out[0];
-    if (!(out[0] > 0) || !(S->rz > 0)) {
-      S->active = 0;
-      S->alpha = 0;
+  double out = 0.0;
+  if (rhs_reduce((double)acc.s + (double)acc.e, t.m, t.zc, rb, &out) && lin_tid() == 0) {
+    MgScalars& R = S[t.m];
+    R.pq = out;
+    if (!(out > 0) || !(R.rz > 0)) {
+      R.active = 0;
+      R.alpha = 0;
     } else {
-      S->alpha = S->rz / out[0];
+      R.alpha = R.rz / out;
     }
   }
 }
 
 // res = r - A t on level 0 (the residual of the pre-smoothed iterate)
-__global__ void __launch_bounds__(128, 6) k_mg0_residual(MixedGrid G, MgLevel L, Ops0 O, const float* __restrict__ r,
-                                                      float* __restrict__ res, const MgScalars* S, int start) {
-  if (!start && !S->active) return;
+__global__ void __launch_bounds__(128, 6) k_mg0_residual(MixedGrid G, MgLevel L, Ops0 O, MgVecs v,
+                                                      const MgScalars* S, unsigned mask) {
   const P0 t = p0_pos(G);
+  MG_SKIP(t.m);
+  const float* __restrict__ r = v.r[t.m];
+  float* __restrict__ res = L.b[t.m];
   const int lane = threadIdx.x;
   const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
   const long long px = G.px, pl = G.plane;
-  const float* __restrict__ x = L.t;
+  const float* __restrict__ x = L.t[t.m];
   float4 pc = zero4(), pb = zero4();
   uchar4 fbel = make_uchar4(0, 0, 0, 0);
   const Row0 R = row0(O, t);
@@ -535,13 +599,17 @@ __global__ void __launch_bounds__(128, 6) k_mg0_residual(MixedGrid G, MgLevel L,
 
 // e += alpha p; r -= alpha q; t = omega dinv r (the V-cycle's first
 // pre-smoothing sweep from zero)
-__global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, const float* __restrict__ p,
-                                                    const float* __restrict__ q, float* __restrict__ e,
-                                                    float* __restrict__ r, float omega, const MgScalars* S) {
-  if (!S->active) return;
-  const float a = (float)S->alpha;
+__global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, MgVecs v, float omega, const MgScalars* S,
+                                                    unsigned mask) {
   const P0 t = p0_pos(G);
+  MG_SKIP(t.m);
   if (!t.live) return;
+  const float a = (float)S[t.m].alpha;
+  const float* __restrict__ p = v.p[t.m];
+  const float* __restrict__ q = v.q[t.m];
+  float* __restrict__ e = v.e[t.m];
+  float* __restrict__ r = v.r[t.m];
+  float* __restrict__ tt = L.t[t.m];
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
     const float4 pp = ld4(p + base), qq = ld4(q + base), dv = ld4(L.dinv + base);
@@ -550,23 +618,25 @@ __global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, cons
     rr = make_float4(fmaf(-a, qq.x, rr.x), fmaf(-a, qq.y, rr.y), fmaf(-a, qq.z, rr.z), fmaf(-a, qq.w, rr.w));
     st4(e + base, ee);
     st4(r + base, rr);
-    st4(L.t + base, make_float4(omega * dv.x * rr.x, omega * dv.y * rr.y, omega * dv.z * rr.z, omega * dv.w * rr.w));
+    st4(tt + base, make_float4(omega * dv.x * rr.x, omega * dv.y * rr.y, omega * dv.z * rr.z, omega * dv.w * rr.w));
   }
 }
 
 // z = y + omega dinv (r - A y), y = t + P xc (the coarse correction added to
 // the pre-smoothed level-0 iterate, also at the neighbours), and r.z with the
 // PCG scalar updates (start: rz = rz0; otherwise beta and the stop test).
-__global__ void __launch_bounds__(128, 6) k_mg0_prolong_smooth(MixedGrid G, MgLevel L, Ops0 O, MgLevel C,
-                                                            const float* __restrict__ r, float* __restrict__ z,
-                                                            float omega, MgScalars* S, RedBuf rb, int start) {
-  if (!start && !S->active) return;
+__global__ void __launch_bounds__(128, 6) k_mg0_prolong_smooth(MixedGrid G, MgLevel L, Ops0 O, MgLevel C, MgVecs v,
+                                                            float omega, MgScalars* S, MgRed rb, unsigned mask,
+                                                            int start) {
   const P0 t = p0_pos(G);
+  MG_SKIP(t.m);
+  const float* __restrict__ r = v.r[t.m];
+  float* __restrict__ z = v.z[t.m];
   const int lane = threadIdx.x;
   const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
   const long long px = G.px, pl = G.plane;
-  const float* __restrict__ tv = L.t;
-  const float* __restrict__ xc = C.x;
+  const float* __restrict__ tv = L.t[t.m];
+  const float* __restrict__ xc = C.x[t.m];
   const int jj = t.j - 1, i0 = 4 * t.g;  // 0-based row and first cell
   // coarse value at (ci, cj, ck) or 0 outside
   auto cval = [&](int ci, int cj, int ck) -> float {
@@ -636,37 +706,41 @@ __global__ void __launch_bounds__(128, 6) k_mg0_prolong_smooth(MixedGrid G, MgLe
     yc = yt;
     fbel = f4;
   }
-  double s[1] = {(double)acc.s + (double)acc.e}, m[1] = {0.0}, out[1];
-  if (grid_reduce<1, 0>(s, m, rb.partials, rb.ticket, out) && lin_tid() == 0) {
-    const double rz = out[0];
+  double rz = 0.0;
+  if (rhs_reduce((double)acc.s + (double)acc.e, t.m, t.zc, rb, &rz) && lin_tid() == 0) {
+    MgScalars& R = S[t.m];
     if (start) {
-      S->rz = rz;
-      S->rz0 = rz;
-      S->beta = 0.0;
-      S->active = rz > 0 ? 1 : 0;
-      S->dir = S->active;
+      R.rz = rz;
+      R.rz0 = rz;
+      R.beta = 0.0;
+      R.active = rz > 0 ? 1 : 0;
+      R.dir = R.active;
       return;
     }
-    S->iters += 1;
+    R.iters += 1;
     if (!(rz >= 0)) {
-      S->active = 0;
-      S->dir = 0;
+      R.active = 0;
+      R.dir = 0;
       return;
     }
-    S->beta = rz / S->rz;
-    S->rz = rz;
-    S->dir = 1;
-    if (rz <= S->tol2 * S->rz0) S->active = 0;
+    R.beta = rz / R.rz;
+    R.rz = rz;
+    R.dir = 1;
+    if (rz <= R.tol2 * R.rz0) R.active = 0;
   }
 }
 
-// p = z + beta p (start: p = z)
-__global__ void __launch_bounds__(128) k_mg0_direction(MixedGrid G, const float* __restrict__ z, float* __restrict__ p,
-                                                       const MgScalars* S, int start) {
-  if (!start && !S->dir) return;
-  const float b = start ? 0.f : (float)S->beta;
+// p = z + beta p (start: p = z).  dir stays set once a right-hand side has
+// stopped, so later launches of the same chunk may rescale its p again; the
+// next start overwrites p, so that direction is never used.
+__global__ void __launch_bounds__(128) k_mg0_direction(MixedGrid G, MgVecs v, const MgScalars* S, unsigned mask,
+                                                       int start) {
   const P0 t = p0_pos(G);
+  if (!((mask >> t.m) & 1u) || !(start || S[t.m].dir)) return;
   if (!t.live) return;
+  const float b = start ? 0.f : (float)S[t.m].beta;
+  const float* __restrict__ z = v.z[t.m];
+  float* __restrict__ p = v.p[t.m];
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
     const float4 zz = ld4(z + base);
@@ -677,19 +751,33 @@ __global__ void __launch_bounds__(128) k_mg0_direction(MixedGrid G, const float*
   }
 }
 
+struct Scale4 {
+  double s[kMaxRhs];
+};
+
 // r = scale * rV (compact FP64 projected residual) on fluid cells, e = 0
-__global__ void k_mgp_load(MgLevel L, const double* __restrict__ rv, double scale, float* __restrict__ r,
-                           float* __restrict__ e) {
+__global__ void k_mgp_load(MgLevel L, DPtr4 rv, Scale4 sc, unsigned mask, MgVecs v) {
+  MG_RHS(L);
+  if (!((mask >> mrhs) & 1u)) return;
+  const double* __restrict__ rm = rv.p[mrhs];
+  const double scale = sc.s[mrhs];
+  float* __restrict__ r = v.r[mrhs];
+  float* __restrict__ e = v.e[mrhs];
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const long long cc = i + (long long)L.nx * (j + (long long)L.ny * k);
-    r[c] = L.dinv[c] > 0.f ? (float)(rv[cc] * scale) : 0.f;
+    r[c] = L.dinv[c] > 0.f ? (float)(rm[cc] * scale) : 0.f;
     e[c] = 0.f;
   }
 }
 
 // phi(padded) += e / scale on fluid cells
-__global__ void k_mgp_apply(MgLevel L, Dims d, const float* __restrict__ e, double scale, double* __restrict__ phi) {
+__global__ void k_mgp_apply(MgLevel L, Dims d, MgVecs v, Scale4 sc, unsigned mask, DPtr4 phiv) {
+  MG_RHS(L);
+  if (!((mask >> mrhs) & 1u)) return;
+  const float* __restrict__ e = v.e[mrhs];
+  const double scale = sc.s[mrhs];
+  double* __restrict__ phi = phiv.p[mrhs];
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     if (L.dinv[c] > 0.f) phi[d.ph(i + 1, j + 1, k + 1)] += (double)e[c] / scale;
@@ -708,63 +796,80 @@ Ops0 ops0(const MgHierarchy& H) {
   return O;
 }
 
-dim3 g0_grid(const MixedGrid& G) {
-  return dim3((unsigned)((G.ng + 31) / 32), (unsigned)((G.ny + 3) / 4), (unsigned)((G.nz + G.kc - 1) / G.kc));
+dim3 g0_grid(const MixedGrid& G, int nrhs) {
+  return dim3((unsigned)((G.ng + 31) / 32), (unsigned)((G.ny + 3) / 4),
+              (unsigned)(((G.nz + G.kc - 1) / G.kc) * nrhs));
+}
+
+Scale4 scale4(const double* s, unsigned mask) {
+  Scale4 r;
+  for (int m = 0; m < kMaxRhs; m++) r.s[m] = ((mask >> m) & 1u) ? s[m] : 1.0;
+  return r;
 }
 
 }  // namespace
 
 // Level-0 V-cycle tail shared by start and iteration: restriction of
 // r - A t, the coarse cycle, and the prolongation + post-smoothing + r.z pass.
-static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, int start,
-                               cudaStream_t st) {
+static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, unsigned mask,
+                               int start, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const MgLevel& C = H.lv[1];
-  k_mg0_residual<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, ops0(H), v.r, L.b, S, start);
+  const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
+  k_mg0_residual<<<g0, b0, 0, st>>>(H.g0, L, ops0(H), v, S, mask);
   note_launch();
-  k_mg_restrict<<<mg_grid(C), dim3(32, 8), 0, st>>>(L, C, L.b, C.b, H.cscale);
+  k_mg_restrict<<<rhs_grid(C, H.nrhs), dim3(32, 8), 0, st>>>(L, C, vec4(L.b), vec4(C.b), H.cscale, S, mask);
   note_launch();
-  cudaError_t e = vcycle(H, 1, C.b, C.x, st);
+  cudaError_t e = vcycle(H, 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  k_mg0_prolong_smooth<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, ops0(H), C, v.r, v.z, H.omega, S, rb,
-                                                             start);
+  k_mg0_prolong_smooth<<<g0, b0, 0, st>>>(H.g0, L, ops0(H), C, v, H.omega, S, rb, mask, start);
   note_launch();
-  k_mg0_direction<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, v.z, v.p, S, start);
-  note_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t mg_pcg_start(const MgHierarchy& H, const double* rv, double scale, MgVecs& v, MgScalars* S, const RedBuf& rb,
-                         cudaStream_t st) {
-  const MgLevel& L = H.lv[0];
-  const dim3 blk(32, 8), g = mg_grid(L);
-  k_mgp_load<<<g, blk, 0, st>>>(L, rv, scale, v.r, v.e);
-  note_launch();
-  k_mg_smooth<<<g, blk, 0, st>>>(L, L.t, v.r, L.t, H.omega, 1);
-  note_launch();
-  return level0_tail(H, v, S, rb, 1, st);
-}
-
-cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const RedBuf& rb, cudaStream_t st) {
-  const MgLevel& L = H.lv[0];
-  k_mg0_spmv<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, ops0(H), v.p, v.q, S, rb);
-  note_launch();
-  k_mg0_update<<<g0_grid(H.g0), dim3(32, 4), 0, st>>>(H.g0, L, v.p, v.q, v.e, v.r, H.omega, S);
-  note_launch();
-  return level0_tail(H, v, S, rb, 0, st);
-}
-
-cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, double scale, double* phi,
-                         cudaStream_t st) {
-  const MgLevel& L = H.lv[0];
-  k_mgp_apply<<<mg_grid(L), dim3(32, 8), 0, st>>>(L, d, v.e, scale, phi);
+  k_mg0_direction<<<g0, b0, 0, st>>>(H.g0, v, S, mask, start);
   note_launch();
   return cudaGetLastError();
 }
 
-int mg_grid_blocks(const MixedGrid& G) {
-  const dim3 g = g0_grid(G);
-  return (int)(g.x * g.y * g.z);
+cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* scale, unsigned mask, MgVecs& v,
+                         MgScalars* S, const MgRed& rb, cudaStream_t st) {
+  const MgLevel& L = H.lv[0];
+  const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
+  k_mgp_load<<<g, blk, 0, st>>>(L, rv, scale4(scale, mask), mask, v);
+  note_launch();
+  k_mg_smooth<<<g, blk, 0, st>>>(L, vec4(L.t), vec4(v.r), vec4(L.t), H.omega, 1, S, mask);
+  note_launch();
+  return level0_tail(H, v, S, rb, mask, 1, st);
+}
+
+cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, cudaStream_t st) {
+  const MgLevel& L = H.lv[0];
+  const unsigned all = (1u << H.nrhs) - 1u;
+  const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
+  k_mg0_spmv<<<g0, b0, 0, st>>>(H.g0, ops0(H), v, S, rb, all);
+  note_launch();
+  k_mg0_update<<<g0, b0, 0, st>>>(H.g0, L, v, H.omega, S, all);
+  note_launch();
+  return level0_tail(H, v, S, rb, all, 0, st);
+}
+
+cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const double* scale, unsigned mask,
+                         const DPtr4& phi, cudaStream_t st) {
+  const MgLevel& L = H.lv[0];
+  k_mgp_apply<<<rhs_grid(L, H.nrhs), dim3(32, 8), 0, st>>>(L, d, v, scale4(scale, mask), mask, phi);
+  note_launch();
+  return cudaGetLastError();
+}
+
+long long mg_red_partials(const MixedGrid& G) {
+  const dim3 g = g0_grid(G, 1);
+  return (long long)kMaxRhs * g.x * g.y * g.z;
+}
+
+int mg_zchunks(int nx, int ny, int nz, int nrhs) {
+  const long long gxy = (long long)((nx + 31) / 32) * ((ny + 7) / 8) * (nrhs < 1 ? 1 : nrhs);
+  long long zc = (152LL * 16 + gxy - 1) / gxy;
+  if (zc > nz) zc = nz;
+  if (zc < 1) zc = 1;
+  return (int)zc;
 }
 
 }  // namespace fpm
