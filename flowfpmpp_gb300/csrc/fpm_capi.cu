@@ -765,8 +765,10 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   H.omega = (float)env_double("FPM_MG_OMEGA", 0.9);
   H.coarse_sweeps = (int)env_double("FPM_MG_COARSE_SWEEPS", 40);
   H.cscale = (float)env_double("FPM_MG_CSCALE", 1.0);
-  // level 0 in the mixed solver's FP32 layout (zero halo), coarse levels compact
-  H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk());
+  // level 0 in the mixed solver's FP32 layout (zero halo), coarse levels
+  // compact; the level-0 passes take an even number of planes per chunk (whole
+  // aggregates)
+  H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk() + (mixed_kchunk() & 1));
   auto zeros = [&](long long n) {
     float* x = A.get<float>(n);
     CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(float), st));
@@ -778,7 +780,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     L.nx = nx;
     L.ny = ny;
     L.nz = nz;
-    L.zc = mg_zchunks(nx, ny, nz, nrhs);
+    L.zc = std::min(nz, 65535 / kMaxRhs);  // one plane per thread (the most loads in flight) where the grid allows
     if (H.nlev == 0) {
       L.off = 4 + H.g0.px;
       L.sy = H.g0.px;
@@ -797,7 +799,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     for (int m = 0; m < nrhs; m++) {
       L.t[m] = zeros(L.alloc);
       L.x[m] = H.nlev == 0 ? nullptr : zeros(L.alloc);
-      L.b[m] = zeros(L.alloc);  // level 0: the residual of the pre-smoothed iterate
+      L.b[m] = H.nlev == 0 ? nullptr : zeros(L.alloc);
     }
     H.nlev++;
     if (L.n() <= 1024 || H.nlev == kMgMaxLevels) break;
@@ -807,6 +809,8 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   }
   if (H.nlev < 2 || H.lv[H.nlev - 1].n() > 1024)
     throw Error{FPM_E_LIMIT, "grid too small or too large for the multigrid hierarchy"};
+  if ((d.ny + 3) / 4 > 65535 || (long long)((d.nz + H.g0.kc - 1) / H.g0.kc) * nrhs > 65535)
+    throw Error{FPM_E_LIMIT, "grid too large for the multigrid launch geometry"};
   if (H.nu != 1) throw Error{FPM_E_ARG, "the multigrid cycle uses one smoothing sweep on level 0"};
   H.fb0 = A.get<uint8_t>(H.g0.size);
   CUDA_TRY(cudaMemsetAsync(H.fb0, 0, H.g0.size, st));

@@ -246,7 +246,7 @@ void note_launch();
 // V-cycle cover all of them in one launch (blockIdx.z = chunk + chunks x rhs).
 struct MgLevel {
   int nx, ny, nz;
-  int zc;                      // chunks of planes per right-hand side (one-thread-per-cell kernels)
+  int zc;                      // planes per thread in the one-thread-per-cell kernels: nz / zc
   long long off, sy, sz;       // cell (i, j, k) (0-based) at off + i + sy j + sz k
   long long alloc;             // elements per array
   float *te, *tn, *tt, *dinv;  // face transmissibilities, inverse diagonal
@@ -293,7 +293,6 @@ cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* sc
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, cudaStream_t st);
 cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const double* scale, unsigned mask,
                          const DPtr4& phi, cudaStream_t st);
-int mg_zchunks(int nx, int ny, int nz, int nrhs);
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,

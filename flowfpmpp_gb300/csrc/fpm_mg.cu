@@ -38,6 +38,13 @@ __device__ __forceinline__ long long ix(const MgLevel& L, int i, int j, int k) {
 struct Vec4 {
   float* p[kMaxRhs];
 };
+// p[m] of a kernel-parameter pointer table, selected with constant indices
+// (a dynamic index would copy the table to local memory in every thread).
+template <class T>
+__device__ __forceinline__ T pick(T const (&p)[kMaxRhs], int m) {
+  static_assert(kMaxRhs == 4, "pick covers four right-hand sides");
+  return m == 0 ? p[0] : (m == 1 ? p[1] : (m == 2 ? p[2] : p[3]));
+}
 #define MG_CELLS(L)                                                                       \
   for (int k = (int)blockIdx.z % (L).zc; k < (L).nz; k += (L).zc)                         \
     for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < (L).ny; j += gridDim.y * blockDim.y) \
@@ -139,9 +146,9 @@ __global__ void k_mg_smooth(MgLevel L, Vec4 xv, Vec4 bv, Vec4 xov, float omega, 
                             unsigned mask) {
   MG_RHS(L);
   MG_SKIP(mrhs);
-  const float* __restrict__ x = xv.p[mrhs];
-  const float* __restrict__ b = bv.p[mrhs];
-  float* __restrict__ xo = xov.p[mrhs];
+  const float* __restrict__ x = pick(xv.p, mrhs);
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ xo = pick(xov.p, mrhs);
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const float w = omega * L.dinv[c];
@@ -156,9 +163,9 @@ __global__ void k_mg_resrestrict(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bc
                                  unsigned mask) {
   MG_RHS(C);
   MG_SKIP(mrhs);
-  const float* __restrict__ x = xv.p[mrhs];
-  const float* __restrict__ b = bv.p[mrhs];
-  float* __restrict__ bc = bcv.p[mrhs];
+  const float* __restrict__ x = pick(xv.p, mrhs);
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ bc = pick(bcv.p, mrhs);
   MG_CELLS(C) {
     float s = 0.f;
     for (int o = 0; o < 8; o++) {
@@ -172,34 +179,45 @@ __global__ void k_mg_resrestrict(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bc
   }
 }
 
-// bc = scale x the sum of the fine residuals rf of each aggregate.
-__global__ void k_mg_restrict(MgLevel F, MgLevel C, Vec4 rfv, Vec4 bcv, float scale, const MgScalars* S,
-                              unsigned mask) {
-  MG_RHS(C);
-  MG_SKIP(mrhs);
-  const float* __restrict__ rf = rfv.p[mrhs];
-  float* __restrict__ bc = bcv.p[mrhs];
-  MG_CELLS(C) {
-    float s = 0.f;
-    for (int o = 0; o < 8; o++) {
-      const int fi = 2 * i + (o & 1), fj = 2 * j + ((o >> 1) & 1), fk = 2 * k + (o >> 2);
-      if (fi < F.nx && fj < F.ny && fk < F.nz) s += rf[ix(F, fi, fj, fk)];
-    }
-    bc[ix(C, i, j, k)] = scale * s;
+// t0 += v on the (up to 8) level-0 cells of level-1 cell (i, j, k): the
+// prolongation of the final level-1 correction into the pre-smoothed level-0
+// iterate, done by the last kernel of level 1.
+// Level 0 uses the mixed layout, where cell pairs (2i, 2i+1) are 8-byte
+// aligned (off, sy and sz are even), so each row takes one float2.
+__device__ __forceinline__ void add_fine(const MgLevel& Z, float* __restrict__ t0, int i, int j, int k, float v) {
+  const int fi = 2 * i;
+  const bool two = fi + 1 < Z.nx;
+  float2* p[4];
+  float2 w[4];
+  bool ok[4];
+#pragma unroll
+  for (int o = 0; o < 4; o++) {
+    const int fj = 2 * j + (o & 1), fk = 2 * k + (o >> 1);
+    ok[o] = fj < Z.ny && fk < Z.nz;
+    p[o] = reinterpret_cast<float2*>(t0 + ix(Z, fi, fj, fk));
+    if (ok[o]) w[o] = *p[o];
+  }
+#pragma unroll
+  for (int o = 0; o < 4; o++) {
+    if (!ok[o]) continue;
+    w[o].x += v;
+    if (two) w[o].y += v;  // the cell after the last one is the zero halo
+    *p[o] = w[o];
   }
 }
 
 // xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
 // added on the fly, also at the neighbours): prolongation and the first
-// post-smoothing sweep in one pass.
+// post-smoothing sweep in one pass.  add0: F is level 1 and this is its last
+// kernel; xo is also prolonged into level 0 (Z).
 __global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv, Vec4 xov, float omega,
-                                    const MgScalars* S, unsigned mask) {
+                                    const MgScalars* S, unsigned mask, MgLevel Z, int add0) {
   MG_RHS(F);
   MG_SKIP(mrhs);
-  const float* __restrict__ x = xv.p[mrhs];
-  const float* __restrict__ xcrs = xcv.p[mrhs];
-  const float* __restrict__ b = bv.p[mrhs];
-  float* __restrict__ xo = xov.p[mrhs];
+  const float* __restrict__ x = pick(xv.p, mrhs);
+  const float* __restrict__ xcrs = pick(xcv.p, mrhs);
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ xo = pick(xov.p, mrhs);
   const long long sy = F.sy, sz = F.sz, cy = C.sy, cz = C.sz;
   MG_CELLS(F) {
     const long long c = ix(F, i, j, k), pc = ix(C, i >> 1, j >> 1, k >> 1);
@@ -211,19 +229,23 @@ __global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec
     if (j > 0) u = fmaf(F.tn[c - sy], yc - (x[c - sy] + xcrs[(j & 1) ? pc : pc - cy]), u);
     if (k + 1 < F.nz) u = fmaf(F.tt[c], yc - (x[c + sz] + xcrs[(k & 1) ? pc + cz : pc]), u);
     if (k > 0) u = fmaf(F.tt[c - sz], yc - (x[c - sz] + xcrs[(k & 1) ? pc : pc - cz]), u);
-    xo[c] = fmaf(omega * F.dinv[c], b[c] - u, yc);
+    const float xn = fmaf(omega * F.dinv[c], b[c] - u, yc);
+    xo[c] = xn;
+    if (add0) add_fine(Z, pick(Z.t, mrhs), i, j, k, xn);
   }
 }
 
 // Coarsest level (at most 1024 cells, compact layout): nsweeps weighted
 // Jacobi sweeps from 0 in one block per right-hand side, with the level's
-// operator, right-hand side and iterate in shared memory.
+// operator, right-hand side and iterate in shared memory.  add0: this is
+// level 1; the result is also prolonged into level 0 (Z).
 __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, Vec4 bv, Vec4 xv, float omega, int nsweeps,
-                                                    const MgScalars* S, unsigned mask) {
+                                                    const MgScalars* S, unsigned mask, MgLevel Z,
+                                                    int add0) {
   const int mrhs = blockIdx.x;
   MG_SKIP(mrhs);
-  const float* __restrict__ b = bv.p[mrhs];
-  float* __restrict__ x = xv.p[mrhs];
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ x = pick(xv.p, mrhs);
   __shared__ float te[1024], tn[1024], tt[1024], wd[1024], bb[1024], xa[1024], xb[1024];
   const int n = (int)L.n();
   const int c = threadIdx.x;
@@ -260,7 +282,10 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, Vec4 bv, Vec4 xv,
     a = o;
     o = t;
   }
-  if (c < n) x[c] = a[c];
+  if (c < n) {
+    x[c] = a[c];
+    if (add0) add_fine(Z, pick(Z.t, mrhs), i, j, k, a[c]);
+  }
 }
 
 dim3 mg_grid(const MgLevel& L) { return dim3((L.nx + 31) / 32, (L.ny + 7) / 8, (unsigned)L.zc); }
@@ -298,7 +323,7 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
   const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
   const Vec4 b = vec4(L.b), x = vec4(L.x), t = vec4(L.t);
   if (l == H.nlev - 1) {
-    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask);
+    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask, H.lv[0], l == 1);
     note_launch();
     return cudaGetLastError();
   }
@@ -315,7 +340,9 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
   note_launch();
   cudaError_t e = vcycle(H, l + 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask);
+  // with one sweep (H.nu == 1) this is the level's last kernel
+  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask, H.lv[0],
+                                         l == 1 && H.nu == 1);
   note_launch();
   std::swap(cur, oth);
   for (int s = 1; s < H.nu; s++) {
@@ -476,84 +503,68 @@ __device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, co
   return F;
 }
 
-// q = A p, pq = p.q, alpha = rz / pq
-__global__ void __launch_bounds__(128, 6) k_mg0_spmv(MixedGrid G, Ops0 O, MgVecs v, MgScalars* S, MgRed rb,
-                                                  unsigned mask) {
-  const P0 t = p0_pos(G);
-  MG_SKIP(t.m);
-  const float* __restrict__ p = v.p[t.m];
-  float* __restrict__ q = v.q[t.m];
-  const int lane = threadIdx.x;
-  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
-  const long long px = G.px, pl = G.plane;
-  Acc2 acc;
-  float4 pc = zero4(), pb = zero4();
-  uchar4 fbel = make_uchar4(0, 0, 0, 0);
-  const Row0 R = row0(O, t);
-  if (t.live) {
-    pc = ld4(p + t.base);
-    pb = t.k0 > 1 ? ld4(p + t.base - pl) : pc;
-    if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
-  }
-  long long base = t.base;
-  for (int k = t.k0; k <= t.k1; k++, base += pl) {
-    float4 pt = pc, ps = zero4(), pn = zero4();
-    float lft = 0.f, rgt = 0.f;
-    uchar4 f4 = make_uchar4(0, 0, 0, 0), fs4 = f4;
-    int fw = 0;
-    if (t.live) {
-      if (k < G.nz) pt = ld4(p + base + pl);
-      ps = ld4(p + base - px);
-      pn = ld4(p + base + px);
-      f4 = ldb4(O.fb + base);
-      fs4 = ldb4(O.fb + base - px);
-      if (lane == 0) {
-        lft = __ldg(p + base - 1);
-        fw = O.fb[base - 1];
-      }
-      if (fetch_right) rgt = __ldg(p + base + 4);
-    }
-    float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
-    const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, fw);
-    float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
-    if (lane == 0) {
-      left = lft;
-      te_left = Fc.te_w;
-    }
-    if (fetch_right) right = rgt;
-    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
-    if (t.live) {
-      st4(q + base, u);
-      acc.add4(pc, u);
-    }
-    pb = pc;
-    pc = pt;
-    fbel = f4;
-  }
-  double out = 0.0;
-  if (rhs_reduce((double)acc.s + (double)acc.e, t.m, t.zc, rb, &out) && lin_tid() == 0) {
-    MgScalars& R = S[t.m];
-    R.pq = out;
-    if (!(out > 0) || !(R.rz > 0)) {
-      R.active = 0;
-      R.alpha = 0;
-    } else {
-      R.alpha = R.rz / out;
-    }
-  }
-}
+// Level-0 stencil passes, marching through the kc planes of a chunk with
+// the neighbourhood of the next plane loaded one step ahead (the passes are
+// bound by load latency, not by HBM bandwidth):
+//   kSpmv      q = A p, pq = p.q, alpha = rz / pq
+//   kResidual  b1 = cscale x P^T (r - A t): the residual of the pre-smoothed
+//              iterate, restricted to level 1 on the fly (the two planes of an
+//              aggregate are summed in registers, its two rows through shared
+//              memory; kc is even, so chunks hold whole aggregates)
+//   kSmooth    z = t + omega dinv (r - A t), r.z and the PCG scalar updates
+//              (start: rz = rz0; otherwise beta and the stop test); t holds
+//              the pre-smoothed iterate plus the prolonged coarse correction,
+//              added by the last kernel of level 1 (see add_fine)
+enum { kSpmv = 0, kResidual = 1, kSmooth = 2 };
 
-// res = r - A t on level 0 (the residual of the pre-smoothed iterate)
-__global__ void __launch_bounds__(128, 6) k_mg0_residual(MixedGrid G, MgLevel L, Ops0 O, MgVecs v,
-                                                      const MgScalars* S, unsigned mask) {
+// What plane k needs besides the carried centre and bottom values.
+struct Nb {
+  float4 pt, ps, pn, rr, dv;
+  uchar4 f, fs;
+  float lft, rgt;
+  int fw;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(128, MODE == kSmooth ? 4 : 5)
+    k_mg0_stencil(MixedGrid G, MgLevel L, MgLevel C, Ops0 O, MgVecs v, float omega, float cscale, MgScalars* S,
+                  MgRed rb, unsigned mask, int start) {
   const P0 t = p0_pos(G);
   MG_SKIP(t.m);
-  const float* __restrict__ r = v.r[t.m];
-  float* __restrict__ res = L.b[t.m];
+  const int m = t.m;
+  const float* __restrict__ x = MODE == kSpmv ? v.p[m] : L.t[m];
+  const float* __restrict__ r = v.r[m];
+  float* __restrict__ out = MODE == kSpmv ? v.q[m] : (MODE == kResidual ? C.b[m] : v.z[m]);
+  __shared__ float2 pair_sum[2][32];  // kResidual: the odd rows' aggregate sums
+  float2 agg = make_float2(0.f, 0.f);  // kResidual: this row's sums of the group's two aggregates
   const int lane = threadIdx.x;
   const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
   const long long px = G.px, pl = G.plane;
-  const float* __restrict__ x = L.t[t.m];
+  const int i0 = 4 * t.g;  // first cell of the group (0-based)
+  // loads of plane k (1-based) at offset base; nothing when !ok
+  auto load = [&](int k, long long base, bool ok) {
+    Nb n;
+    n.pt = n.ps = n.pn = n.rr = n.dv = zero4();
+    n.f = n.fs = make_uchar4(0, 0, 0, 0);
+    n.lft = n.rgt = 0.f;
+    n.fw = 0;
+    if (t.live && ok) {
+      if (k < G.nz) n.pt = ld4(x + base + pl);
+      n.ps = ld4(x + base - px);
+      n.pn = ld4(x + base + px);
+      n.f = ldb4(O.fb + base);
+      n.fs = ldb4(O.fb + base - px);
+      if (MODE != kSpmv) n.rr = ld4(r + base);
+      if (MODE == kSmooth) n.dv = ld4(L.dinv + base);
+      if (lane == 0) {
+        n.lft = __ldg(x + base - 1);
+        n.fw = O.fb[base - 1];
+      }
+      if (fetch_right) n.rgt = __ldg(x + base + 4);
+    }
+    return n;
+  };
+  Acc2 acc;
   float4 pc = zero4(), pb = zero4();
   uchar4 fbel = make_uchar4(0, 0, 0, 0);
   const Row0 R = row0(O, t);
@@ -563,38 +574,90 @@ __global__ void __launch_bounds__(128, 6) k_mg0_residual(MixedGrid G, MgLevel L,
     if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
   }
   long long base = t.base;
+  Nb cur = load(t.k0, base, true);
   for (int k = t.k0; k <= t.k1; k++, base += pl) {
-    float4 pt = pc, ps = zero4(), pn = zero4(), rr = zero4();
-    float lft = 0.f, rgt = 0.f;
-    uchar4 f4 = make_uchar4(0, 0, 0, 0), fs4 = f4;
-    int fw = 0;
-    if (t.live) {
-      if (k < G.nz) pt = ld4(x + base + pl);
-      ps = ld4(x + base - px);
-      pn = ld4(x + base + px);
-      f4 = ldb4(O.fb + base);
-      fs4 = ldb4(O.fb + base - px);
-      rr = ld4(r + base);
-      if (lane == 0) {
-        lft = __ldg(x + base - 1);
-        fw = O.fb[base - 1];
-      }
-      if (fetch_right) rgt = __ldg(x + base + 4);
-    }
+    const Nb nxt = load(k + 1, base + pl, k < t.k1);
+    const float4 pt = k < G.nz ? cur.pt : pc;
     float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
-    const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, fw);
+    const Faces0 Fc = faces0(O, R, k, cur.f, cur.fs, fbel, cur.fw);
     float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
     if (lane == 0) {
-      left = lft;
+      left = cur.lft;
       te_left = Fc.te_w;
     }
-    if (fetch_right) right = rgt;
-    const float4 u = face_apply(pc, left, right, ps, pn, pb, pt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
-    if (t.live) st4(res + base, make_float4(rr.x - u.x, rr.y - u.y, rr.z - u.z, rr.w - u.w));
+    if (fetch_right) right = cur.rgt;
+    const float4 u =
+        face_apply(pc, left, right, cur.ps, cur.pn, pb, pt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
+    if (t.live) {
+      if (MODE == kSpmv) {
+        st4(out + base, u);
+        acc.add4(pc, u);
+      } else if (MODE == kResidual) {
+        const float4& rr = cur.rr;
+        agg.x += (rr.x - u.x) + (rr.y - u.y);
+        agg.y += (rr.z - u.z) + (rr.w - u.w);
+      } else {
+        float zz[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          zz[q] = i0 + q < L.nx ? fmaf(omega * el(cur.dv, q), el(cur.rr, q) - el(u, q), el(pc, q)) : 0.f;
+        const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
+        st4(out + base, z4);
+        acc.add4(cur.rr, z4);
+      }
+    }
+    if (MODE == kResidual && (((k - 1) & 1) || k == G.nz)) {  // an aggregate's planes are done
+      // rows 2c and 2c+1 (0-based) are threadIdx.y = 2h and 2h+1 of the block
+      if (threadIdx.y & 1) pair_sum[threadIdx.y >> 1][lane] = agg;
+      __syncthreads();
+      if (!(threadIdx.y & 1) && t.live) {
+        const float2 o = pair_sum[threadIdx.y >> 1][lane];
+        const int ci = 2 * t.g, cj = (t.j - 1) >> 1, ck = (k - 1) >> 1;
+        float* bc = out + ix(C, ci, cj, ck);
+        bc[0] = cscale * (agg.x + o.x);
+        if (ci + 1 < C.nx) bc[1] = cscale * (agg.y + o.y);
+      }
+      __syncthreads();
+      agg = make_float2(0.f, 0.f);
+    }
     pb = pc;
     pc = pt;
-    fbel = f4;
+    fbel = cur.f;
+    cur = nxt;
   }
+  if (MODE == kResidual) return;
+  double out_sum = 0.0;
+  if (!rhs_reduce((double)acc.s + (double)acc.e, m, t.zc, rb, &out_sum) || lin_tid() != 0) return;
+  MgScalars& Q = S[m];
+  if (MODE == kSpmv) {
+    Q.pq = out_sum;
+    if (!(out_sum > 0) || !(Q.rz > 0)) {
+      Q.active = 0;
+      Q.alpha = 0;
+    } else {
+      Q.alpha = Q.rz / out_sum;
+    }
+    return;
+  }
+  const double rz = out_sum;
+  if (start) {
+    Q.rz = rz;
+    Q.rz0 = rz;
+    Q.beta = 0.0;
+    Q.active = rz > 0 ? 1 : 0;
+    Q.dir = Q.active;
+    return;
+  }
+  Q.iters += 1;
+  if (!(rz >= 0)) {
+    Q.active = 0;
+    Q.dir = 0;
+    return;
+  }
+  Q.beta = rz / Q.rz;
+  Q.rz = rz;
+  Q.dir = 1;
+  if (rz <= Q.tol2 * Q.rz0) Q.active = 0;
 }
 
 // e += alpha p; r -= alpha q; t = omega dinv r (the V-cycle's first
@@ -605,11 +668,11 @@ __global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, MgVe
   MG_SKIP(t.m);
   if (!t.live) return;
   const float a = (float)S[t.m].alpha;
-  const float* __restrict__ p = v.p[t.m];
-  const float* __restrict__ q = v.q[t.m];
-  float* __restrict__ e = v.e[t.m];
-  float* __restrict__ r = v.r[t.m];
-  float* __restrict__ tt = L.t[t.m];
+  const float* __restrict__ p = pick(v.p, t.m);
+  const float* __restrict__ q = pick(v.q, t.m);
+  float* __restrict__ e = pick(v.e, t.m);
+  float* __restrict__ r = pick(v.r, t.m);
+  float* __restrict__ tt = pick(L.t, t.m);
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
     const float4 pp = ld4(p + base), qq = ld4(q + base), dv = ld4(L.dinv + base);
@@ -622,114 +685,6 @@ __global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, MgVe
   }
 }
 
-// z = y + omega dinv (r - A y), y = t + P xc (the coarse correction added to
-// the pre-smoothed level-0 iterate, also at the neighbours), and r.z with the
-// PCG scalar updates (start: rz = rz0; otherwise beta and the stop test).
-__global__ void __launch_bounds__(128, 6) k_mg0_prolong_smooth(MixedGrid G, MgLevel L, Ops0 O, MgLevel C, MgVecs v,
-                                                            float omega, MgScalars* S, MgRed rb, unsigned mask,
-                                                            int start) {
-  const P0 t = p0_pos(G);
-  MG_SKIP(t.m);
-  const float* __restrict__ r = v.r[t.m];
-  float* __restrict__ z = v.z[t.m];
-  const int lane = threadIdx.x;
-  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
-  const long long px = G.px, pl = G.plane;
-  const float* __restrict__ tv = L.t[t.m];
-  const float* __restrict__ xc = C.x[t.m];
-  const int jj = t.j - 1, i0 = 4 * t.g;  // 0-based row and first cell
-  // coarse value at (ci, cj, ck) or 0 outside
-  auto cval = [&](int ci, int cj, int ck) -> float {
-    if (ci < 0 || ci >= C.nx || cj < 0 || cj >= C.ny || ck < 0 || ck >= C.nz) return 0.f;
-    return __ldg(xc + ci + C.sy * cj + C.sz * ck);
-  };
-  // P xc for the four cells of the group in fine row jr, fine plane kr
-  auto prol4 = [&](int jr, int kr) -> float4 {
-    if (jr < 0 || jr >= L.ny || kr < 0 || kr >= L.nz) return zero4();
-    const float a = cval(i0 >> 1, jr >> 1, kr >> 1), b = cval((i0 >> 1) + 1, jr >> 1, kr >> 1);
-    float v[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) v[q] = i0 + q < L.nx ? (q < 2 ? a : b) : 0.f;
-    return make_float4(v[0], v[1], v[2], v[3]);
-  };
-  auto add4 = [](const float4& a, const float4& b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); };
-  Acc2 acc;
-  float4 yc = zero4(), yb = zero4();
-  uchar4 fbel = make_uchar4(0, 0, 0, 0);
-  const Row0 R = row0(O, t);
-  if (t.live) {
-    yc = add4(ld4(tv + t.base), prol4(jj, t.k0 - 1));
-    yb = t.k0 > 1 ? add4(ld4(tv + t.base - pl), prol4(jj, t.k0 - 2)) : yc;
-    if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
-  }
-  long long base = t.base;
-  for (int k = t.k0; k <= t.k1; k++, base += pl) {
-    const int kk = k - 1;
-    float4 yt = yc, ys = zero4(), yn = zero4(),
-           dv = zero4(), rr = zero4();
-    float lft = 0.f, rgt = 0.f;
-    uchar4 f4 = make_uchar4(0, 0, 0, 0), fs4 = f4;
-    int fw = 0;
-    if (t.live) {
-      if (k < G.nz) yt = add4(ld4(tv + base + pl), prol4(jj, kk + 1));
-      ys = add4(ld4(tv + base - px), prol4(jj - 1, kk));
-      yn = add4(ld4(tv + base + px), prol4(jj + 1, kk));
-      f4 = ldb4(O.fb + base);
-      fs4 = ldb4(O.fb + base - px);
-      dv = ld4(L.dinv + base);
-      rr = ld4(r + base);
-      if (lane == 0) {
-        lft = i0 > 0 ? __ldg(tv + base - 1) + cval((i0 - 1) >> 1, jj >> 1, kk >> 1) : 0.f;
-        fw = O.fb[base - 1];
-      }
-      if (fetch_right) rgt = i0 + 4 < L.nx ? __ldg(tv + base + 4) + cval((i0 + 4) >> 1, jj >> 1, kk >> 1) : 0.f;
-    }
-    float left = __shfl_up_sync(0xffffffffu, yc.w, 1), right = __shfl_down_sync(0xffffffffu, yc.x, 1);
-    const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, fw);
-    float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
-    if (lane == 0) {
-      left = lft;
-      te_left = Fc.te_w;
-    }
-    if (fetch_right) right = rgt;
-    const float4 u = face_apply(yc, left, right, ys, yn, yb, yt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
-    float zz[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      zz[q] = (t.live && i0 + q < L.nx) ? fmaf(omega * el(dv, q), el(rr, q) - el(u, q), el(yc, q)) : 0.f;
-    const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
-    if (t.live) {
-      st4(z + base, z4);
-      acc.add4(rr, z4);
-    }
-    yb = yc;
-    yc = yt;
-    fbel = f4;
-  }
-  double rz = 0.0;
-  if (rhs_reduce((double)acc.s + (double)acc.e, t.m, t.zc, rb, &rz) && lin_tid() == 0) {
-    MgScalars& R = S[t.m];
-    if (start) {
-      R.rz = rz;
-      R.rz0 = rz;
-      R.beta = 0.0;
-      R.active = rz > 0 ? 1 : 0;
-      R.dir = R.active;
-      return;
-    }
-    R.iters += 1;
-    if (!(rz >= 0)) {
-      R.active = 0;
-      R.dir = 0;
-      return;
-    }
-    R.beta = rz / R.rz;
-    R.rz = rz;
-    R.dir = 1;
-    if (rz <= R.tol2 * R.rz0) R.active = 0;
-  }
-}
-
 // p = z + beta p (start: p = z).  dir stays set once a right-hand side has
 // stopped, so later launches of the same chunk may rescale its p again; the
 // next start overwrites p, so that direction is never used.
@@ -739,8 +694,8 @@ __global__ void __launch_bounds__(128) k_mg0_direction(MixedGrid G, MgVecs v, co
   if (!((mask >> t.m) & 1u) || !(start || S[t.m].dir)) return;
   if (!t.live) return;
   const float b = start ? 0.f : (float)S[t.m].beta;
-  const float* __restrict__ z = v.z[t.m];
-  float* __restrict__ p = v.p[t.m];
+  const float* __restrict__ z = pick(v.z, t.m);
+  float* __restrict__ p = pick(v.p, t.m);
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
     const float4 zz = ld4(z + base);
@@ -759,10 +714,10 @@ struct Scale4 {
 __global__ void k_mgp_load(MgLevel L, DPtr4 rv, Scale4 sc, unsigned mask, MgVecs v) {
   MG_RHS(L);
   if (!((mask >> mrhs) & 1u)) return;
-  const double* __restrict__ rm = rv.p[mrhs];
-  const double scale = sc.s[mrhs];
-  float* __restrict__ r = v.r[mrhs];
-  float* __restrict__ e = v.e[mrhs];
+  const double* __restrict__ rm = pick(rv.p, mrhs);
+  const double scale = pick(sc.s, mrhs);
+  float* __restrict__ r = pick(v.r, mrhs);
+  float* __restrict__ e = pick(v.e, mrhs);
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const long long cc = i + (long long)L.nx * (j + (long long)L.ny * k);
@@ -775,9 +730,9 @@ __global__ void k_mgp_load(MgLevel L, DPtr4 rv, Scale4 sc, unsigned mask, MgVecs
 __global__ void k_mgp_apply(MgLevel L, Dims d, MgVecs v, Scale4 sc, unsigned mask, DPtr4 phiv) {
   MG_RHS(L);
   if (!((mask >> mrhs) & 1u)) return;
-  const float* __restrict__ e = v.e[mrhs];
-  const double scale = sc.s[mrhs];
-  double* __restrict__ phi = phiv.p[mrhs];
+  const float* __restrict__ e = pick(v.e, mrhs);
+  const double scale = pick(sc.s, mrhs);
+  double* __restrict__ phi = pick(phiv.p, mrhs);
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     if (L.dinv[c] > 0.f) phi[d.ph(i + 1, j + 1, k + 1)] += (double)e[c] / scale;
@@ -810,19 +765,18 @@ Scale4 scale4(const double* s, unsigned mask) {
 }  // namespace
 
 // Level-0 V-cycle tail shared by start and iteration: restriction of
-// r - A t, the coarse cycle, and the prolongation + post-smoothing + r.z pass.
+// r - A t, the coarse cycle (which adds its prolonged correction to t), and
+// the post-smoothing + r.z pass.
 static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, unsigned mask,
                                int start, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const MgLevel& C = H.lv[1];
   const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
-  k_mg0_residual<<<g0, b0, 0, st>>>(H.g0, L, ops0(H), v, S, mask);
-  note_launch();
-  k_mg_restrict<<<rhs_grid(C, H.nrhs), dim3(32, 8), 0, st>>>(L, C, vec4(L.b), vec4(C.b), H.cscale, S, mask);
+  k_mg0_stencil<kResidual><<<g0, b0, 0, st>>>(H.g0, L, C, ops0(H), v, H.omega, H.cscale, S, rb, mask, start);
   note_launch();
   cudaError_t e = vcycle(H, 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  k_mg0_prolong_smooth<<<g0, b0, 0, st>>>(H.g0, L, ops0(H), C, v, H.omega, S, rb, mask, start);
+  k_mg0_stencil<kSmooth><<<g0, b0, 0, st>>>(H.g0, L, C, ops0(H), v, H.omega, H.cscale, S, rb, mask, start);
   note_launch();
   k_mg0_direction<<<g0, b0, 0, st>>>(H.g0, v, S, mask, start);
   note_launch();
@@ -844,7 +798,7 @@ cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, cons
   const MgLevel& L = H.lv[0];
   const unsigned all = (1u << H.nrhs) - 1u;
   const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
-  k_mg0_spmv<<<g0, b0, 0, st>>>(H.g0, ops0(H), v, S, rb, all);
+  k_mg0_stencil<kSpmv><<<g0, b0, 0, st>>>(H.g0, L, H.lv[1], ops0(H), v, H.omega, H.cscale, S, rb, all, 0);
   note_launch();
   k_mg0_update<<<g0, b0, 0, st>>>(H.g0, L, v, H.omega, S, all);
   note_launch();
@@ -862,14 +816,6 @@ cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, c
 long long mg_red_partials(const MixedGrid& G) {
   const dim3 g = g0_grid(G, 1);
   return (long long)kMaxRhs * g.x * g.y * g.z;
-}
-
-int mg_zchunks(int nx, int ny, int nz, int nrhs) {
-  const long long gxy = (long long)((nx + 31) / 32) * ((ny + 7) / 8) * (nrhs < 1 ? 1 : nrhs);
-  long long zc = (152LL * 16 + gxy - 1) / gxy;
-  if (zc > nz) zc = nz;
-  if (zc < 1) zc = 1;
-  return (int)zc;
 }
 
 }  // namespace fpm
