@@ -769,6 +769,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   // compact; the level-0 passes take an even number of planes per chunk (whole
   // aggregates)
   H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk() + (mixed_kchunk() & 1));
+  H.kc0 = (int)env_double("FPM_MG_KCHUNK", 16);
+  H.kc0 = H.kc0 < 2 ? 2 : H.kc0 + (H.kc0 & 1);
+  H.pxb = (H.g0.px + 15) / 16 * 16;
   auto zeros = [&](long long n) {
     float* x = A.get<float>(n);
     CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(float), st));
@@ -812,8 +815,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   if ((d.ny + 3) / 4 > 65535 || (long long)((d.nz + H.g0.kc - 1) / H.g0.kc) * nrhs > 65535)
     throw Error{FPM_E_LIMIT, "grid too large for the multigrid launch geometry"};
   if (H.nu != 1) throw Error{FPM_E_ARG, "the multigrid cycle uses one smoothing sweep on level 0"};
-  H.fb0 = A.get<uint8_t>(H.g0.size);
-  CUDA_TRY(cudaMemsetAsync(H.fb0, 0, H.g0.size, st));
+  const long long fb_size = H.pxb * (d.ny + 2) * (long long)d.nz;
+  H.fb0 = A.get<uint8_t>(fb_size);
+  CUDA_TRY(cudaMemsetAsync(H.fb0, 0, fb_size, st));
   H.aex = zeros(H.g0.px);
   H.dxr = zeros(H.g0.px);
   H.dy = zeros(d.ny);
@@ -837,14 +841,18 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     S64[m] = A.get<SolveScalars>(1);
     CUDA_TRY(cudaMemsetAsync(S64[m], 0, sizeof(SolveScalars), st));
   }
+  CUDA_TRY(mg_encode(H, v));
   MgRed rb;
-  rb.partials = A.get<double>((size_t)mg_red_partials(H.g0));
+  rb.partials = A.get<double>((size_t)mg_red_partials(H));
   rb.tickets = A.get<unsigned int>(kMaxRhs);
   CUDA_TRY(cudaMemsetAsync(rb.tickets, 0, kMaxRhs * sizeof(unsigned int), st));
+  rb.err = A.get<int>(1);
+  CUDA_TRY(cudaMemsetAsync(rb.err, 0, sizeof(int), st));
   MgScalars* S = A.get<MgScalars>(kMaxRhs);
   CUDA_TRY(cudaMemsetAsync(S, 0, kMaxRhs * sizeof(MgScalars), st));
-  MgScalars* hS = nullptr;
-  CUDA_TRY(cudaMallocHost(&hS, kMaxRhs * sizeof(MgScalars)));
+  MgScalars* hS = nullptr;  // kMaxRhs scalars, then the error flag
+  CUDA_TRY(cudaMallocHost(&hS, kMaxRhs * sizeof(MgScalars) + sizeof(int)));
+  int* herr = reinterpret_cast<int*>(hS + kMaxRhs);
   struct HostFree {
     void* p;
     ~HostFree() { cudaFreeHost(p); }
@@ -894,7 +902,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     }
     total += chunk;
     CUDA_TRY(cudaMemcpyAsync(hS, S, kMaxRhs * sizeof(MgScalars), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(herr, rb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    if (*herr) throw Error{FPM_E_TIMEOUT, "multigrid: a bounded wait for a TMA copy gave up"};
     // Which right-hand sides have finished an outer step?
     unsigned upd = 0;
     for (int m = 0; m < nrhs; m++)

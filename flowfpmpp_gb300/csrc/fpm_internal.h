@@ -254,13 +254,22 @@ struct MgLevel {
   __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
 };
 constexpr int kMgMaxLevels = 16;
+// Tensor maps of the level-0 TMA passes: the level-0 vectors p, t and r of
+// each right-hand side, the inverse diagonal and the open-face bits.
+struct MgMaps {
+  CUtensorMap p[kMaxRhs], t[kMaxRhs], r[kMaxRhs], dinv, fb;
+};
 struct MgHierarchy {
   int nlev, nrhs;
+  int kc0;            // planes per CTA of the level-0 TMA passes (even: whole aggregates)
+  long long pxb;      // row pitch of the open-face bits (bytes, a multiple of 16)
+  MgMaps maps;
   MgLevel lv[kMgMaxLevels];
   MixedGrid g0;       // level 0 uses the FP32 layout of the mixed solver (float4 groups, zero halo)
   // level 0 operator for the float4 kernels: open-face bits per cell (1 east,
-  // 2 north, 4 top) and 1-D FP32 axis factors; T_east = dy dz / (xc_{i+1} - xc_i)
-  // etc. are rebuilt from them in registers
+  // 2 north, 4 top; the MixedGrid layout with row pitch pxb) and 1-D FP32 axis
+  // factors; T_east = dy dz / (xc_{i+1} - xc_i) etc. are rebuilt from them in
+  // registers
   uint8_t* fb0;
   float *aex, *dxr;   // row layout (index 3 + i, i 1-based), zero outside
   float *dy, *ayn;    // index j - 1
@@ -283,8 +292,11 @@ struct MgScalars {  // one per right-hand side
 struct MgRed {
   double* partials;
   unsigned int* tickets;
+  int* err;  // set when a bounded TMA wait gave up
 };
-long long mg_red_partials(const MixedGrid& G);
+long long mg_red_partials(const MgHierarchy& H);
+// Tensor maps of the level-0 passes (after the level-0 vectors exist).
+cudaError_t mg_encode(MgHierarchy& H, const MgVecs& v);
 // A launch covers the right-hand sides whose bit is set in mask and whose
 // MgScalars::active is set.
 cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const Axes& ax, cudaStream_t st);
@@ -293,6 +305,11 @@ cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* sc
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, cudaStream_t st);
 cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const double* scale, unsigned mask,
                          const DPtr4& phi, cudaStream_t st);
+
+// 3-D tensor map with box (b0, b1, 1), no swizzle, zero out-of-bounds fill
+// (fpm_jacobi_tma.cu).
+bool tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint64_t d0, uint64_t d1, uint64_t d2,
+                   uint64_t stride1_bytes, uint64_t stride2_bytes, uint32_t b0, uint32_t b1);
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,

@@ -16,9 +16,12 @@
 // valid preconditioner for CG.
 //
 // Level 0 uses the FP32 layout of the mixed solver (16-byte aligned rows,
-// zero x-y halo, see MixedGrid) and float4 kernels that march through k; the
-// coarse levels are compact (x fastest) and use one thread per cell.
+// zero x-y halo, see MixedGrid): its stencil passes stream planes through
+// shared memory with TMA, its vector updates are float4 kernels that march
+// through k.  The coarse levels are compact (x fastest) and use one thread
+// per cell.  All right-hand sides share each launch.
 #include "fpm_internal.h"
+#include "fpm_tma.cuh"
 
 namespace fpm {
 
@@ -51,8 +54,9 @@ __device__ __forceinline__ T pick(T const (&p)[kMaxRhs], int m) {
       for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (L).nx; i += gridDim.x * blockDim.x)
 
 // Level 0 from the solid flags (padded (0:nx+1, 0:ny+1, nz)) and the axes;
-// also the open-face bits of the float4 kernels.
-__global__ void k_mg_level0(MgLevel L, Dims d, const int32_t* __restrict__ solid, Axes ax, uint8_t* __restrict__ fb) {
+// also the open-face bits of the float4 kernels (row pitch pxb).
+__global__ void k_mg_level0(MgLevel L, Dims d, const int32_t* __restrict__ solid, Axes ax, uint8_t* __restrict__ fb,
+                            long long pxb) {
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const bool fl = solid[d.ph(i + 1, j + 1, k + 1)] == 0;
@@ -66,7 +70,8 @@ __global__ void k_mg_level0(MgLevel L, Dims d, const int32_t* __restrict__ solid
     L.te[c] = (float)te;
     L.tn[c] = (float)tn;
     L.tt[c] = (float)tt;
-    fb[c] = (uint8_t)((te > 0.0 ? 1 : 0) | (tn > 0.0 ? 2 : 0) | (tt > 0.0 ? 4 : 0));
+    fb[4 + i + pxb * ((j + 1) + (long long)(L.ny + 2) * k)] =
+        (uint8_t)((te > 0.0 ? 1 : 0) | (tn > 0.0 ? 2 : 0) | (tt > 0.0 ? 4 : 0));
   }
 }
 
@@ -300,7 +305,7 @@ Vec4 vec4(float* const (&p)[kMaxRhs]) {
 
 cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const Axes& ax, cudaStream_t st) {
   const dim3 blk(32, 8);
-  k_mg_level0<<<mg_grid(H.lv[0]), blk, 0, st>>>(H.lv[0], d, solid, ax, H.fb0);
+  k_mg_level0<<<mg_grid(H.lv[0]), blk, 0, st>>>(H.lv[0], d, solid, ax, H.fb0, H.pxb);
   note_launch();
   k_mg_axes0<<<8, 256, 0, st>>>(H.g0, ax, H.aex, H.dxr, H.dy, H.ayn, H.dz, H.azt);
   note_launch();
@@ -449,7 +454,6 @@ __device__ __forceinline__ float4 face_apply(const float4& c, float left, float 
 
 // Level-0 faces rebuilt from the open-face bits and the 1-D factors.
 struct Ops0 {
-  const uint8_t* fb;
   const float *aex, *dxr, *dy, *ayn, *dz, *azt;
 };
 struct Row0 {  // per-thread constants of a group's row
@@ -471,7 +475,6 @@ __device__ __forceinline__ Row0 row0(const Ops0& O, const P0& t) {
   }
   return r;
 }
-__device__ __forceinline__ uchar4 ldb4(const uint8_t* p) { return *reinterpret_cast<const uchar4*>(p); }
 __device__ __forceinline__ int bt(const uchar4& v, int n) { return n == 0 ? v.x : (n == 1 ? v.y : (n == 2 ? v.z : v.w)); }
 // Faces of plane k (1-based): f = bits of the group, fs = bits of the row
 // below, fb = bits of the plane below, fw = bits of the west cell.
@@ -503,131 +506,197 @@ __device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, co
   return F;
 }
 
-// Level-0 stencil passes, marching through the kc planes of a chunk with
-// the neighbourhood of the next plane loaded one step ahead (the passes are
-// bound by load latency, not by HBM bandwidth):
+// Level-0 stencil passes, streamed through shared memory by TMA:
 //   kSpmv      q = A p, pq = p.q, alpha = rz / pq
 //   kResidual  b1 = cscale x P^T (r - A t): the residual of the pre-smoothed
 //              iterate, restricted to level 1 on the fly (the two planes of an
 //              aggregate are summed in registers, its two rows through shared
-//              memory; kc is even, so chunks hold whole aggregates)
+//              memory; chunks hold whole aggregates)
 //   kSmooth    z = t + omega dinv (r - A t), r.z and the PCG scalar updates
 //              (start: rz = rz0; otherwise beta and the stop test); t holds
 //              the pre-smoothed iterate plus the prolonged coarse correction,
 //              added by the last kernel of level 1 (see add_fine)
+// A CTA owns kTX x kTY cells of a plane (a warp per row, four cells per
+// thread) and marches through kc0 planes.  Thread 0 keeps a 4-deep ring of
+// planes of the stencil operand (its tile plus the x-y halo) with their
+// open-face bits in flight, and for kResidual / kSmooth a 3-deep ring of r
+// (and dinv) tiles; every thread reads its seven neighbours from shared
+// memory, so the DRAM stream never waits on a dependent load.
+//
+// TMA boxes (x coordinates in elements of the MixedGrid row, cell i at 3 + i):
+//   operand  (kTX + 8) x (kTY + 2) floats from (kTX bx, kTY by): cells
+//            kTX bx - 3 .. kTX bx + kTX + 4, so the tile's cells and both
+//            x neighbours; the x start is a multiple of 4 (16 bytes)
+//   bits     (kTX + 16) x (kTY + 2) bytes from the same corner (x a multiple
+//            of 16 bytes; the bits' row pitch pxb is a multiple of 16)
+//   r, dinv  kTX x kTY floats from (4 + kTX bx, 1 + kTY by): the tile's cells
+// Rows and planes outside the grid (plane 0 and nz + 1) read as zero, where
+// the open-face bits are zero as well.
 enum { kSpmv = 0, kResidual = 1, kSmooth = 2 };
+constexpr int kTX = 128, kTY = 8, kTThreads = (kTX / 4) * kTY;
+constexpr int kPW = kTX + 8, kPWB = kTX + 16, kPH = kTY + 2;
+constexpr uint32_t kXBytes = kPW * kPH * 4, kBBytes = kPWB * kPH, kCBytes = kTX * kTY * 4;
+constexpr uint32_t kXStage = (kXBytes + 127) / 128 * 128, kBStage = (kBBytes + 127) / 128 * 128;
+constexpr int kXSt = 4, kCSt = 3;
+static_assert(kTX % 16 == 0 && kTY % 2 == 0, "tile: bits box start and row pairs");
+static_assert((kPW * 4) % 16 == 0 && kPWB % 16 == 0, "TMA box rows are whole 16-byte units");
 
-// What plane k needs besides the carried centre and bottom values.
-struct Nb {
-  float4 pt, ps, pn, rr, dv;
-  uchar4 f, fs;
-  float lft, rgt;
-  int fw;
-};
+__host__ __device__ constexpr uint32_t tma_smem(int mode) {
+  return kXSt * (kXStage + kBStage) + (mode == kSpmv ? 0u : kCSt * 2 * kCBytes) + 8 * (kXSt + kCSt);
+}
 
 template <int MODE>
-__global__ void __launch_bounds__(128, MODE == kSmooth ? 4 : 5)
-    k_mg0_stencil(MixedGrid G, MgLevel L, MgLevel C, Ops0 O, MgVecs v, float omega, float cscale, MgScalars* S,
-                  MgRed rb, unsigned mask, int start) {
-  const P0 t = p0_pos(G);
-  MG_SKIP(t.m);
-  const int m = t.m;
-  const float* __restrict__ x = MODE == kSpmv ? v.p[m] : L.t[m];
-  const float* __restrict__ r = v.r[m];
-  float* __restrict__ out = MODE == kSpmv ? v.q[m] : (MODE == kResidual ? C.b[m] : v.z[m]);
-  __shared__ float2 pair_sum[2][32];  // kResidual: the odd rows' aggregate sums
-  float2 agg = make_float2(0.f, 0.f);  // kResidual: this row's sums of the group's two aggregates
-  const int lane = threadIdx.x;
-  const bool fetch_right = t.live && (lane == 31 || t.g + 1 >= G.ng);
-  const long long px = G.px, pl = G.plane;
-  const int i0 = 4 * t.g;  // first cell of the group (0-based)
-  // loads of plane k (1-based) at offset base; nothing when !ok
-  auto load = [&](int k, long long base, bool ok) {
-    Nb n;
-    n.pt = n.ps = n.pn = n.rr = n.dv = zero4();
-    n.f = n.fs = make_uchar4(0, 0, 0, 0);
-    n.lft = n.rgt = 0.f;
-    n.fw = 0;
-    if (t.live && ok) {
-      if (k < G.nz) n.pt = ld4(x + base + pl);
-      n.ps = ld4(x + base - px);
-      n.pn = ld4(x + base + px);
-      n.f = ldb4(O.fb + base);
-      n.fs = ldb4(O.fb + base - px);
-      if (MODE != kSpmv) n.rr = ld4(r + base);
-      if (MODE == kSmooth) n.dv = ld4(L.dinv + base);
-      if (lane == 0) {
-        n.lft = __ldg(x + base - 1);
-        n.fw = O.fb[base - 1];
-      }
-      if (fetch_right) n.rgt = __ldg(x + base + 4);
-    }
-    return n;
-  };
-  Acc2 acc;
-  float4 pc = zero4(), pb = zero4();
-  uchar4 fbel = make_uchar4(0, 0, 0, 0);
-  const Row0 R = row0(O, t);
-  if (t.live) {
-    pc = ld4(x + t.base);
-    pb = t.k0 > 1 ? ld4(x + t.base - pl) : pc;
-    if (t.k0 > 1) fbel = ldb4(O.fb + t.base - pl);
+__global__ void __launch_bounds__(kTThreads, 3)
+    k_mg0_tma(const __grid_constant__ MgMaps M, MixedGrid G, int kc, MgLevel L, MgLevel C, Ops0 O, MgVecs v,
+              float omega, float cscale, MgScalars* S, MgRed rb, unsigned mask, int start) {
+  const int zc = (G.nz + kc - 1) / kc;
+  const int m = (int)blockIdx.z / zc;
+  MG_SKIP(m);
+  if (*reinterpret_cast<volatile int*>(rb.err)) return;  // an earlier wait gave up: the solve is abandoned
+  const int k0 = ((int)blockIdx.z - m * zc) * kc + 1;
+  const int k1 = min(G.nz, k0 + kc - 1);
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char* cs = smem + kXSt * (kXStage + kBStage);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(cs + (MODE == kSpmv ? 0 : kCSt * 2 * kCBytes));
+  const uint32_t s_base = tma::smem_u32(smem), c_base = tma::smem_u32(cs), bar_base = tma::smem_u32(bars);
+  const int tid = threadIdx.x, q = tid & 31, ty = tid >> 5;
+  const int x0 = kTX * (int)blockIdx.x, y0 = kTY * (int)blockIdx.y;
+  P0 t;
+  t.g = x0 / 4 + q;
+  t.j = y0 + ty + 1;
+  t.live = t.g < G.ng && t.j <= G.ny;
+  const CUtensorMap* mx = MODE == kSpmv ? (m == 0 ? &M.p[0] : m == 1 ? &M.p[1] : m == 2 ? &M.p[2] : &M.p[3])
+                                        : (m == 0 ? &M.t[0] : m == 1 ? &M.t[1] : m == 2 ? &M.t[2] : &M.t[3]);
+  const CUtensorMap* mr = m == 0 ? &M.r[0] : m == 1 ? &M.r[1] : m == 2 ? &M.r[2] : &M.r[3];
+  if (tid == 0) {
+    for (int s = 0; s < kXSt + kCSt; s++) tma::mbar_init(bar_base + 8 * s, 1);
+    tma::mbar_init_fence();
   }
-  long long base = t.base;
-  Nb cur = load(t.k0, base, true);
-  for (int k = t.k0; k <= t.k1; k++, base += pl) {
-    const Nb nxt = load(k + 1, base + pl, k < t.k1);
-    const float4 pt = k < G.nz ? cur.pt : pc;
-    float left = __shfl_up_sync(0xffffffffu, pc.w, 1), right = __shfl_down_sync(0xffffffffu, pc.x, 1);
-    const Faces0 Fc = faces0(O, R, k, cur.f, cur.fs, fbel, cur.fw);
-    float te_left = __shfl_up_sync(0xffffffffu, Fc.te.w, 1);
-    if (lane == 0) {
-      left = cur.lft;
-      te_left = Fc.te_w;
-    }
-    if (fetch_right) right = cur.rgt;
-    const float4 u =
-        face_apply(pc, left, right, cur.ps, cur.pn, pb, pt, Fc.te, te_left, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
-    if (t.live) {
+  __syncthreads();
+  // Operand / bits plane p (p = k0 - 1 .. k1 + 1) goes to ring slot
+  // (p - (k0 - 1)) % kXSt, r / dinv plane p (k0 .. k1) to (p - k0) % kCSt; the
+  // n-th use of a slot completes its barrier's phase n.
+  auto issue_x = [&](int p) {
+    const int s = (p - (k0 - 1)) % kXSt;
+    const uint32_t bar = bar_base + 8 * s, dst = s_base + s * (kXStage + kBStage);
+    tma::mbar_expect_tx(bar, kXBytes + kBBytes);
+    tma::load_3d(dst, mx, x0, y0, p - 1, bar);
+    tma::load_3d(dst + kXStage, &M.fb, x0, y0, p - 1, bar);
+  };
+  auto issue_c = [&](int p) {
+    const int s = (p - k0) % kCSt;
+    const uint32_t bar = bar_base + 8 * (kXSt + s), dst = c_base + s * 2 * kCBytes;
+    tma::mbar_expect_tx(bar, (MODE == kSmooth ? 2 : 1) * kCBytes);
+    tma::load_3d(dst, mr, 4 + x0, y0 + 1, p - 1, bar);
+    if (MODE == kSmooth) tma::load_3d(dst + kCBytes, &M.dinv, 4 + x0, y0 + 1, p - 1, bar);
+  };
+  auto x_ready = [&](int p) {
+    const int u = p - (k0 - 1);
+    return tma::mbar_wait(bar_base + 8 * (u % kXSt), (uint32_t)((u / kXSt) & 1));
+  };
+  auto c_ready = [&](int p) {
+    const int u = p - k0;
+    return tma::mbar_wait(bar_base + 8 * (kXSt + u % kCSt), (uint32_t)((u / kCSt) & 1));
+  };
+  int next_x = k0 - 1, next_c = k0;
+  if (tid == 0) {
+    for (; next_x <= k0 + 2 && next_x <= k1 + 1; next_x++) issue_x(next_x);
+    if (MODE != kSpmv)
+      for (; next_c <= k0 + 2 && next_c <= k1; next_c++) issue_c(next_c);
+  }
+
+  float* __restrict__ out = MODE == kSpmv ? v.q[m] : (MODE == kResidual ? C.b[m] : v.z[m]);
+  // kResidual: the odd rows' aggregate sums, double-buffered by aggregate
+  // plane (with an odd nz the last two planes complete aggregates in
+  // consecutive steps)
+  __shared__ float2 pair_sum[2][kTY / 2][32];
+  float2 agg = make_float2(0.f, 0.f);        // kResidual: this row's sums of the group's two aggregates
+  const int i0 = 4 * t.g;                    // first cell of the group (0-based)
+  const int cx = (ty + 1) * kPW + 4 + 4 * q, cb = (ty + 1) * kPWB + 4 + 4 * q, cc = ty * kTX + 4 * q;
+  const Row0 R = row0(O, t);
+  Acc2 acc;
+  bool ok = x_ready(k0 - 1) && x_ready(k0);
+  int kfail = k0;
+  bool failed = false;
+  for (int k = k0; k <= k1; k++) {
+    ok = ok && x_ready(k + 1) && (MODE == kSpmv || c_ready(k));
+    const bool pair_done = MODE == kResidual && (((k - 1) & 1) || k == G.nz);
+    if (ok && t.live) {
+      const int u = k - k0;  // plane k - 1 is in slot u % kXSt
+      const unsigned char* s0 = smem + (u % kXSt) * (kXStage + kBStage);
+      const unsigned char* s1 = smem + ((u + 1) % kXSt) * (kXStage + kBStage);
+      const unsigned char* s2 = smem + ((u + 2) % kXSt) * (kXStage + kBStage);
+      const float* X0 = reinterpret_cast<const float*>(s0);
+      const float* X1 = reinterpret_cast<const float*>(s1);
+      const float* X2 = reinterpret_cast<const float*>(s2);
+      const uint8_t* B0 = s0 + kXStage;
+      const uint8_t* B1 = s1 + kXStage;
+      const float4 pc = *reinterpret_cast<const float4*>(X1 + cx);
+      const float4 pb = *reinterpret_cast<const float4*>(X0 + cx);
+      const float4 pt = *reinterpret_cast<const float4*>(X2 + cx);
+      const float4 ps = *reinterpret_cast<const float4*>(X1 + cx - kPW);
+      const float4 pn = *reinterpret_cast<const float4*>(X1 + cx + kPW);
+      const float left = X1[cx - 1], right = X1[cx + 4];
+      const uchar4 f4 = *reinterpret_cast<const uchar4*>(B1 + cb);
+      const uchar4 fs4 = *reinterpret_cast<const uchar4*>(B1 + cb - kPWB);
+      const uchar4 fbel = *reinterpret_cast<const uchar4*>(B0 + cb);
+      const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, B1[cb - 1]);
+      const float4 uu = face_apply(pc, left, right, ps, pn, pb, pt, Fc.te, Fc.te_w, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
+      const long long base = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (k - 1));
       if (MODE == kSpmv) {
-        st4(out + base, u);
-        acc.add4(pc, u);
-      } else if (MODE == kResidual) {
-        const float4& rr = cur.rr;
-        agg.x += (rr.x - u.x) + (rr.y - u.y);
-        agg.y += (rr.z - u.z) + (rr.w - u.w);
+        st4(out + base, uu);
+        acc.add4(pc, uu);
       } else {
-        float zz[4];
+        const float* Rt = reinterpret_cast<const float*>(cs + (u % kCSt) * 2 * kCBytes);
+        const float4 rr = *reinterpret_cast<const float4*>(Rt + cc);
+        if (MODE == kResidual) {
+          agg.x += (rr.x - uu.x) + (rr.y - uu.y);
+          agg.y += (rr.z - uu.z) + (rr.w - uu.w);
+        } else {
+          const float4 dv = *reinterpret_cast<const float4*>(Rt + kTX * kTY + cc);
+          float zz[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-          zz[q] = i0 + q < L.nx ? fmaf(omega * el(cur.dv, q), el(cur.rr, q) - el(u, q), el(pc, q)) : 0.f;
-        const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
-        st4(out + base, z4);
-        acc.add4(cur.rr, z4);
+          for (int n = 0; n < 4; n++)
+            zz[n] = i0 + n < L.nx ? fmaf(omega * el(dv, n), el(rr, n) - el(uu, n), el(pc, n)) : 0.f;
+          const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
+          st4(out + base, z4);
+          acc.add4(rr, z4);
+        }
       }
     }
-    if (MODE == kResidual && (((k - 1) & 1) || k == G.nz)) {  // an aggregate's planes are done
-      // rows 2c and 2c+1 (0-based) are threadIdx.y = 2h and 2h+1 of the block
-      if (threadIdx.y & 1) pair_sum[threadIdx.y >> 1][lane] = agg;
-      __syncthreads();
-      if (!(threadIdx.y & 1) && t.live) {
-        const float2 o = pair_sum[threadIdx.y >> 1][lane];
+    // rows 2c and 2c+1 (0-based) of an aggregate are warps ty = 2h and 2h+1
+    if (pair_done && (ty & 1)) pair_sum[((k - 1) >> 1) & 1][ty >> 1][q] = agg;
+    if (__syncthreads_or(!ok)) {  // also: every thread is done with plane k - 1's slot
+      failed = true;
+      kfail = k;
+      break;
+    }
+    if (pair_done) {
+      if (!(ty & 1) && t.live) {
+        const float2 o = pair_sum[((k - 1) >> 1) & 1][ty >> 1][q];
         const int ci = 2 * t.g, cj = (t.j - 1) >> 1, ck = (k - 1) >> 1;
         float* bc = out + ix(C, ci, cj, ck);
         bc[0] = cscale * (agg.x + o.x);
         if (ci + 1 < C.nx) bc[1] = cscale * (agg.y + o.y);
       }
-      __syncthreads();
       agg = make_float2(0.f, 0.f);
     }
-    pb = pc;
-    pc = pt;
-    fbel = cur.f;
-    cur = nxt;
+    if (tid == 0) {
+      if (next_x <= k1 + 1) issue_x(next_x++);
+      if (MODE != kSpmv && next_c <= k1) issue_c(next_c++);
+    }
+  }
+  if (failed && tid == 0) {
+    atomicExch(rb.err, 1);
+    // drain the copies still in flight (bounded) before the CTA exits
+    for (int p = kfail - 1; p < next_x; p++) x_ready(p);
+    if (MODE != kSpmv)
+      for (int p = kfail; p < next_c; p++) c_ready(p);
   }
   if (MODE == kResidual) return;
+  // every block of the right-hand side takes part, also after a failure
   double out_sum = 0.0;
-  if (!rhs_reduce((double)acc.s + (double)acc.e, m, t.zc, rb, &out_sum) || lin_tid() != 0) return;
+  if (!rhs_reduce((double)acc.s + (double)acc.e, m, zc, rb, &out_sum) || tid != 0) return;
   MgScalars& Q = S[m];
   if (MODE == kSpmv) {
     Q.pq = out_sum;
@@ -741,7 +810,6 @@ __global__ void k_mgp_apply(MgLevel L, Dims d, MgVecs v, Scale4 sc, unsigned mas
 
 Ops0 ops0(const MgHierarchy& H) {
   Ops0 O;
-  O.fb = H.fb0;
   O.aex = H.aex;
   O.dxr = H.dxr;
   O.dy = H.dy;
@@ -749,6 +817,11 @@ Ops0 ops0(const MgHierarchy& H) {
   O.dz = H.dz;
   O.azt = H.azt;
   return O;
+}
+
+dim3 tma_grid(const MgHierarchy& H) {
+  return dim3((unsigned)((H.g0.ng + kTX / 4 - 1) / (kTX / 4)), (unsigned)((H.g0.ny + kTY - 1) / kTY),
+              (unsigned)(((H.g0.nz + H.kc0 - 1) / H.kc0) * H.nrhs));
 }
 
 dim3 g0_grid(const MixedGrid& G, int nrhs) {
@@ -771,12 +844,14 @@ static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, co
                                int start, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const MgLevel& C = H.lv[1];
-  const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
-  k_mg0_stencil<kResidual><<<g0, b0, 0, st>>>(H.g0, L, C, ops0(H), v, H.omega, H.cscale, S, rb, mask, start);
+  const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4), gt = tma_grid(H);
+  k_mg0_tma<kResidual><<<gt, kTThreads, tma_smem(kResidual), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.omega,
+                                                                   H.cscale, S, rb, mask, start);
   note_launch();
   cudaError_t e = vcycle(H, 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  k_mg0_stencil<kSmooth><<<g0, b0, 0, st>>>(H.g0, L, C, ops0(H), v, H.omega, H.cscale, S, rb, mask, start);
+  k_mg0_tma<kSmooth><<<gt, kTThreads, tma_smem(kSmooth), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.omega,
+                                                                 H.cscale, S, rb, mask, start);
   note_launch();
   k_mg0_direction<<<g0, b0, 0, st>>>(H.g0, v, S, mask, start);
   note_launch();
@@ -798,7 +873,8 @@ cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, cons
   const MgLevel& L = H.lv[0];
   const unsigned all = (1u << H.nrhs) - 1u;
   const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
-  k_mg0_stencil<kSpmv><<<g0, b0, 0, st>>>(H.g0, L, H.lv[1], ops0(H), v, H.omega, H.cscale, S, rb, all, 0);
+  k_mg0_tma<kSpmv><<<tma_grid(H), kTThreads, tma_smem(kSpmv), st>>>(H.maps, H.g0, H.kc0, L, H.lv[1], ops0(H), v,
+                                                                     H.omega, H.cscale, S, rb, all, 0);
   note_launch();
   k_mg0_update<<<g0, b0, 0, st>>>(H.g0, L, v, H.omega, S, all);
   note_launch();
@@ -813,9 +889,33 @@ cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, c
   return cudaGetLastError();
 }
 
-long long mg_red_partials(const MixedGrid& G) {
-  const dim3 g = g0_grid(G, 1);
-  return (long long)kMaxRhs * g.x * g.y * g.z;
+long long mg_red_partials(const MgHierarchy& H) {
+  const dim3 g = tma_grid(H);  // z covers all right-hand sides: blocks per right-hand side x kMaxRhs
+  return (long long)kMaxRhs * g.x * g.y * (g.z / H.nrhs);
+}
+
+cudaError_t mg_encode(MgHierarchy& H, const MgVecs& v) {
+  const MixedGrid& G = H.g0;
+  const uint64_t rows = (uint64_t)G.ny + 2, pitch = 4ULL * G.px;
+  auto f32 = [&](CUtensorMap* map, float* base, uint32_t b0, uint32_t b1) {
+    return tma_encode_3d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, base, G.px, rows, G.nz, pitch, pitch * rows, b0, b1);
+  };
+  bool ok = true;
+  for (int m = 0; m < H.nrhs; m++) {
+    ok = ok && f32(&H.maps.p[m], v.p[m], kPW, kPH) && f32(&H.maps.t[m], H.lv[0].t[m], kPW, kPH) &&
+         f32(&H.maps.r[m], v.r[m], kTX, kTY);
+  }
+  ok = ok && f32(&H.maps.dinv, H.lv[0].dinv, kTX, kTY) &&
+       tma_encode_3d(&H.maps.fb, CU_TENSOR_MAP_DATA_TYPE_UINT8, H.fb0, (uint64_t)H.pxb, rows, G.nz, (uint64_t)H.pxb,
+                     (uint64_t)H.pxb * rows, kPWB, kPH);
+  if (!ok) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_mg0_tma<kResidual>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tma_smem(kResidual));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mg0_tma<kSmooth>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem(kSmooth));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mg0_tma<kSpmv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem(kSpmv));
+  return e;
 }
 
 }  // namespace fpm
