@@ -789,11 +789,11 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
       L.sy = H.g0.px;
       L.sz = H.g0.plane;
       L.alloc = H.g0.size;
-    } else {
+    } else {  // rows padded to 16 bytes (TMA tiles of level 1)
       L.off = 0;
-      L.sy = nx;
-      L.sz = (long long)nx * ny;
-      L.alloc = L.n();
+      L.sy = (nx + 3) / 4 * 4;
+      L.sz = L.sy * ny;
+      L.alloc = L.sz * nz;
     }
     L.te = zeros(L.alloc);
     L.tn = zeros(L.alloc);

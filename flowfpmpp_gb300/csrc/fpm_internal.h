@@ -254,10 +254,11 @@ struct MgLevel {
   __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
 };
 constexpr int kMgMaxLevels = 16;
-// Tensor maps of the level-0 TMA passes: the level-0 vectors p, t and r of
-// each right-hand side, the inverse diagonal and the open-face bits.
+// Tensor maps of the level-0 TMA passes: the level-0 vectors p, t and r and
+// the level-1 solution x1 of each right-hand side, the level-0 inverse
+// diagonal and the open-face bits.
 struct MgMaps {
-  CUtensorMap p[kMaxRhs], t[kMaxRhs], r[kMaxRhs], dinv, fb;
+  CUtensorMap p[kMaxRhs], t[kMaxRhs], r[kMaxRhs], x1[kMaxRhs], dinv, fb;
 };
 struct MgHierarchy {
   int nlev, nrhs;

@@ -184,39 +184,11 @@ __global__ void k_mg_resrestrict(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bc
   }
 }
 
-// t0 += v on the (up to 8) level-0 cells of level-1 cell (i, j, k): the
-// prolongation of the final level-1 correction into the pre-smoothed level-0
-// iterate, done by the last kernel of level 1.
-// Level 0 uses the mixed layout, where cell pairs (2i, 2i+1) are 8-byte
-// aligned (off, sy and sz are even), so each row takes one float2.
-__device__ __forceinline__ void add_fine(const MgLevel& Z, float* __restrict__ t0, int i, int j, int k, float v) {
-  const int fi = 2 * i;
-  const bool two = fi + 1 < Z.nx;
-  float2* p[4];
-  float2 w[4];
-  bool ok[4];
-#pragma unroll
-  for (int o = 0; o < 4; o++) {
-    const int fj = 2 * j + (o & 1), fk = 2 * k + (o >> 1);
-    ok[o] = fj < Z.ny && fk < Z.nz;
-    p[o] = reinterpret_cast<float2*>(t0 + ix(Z, fi, fj, fk));
-    if (ok[o]) w[o] = *p[o];
-  }
-#pragma unroll
-  for (int o = 0; o < 4; o++) {
-    if (!ok[o]) continue;
-    w[o].x += v;
-    if (two) w[o].y += v;  // the cell after the last one is the zero halo
-    *p[o] = w[o];
-  }
-}
-
 // xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
 // added on the fly, also at the neighbours): prolongation and the first
-// post-smoothing sweep in one pass.  add0: F is level 1 and this is its last
-// kernel; xo is also prolonged into level 0 (Z).
+// post-smoothing sweep in one pass.
 __global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv, Vec4 xov, float omega,
-                                    const MgScalars* S, unsigned mask, MgLevel Z, int add0) {
+                                    const MgScalars* S, unsigned mask) {
   MG_RHS(F);
   MG_SKIP(mrhs);
   const float* __restrict__ x = pick(xv.p, mrhs);
@@ -234,19 +206,15 @@ __global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec
     if (j > 0) u = fmaf(F.tn[c - sy], yc - (x[c - sy] + xcrs[(j & 1) ? pc : pc - cy]), u);
     if (k + 1 < F.nz) u = fmaf(F.tt[c], yc - (x[c + sz] + xcrs[(k & 1) ? pc + cz : pc]), u);
     if (k > 0) u = fmaf(F.tt[c - sz], yc - (x[c - sz] + xcrs[(k & 1) ? pc : pc - cz]), u);
-    const float xn = fmaf(omega * F.dinv[c], b[c] - u, yc);
-    xo[c] = xn;
-    if (add0) add_fine(Z, pick(Z.t, mrhs), i, j, k, xn);
+    xo[c] = fmaf(omega * F.dinv[c], b[c] - u, yc);
   }
 }
 
-// Coarsest level (at most 1024 cells, compact layout): nsweeps weighted
-// Jacobi sweeps from 0 in one block per right-hand side, with the level's
-// operator, right-hand side and iterate in shared memory.  add0: this is
-// level 1; the result is also prolonged into level 0 (Z).
+// Coarsest level (at most 1024 cells): nsweeps weighted Jacobi sweeps from 0
+// in one block per right-hand side, with the level's operator, right-hand side
+// and iterate in shared memory (compact there, x fastest).
 __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, Vec4 bv, Vec4 xv, float omega, int nsweeps,
-                                                    const MgScalars* S, unsigned mask, MgLevel Z,
-                                                    int add0) {
+                                                    const MgScalars* S, unsigned mask) {
   const int mrhs = blockIdx.x;
   MG_SKIP(mrhs);
   const float* __restrict__ b = pick(bv.p, mrhs);
@@ -254,18 +222,20 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, Vec4 bv, Vec4 xv,
   __shared__ float te[1024], tn[1024], tt[1024], wd[1024], bb[1024], xa[1024], xb[1024];
   const int n = (int)L.n();
   const int c = threadIdx.x;
-  const int sy = (int)L.sy, sz = (int)L.sz;
+  const int sy = L.nx, sz = L.nx * L.ny;  // shared-memory strides
   int i = 0, j = 0, k = 0;
+  long long gc = 0;
   if (c < n) {
-    te[c] = L.te[c];
-    tn[c] = L.tn[c];
-    tt[c] = L.tt[c];
-    wd[c] = omega * L.dinv[c];
-    bb[c] = b[c];
-    xa[c] = wd[c] * bb[c];
     i = c % L.nx;
     j = (c / L.nx) % L.ny;
     k = c / (L.nx * L.ny);
+    gc = ix(L, i, j, k);
+    te[c] = L.te[gc];
+    tn[c] = L.tn[gc];
+    tt[c] = L.tt[gc];
+    wd[c] = omega * L.dinv[gc];
+    bb[c] = b[gc];
+    xa[c] = wd[c] * bb[c];
   }
   __syncthreads();
   float* a = xa;
@@ -287,10 +257,7 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, Vec4 bv, Vec4 xv,
     a = o;
     o = t;
   }
-  if (c < n) {
-    x[c] = a[c];
-    if (add0) add_fine(Z, pick(Z.t, mrhs), i, j, k, a[c]);
-  }
+  if (c < n) x[gc] = a[c];
 }
 
 dim3 mg_grid(const MgLevel& L) { return dim3((L.nx + 31) / 32, (L.ny + 7) / 8, (unsigned)L.zc); }
@@ -328,7 +295,7 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
   const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
   const Vec4 b = vec4(L.b), x = vec4(L.x), t = vec4(L.t);
   if (l == H.nlev - 1) {
-    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask, H.lv[0], l == 1);
+    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask);
     note_launch();
     return cudaGetLastError();
   }
@@ -345,9 +312,7 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
   note_launch();
   cudaError_t e = vcycle(H, l + 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  // with one sweep (H.nu == 1) this is the level's last kernel
-  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask, H.lv[0],
-                                         l == 1 && H.nu == 1);
+  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask);
   note_launch();
   std::swap(cur, oth);
   for (int s = 1; s < H.nu; s++) {
@@ -512,10 +477,12 @@ __device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, co
 //              iterate, restricted to level 1 on the fly (the two planes of an
 //              aggregate are summed in registers, its two rows through shared
 //              memory; chunks hold whole aggregates)
-//   kSmooth    z = t + omega dinv (r - A t), r.z and the PCG scalar updates
-//              (start: rz = rz0; otherwise beta and the stop test); t holds
-//              the pre-smoothed iterate plus the prolonged coarse correction,
-//              added by the last kernel of level 1 (see add_fine)
+//   kSmooth    z = y + omega dinv (r - A y), y = t + P x1 (the pre-smoothed
+//              iterate plus the prolonged level-1 correction), r.z and the PCG
+//              scalar updates (start: rz = rz0; otherwise beta and the stop
+//              test); each operand plane is loaded with the level-1 tile of
+//              its parent plane and turned into y in shared memory when it
+//              lands
 // A CTA owns kTX x kTY cells of a plane (a warp per row, four cells per
 // thread) and marches through kc0 planes.  Thread 0 keeps a 4-deep ring of
 // planes of the stencil operand (its tile plus the x-y halo) with their
@@ -530,19 +497,32 @@ __device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, co
 //   bits     (kTX + 16) x (kTY + 2) bytes from the same corner (x a multiple
 //            of 16 bytes; the bits' row pitch pxb is a multiple of 16)
 //   r, dinv  kTX x kTY floats from (4 + kTX bx, 1 + kTY by): the tile's cells
+//   x1       kCW x kCH floats of level 1 (rows padded to 16 bytes) from
+//            (kTX bx / 2 - 4, kTY by / 2 - 1, parent plane): the parents of
+//            the operand tile's cells
 // Rows and planes outside the grid (plane 0 and nz + 1) read as zero, where
-// the open-face bits are zero as well.
+// the open-face bits are zero as well; the halo cells may pick up a level-1
+// value, which only ever meets a zero face.
 enum { kSpmv = 0, kResidual = 1, kSmooth = 2 };
 constexpr int kTX = 128, kTY = 8, kTThreads = (kTX / 4) * kTY;
 constexpr int kPW = kTX + 8, kPWB = kTX + 16, kPH = kTY + 2;
 constexpr uint32_t kXBytes = kPW * kPH * 4, kBBytes = kPWB * kPH, kCBytes = kTX * kTY * 4;
-constexpr uint32_t kXStage = (kXBytes + 127) / 128 * 128, kBStage = (kBBytes + 127) / 128 * 128;
+constexpr int kCW = kTX / 2 + 8, kCH = kTY / 2 + 2;  // level-1 tile: columns -4 .. kTX/2+3, rows -1 .. kTY/2
+constexpr uint32_t kX1Bytes = kCW * kCH * 4;
+constexpr uint32_t kXStage = (kXBytes + 127) / 128 * 128, kBStage = (kBBytes + 127) / 128 * 128,
+                   kX1Stage = (kX1Bytes + 127) / 128 * 128;
 constexpr int kXSt = 4, kCSt = 3;
+static_assert((kCW * 4) % 16 == 0, "level-1 box rows are whole 16-byte units");
+static_assert(kPW % 4 == 0 && 2 * (kPW / 4 - 1) + 3 < kCW, "prolongation: float4 rows, parents inside the tile");
 static_assert(kTX % 16 == 0 && kTY % 2 == 0, "tile: bits box start and row pairs");
 static_assert((kPW * 4) % 16 == 0 && kPWB % 16 == 0, "TMA box rows are whole 16-byte units");
 
+// Bytes of one operand ring stage (operand, bits, and for kSmooth the level-1 tile).
+__host__ __device__ constexpr uint32_t tma_stage(int mode) {
+  return kXStage + kBStage + (mode == kSmooth ? kX1Stage : 0u);
+}
 __host__ __device__ constexpr uint32_t tma_smem(int mode) {
-  return kXSt * (kXStage + kBStage) + (mode == kSpmv ? 0u : kCSt * 2 * kCBytes) + 8 * (kXSt + kCSt);
+  return kXSt * tma_stage(mode) + (mode == kSpmv ? 0u : kCSt * 2 * kCBytes) + 8 * (kXSt + kCSt);
 }
 
 template <int MODE>
@@ -556,7 +536,8 @@ __global__ void __launch_bounds__(kTThreads, 3)
   const int k0 = ((int)blockIdx.z - m * zc) * kc + 1;
   const int k1 = min(G.nz, k0 + kc - 1);
   extern __shared__ __align__(128) unsigned char smem[];
-  unsigned char* cs = smem + kXSt * (kXStage + kBStage);
+  constexpr uint32_t kStage = tma_stage(MODE);
+  unsigned char* cs = smem + kXSt * kStage;
   uint64_t* bars = reinterpret_cast<uint64_t*>(cs + (MODE == kSpmv ? 0 : kCSt * 2 * kCBytes));
   const uint32_t s_base = tma::smem_u32(smem), c_base = tma::smem_u32(cs), bar_base = tma::smem_u32(bars);
   const int tid = threadIdx.x, q = tid & 31, ty = tid >> 5;
@@ -568,6 +549,7 @@ __global__ void __launch_bounds__(kTThreads, 3)
   const CUtensorMap* mx = MODE == kSpmv ? (m == 0 ? &M.p[0] : m == 1 ? &M.p[1] : m == 2 ? &M.p[2] : &M.p[3])
                                         : (m == 0 ? &M.t[0] : m == 1 ? &M.t[1] : m == 2 ? &M.t[2] : &M.t[3]);
   const CUtensorMap* mr = m == 0 ? &M.r[0] : m == 1 ? &M.r[1] : m == 2 ? &M.r[2] : &M.r[3];
+  const CUtensorMap* m1 = m == 0 ? &M.x1[0] : m == 1 ? &M.x1[1] : m == 2 ? &M.x1[2] : &M.x1[3];
   if (tid == 0) {
     for (int s = 0; s < kXSt + kCSt; s++) tma::mbar_init(bar_base + 8 * s, 1);
     tma::mbar_init_fence();
@@ -578,10 +560,32 @@ __global__ void __launch_bounds__(kTThreads, 3)
   // n-th use of a slot completes its barrier's phase n.
   auto issue_x = [&](int p) {
     const int s = (p - (k0 - 1)) % kXSt;
-    const uint32_t bar = bar_base + 8 * s, dst = s_base + s * (kXStage + kBStage);
-    tma::mbar_expect_tx(bar, kXBytes + kBBytes);
+    const uint32_t bar = bar_base + 8 * s, dst = s_base + s * kStage;
+    tma::mbar_expect_tx(bar, kXBytes + kBBytes + (MODE == kSmooth ? kX1Bytes : 0u));
     tma::load_3d(dst, mx, x0, y0, p - 1, bar);
     tma::load_3d(dst + kXStage, &M.fb, x0, y0, p - 1, bar);
+    if (MODE == kSmooth) tma::load_3d(dst + kXStage + kBStage, m1, x0 / 2 - 4, y0 / 2 - 1, (p - 1) >> 1, bar);
+  };
+  // kSmooth: operand plane p (just landed) += its cells' level-1 parents.
+  // Columns 4a .. 4a+3 of a tile row have the parents 2a+2, 2a+2, 2a+3, 2a+3
+  // of the level-1 tile; tile row r has the parent row ((r - 1) >> 1) + 1.
+  auto prolong = [&](int p) {
+    if (MODE != kSmooth) return;
+    unsigned char* st = smem + ((p - (k0 - 1)) % kXSt) * kStage;
+    float* X = reinterpret_cast<float*>(st);
+    const float* X1 = reinterpret_cast<const float*>(st + kXStage + kBStage);
+    constexpr int kQ = kPW / 4;  // float4 per tile row
+    for (int e = tid; e < kPH * kQ; e += kTThreads) {
+      const int r = e / kQ, a = e - r * kQ;
+      float4* x4 = reinterpret_cast<float4*>(X + r * kPW) + a;
+      const float2 c = *reinterpret_cast<const float2*>(X1 + (((r - 1) >> 1) + 1) * kCW + 2 * a + 2);
+      float4 v4 = *x4;
+      v4.x += c.x;
+      v4.y += c.x;
+      v4.z += c.y;
+      v4.w += c.y;
+      *x4 = v4;
+    }
   };
   auto issue_c = [&](int p) {
     const int s = (p - k0) % kCSt;
@@ -616,16 +620,24 @@ __global__ void __launch_bounds__(kTThreads, 3)
   const Row0 R = row0(O, t);
   Acc2 acc;
   bool ok = x_ready(k0 - 1) && x_ready(k0);
+  if (MODE == kSmooth && ok) {
+    prolong(k0 - 1);
+    prolong(k0);
+  }
   int kfail = k0;
   bool failed = false;
   for (int k = k0; k <= k1; k++) {
     ok = ok && x_ready(k + 1) && (MODE == kSpmv || c_ready(k));
+    if (MODE == kSmooth) {
+      if (ok) prolong(k + 1);
+      __syncthreads();
+    }
     const bool pair_done = MODE == kResidual && (((k - 1) & 1) || k == G.nz);
     if (ok && t.live) {
       const int u = k - k0;  // plane k - 1 is in slot u % kXSt
-      const unsigned char* s0 = smem + (u % kXSt) * (kXStage + kBStage);
-      const unsigned char* s1 = smem + ((u + 1) % kXSt) * (kXStage + kBStage);
-      const unsigned char* s2 = smem + ((u + 2) % kXSt) * (kXStage + kBStage);
+      const unsigned char* s0 = smem + (u % kXSt) * kStage;
+      const unsigned char* s1 = smem + ((u + 1) % kXSt) * kStage;
+      const unsigned char* s2 = smem + ((u + 2) % kXSt) * kStage;
       const float* X0 = reinterpret_cast<const float*>(s0);
       const float* X1 = reinterpret_cast<const float*>(s1);
       const float* X2 = reinterpret_cast<const float*>(s2);
@@ -905,6 +917,10 @@ cudaError_t mg_encode(MgHierarchy& H, const MgVecs& v) {
     ok = ok && f32(&H.maps.p[m], v.p[m], kPW, kPH) && f32(&H.maps.t[m], H.lv[0].t[m], kPW, kPH) &&
          f32(&H.maps.r[m], v.r[m], kTX, kTY);
   }
+  const MgLevel& L1 = H.lv[1];
+  for (int m = 0; m < H.nrhs; m++)
+    ok = ok && tma_encode_3d(&H.maps.x1[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, L1.x[m], (uint64_t)L1.sy,
+                             (uint64_t)L1.ny, (uint64_t)L1.nz, 4ULL * L1.sy, 4ULL * L1.sz, kCW, kCH);
   ok = ok && f32(&H.maps.dinv, H.lv[0].dinv, kTX, kTY) &&
        tma_encode_3d(&H.maps.fb, CU_TENSOR_MAP_DATA_TYPE_UINT8, H.fb0, (uint64_t)H.pxb, rows, G.nz, (uint64_t)H.pxb,
                      (uint64_t)H.pxb * rows, kPWB, kPH);
