@@ -395,28 +395,6 @@ __device__ bool rhs_reduce(double s, int m, int zc, const MgRed& rb, double* out
   return true;
 }
 
-// u = (A v) for the four cells of a group from the loaded neighbourhood.
-__device__ __forceinline__ float4 face_apply(const float4& c, float left, float right, const float4& s,
-                                             const float4& n, const float4& b, const float4& t, const float4& te,
-                                             float te_left, const float4& tn, const float4& tns, const float4& tt,
-                                             const float4& ttb) {
-  float u[4];
-#pragma unroll
-  for (int q = 0; q < 4; q++) {
-    const float x = el(c, q);
-    const float xw = q == 0 ? left : el(c, q - 1), xe = q == 3 ? right : el(c, q + 1);
-    const float tw = q == 0 ? te_left : el(te, q - 1);
-    float v = el(te, q) * (x - xe);
-    v = fmaf(tw, x - xw, v);
-    v = fmaf(el(tn, q), x - el(n, q), v);
-    v = fmaf(el(tns, q), x - el(s, q), v);
-    v = fmaf(el(tt, q), x - el(t, q), v);
-    v = fmaf(el(ttb, q), x - el(b, q), v);
-    u[q] = v;
-  }
-  return make_float4(u[0], u[1], u[2], u[3]);
-}
-
 // Level-0 faces rebuilt from the open-face bits and the 1-D factors.
 struct Ops0 {
   const float *aex, *dxr, *dy, *ayn, *dz, *azt;
@@ -440,35 +418,72 @@ __device__ __forceinline__ Row0 row0(const Ops0& O, const P0& t) {
   }
   return r;
 }
-__device__ __forceinline__ int bt(const uchar4& v, int n) { return n == 0 ? v.x : (n == 1 ? v.y : (n == 2 ? v.z : v.w)); }
-// Faces of plane k (1-based): f = bits of the group, fs = bits of the row
-// below, fb = bits of the plane below, fw = bits of the west cell.
-struct Faces0 {
-  float4 te, tn, tns, tt, ttb;
+// Faces of a group's cells in pairs (cells 0,1 and 2,3), from the open-face
+// bits of the group (f), of the row below (fs) and of the west cell (fw), one
+// byte per cell; the FP32x2 instructions of sm_100+ give the same per-lane
+// rounding as the scalar ones.
+__device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 dif2(float2 a, float2 b) {  // a - b (fma with -1 rounds like the subtraction)
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 sel2(uint32_t p0, uint32_t p1, float2 v) {
+  return make_float2(p0 ? v.x : 0.f, p1 ? v.y : 0.f);
+}
+struct Faces2 {
+  float2 te[2], tn[2], tns[2], tt[2];
   float te_w;
 };
-__device__ __forceinline__ Faces0 faces0(const Ops0& O, const Row0& R, int k, const uchar4& f, const uchar4& fs,
-                                         const uchar4& fbel, int fw) {
-  const float dz = __ldg(O.dz + k - 1), azt = __ldg(O.azt + k - 1), aztb = k > 1 ? __ldg(O.azt + k - 2) : 0.f;
-  const float ex = R.dy * dz, ny = dz * R.ayn, nys = dz * R.ayn_s, tz = R.dy * azt, tzb = R.dy * aztb;
-  float te[4], tn[4], tns[4], tt[4], ttb[4];
+__device__ __forceinline__ Faces2 faces2(const Row0& R, float dz, float azt, uint32_t f, uint32_t fs, uint32_t fw) {
+  const float ex = R.dy * dz, ny = dz * R.ayn, nys = dz * R.ayn_s, tz = R.dy * azt;
+  Faces2 F;
 #pragma unroll
-  for (int n = 0; n < 4; n++) {
-    const float dxn = el(R.dx, n);
-    te[n] = (bt(f, n) & 1) ? el(R.aex, n) * ex : 0.f;
-    tn[n] = (bt(f, n) & 2) ? dxn * ny : 0.f;
-    tns[n] = (bt(fs, n) & 2) ? dxn * nys : 0.f;
-    tt[n] = (bt(f, n) & 4) ? dxn * tz : 0.f;
-    ttb[n] = (bt(fbel, n) & 4) ? dxn * tzb : 0.f;
+  for (int h = 0; h < 2; h++) {
+    const float2 ax = h ? hi2(R.aex) : lo2(R.aex), dx = h ? hi2(R.dx) : lo2(R.dx);
+    const uint32_t b0 = f >> (16 * h), b1 = f >> (16 * h + 8), s0 = fs >> (16 * h), s1 = fs >> (16 * h + 8);
+    F.te[h] = sel2(b0 & 1u, b1 & 1u, __fmul2_rn(ax, dup2(ex)));
+    F.tn[h] = sel2(b0 & 2u, b1 & 2u, __fmul2_rn(dx, dup2(ny)));
+    F.tns[h] = sel2(s0 & 2u, s1 & 2u, __fmul2_rn(dx, dup2(nys)));
+    F.tt[h] = sel2(b0 & 4u, b1 & 4u, __fmul2_rn(dx, dup2(tz)));
   }
-  Faces0 F;
-  F.te = make_float4(te[0], te[1], te[2], te[3]);
-  F.tn = make_float4(tn[0], tn[1], tn[2], tn[3]);
-  F.tns = make_float4(tns[0], tns[1], tns[2], tns[3]);
-  F.tt = make_float4(tt[0], tt[1], tt[2], tt[3]);
-  F.ttb = make_float4(ttb[0], ttb[1], ttb[2], ttb[3]);
-  F.te_w = (fw & 1) ? R.aex_w * ex : 0.f;
+  F.te_w = (fw & 1u) ? R.aex_w * ex : 0.f;
   return F;
+}
+// Top faces of the plane below (bits fb, its z factor aztb): the bottom faces
+// of a chunk's first plane; later planes carry them over.
+__device__ __forceinline__ void bottom2(const Row0& R, float aztb, uint32_t fb, float2 (&ttb)[2]) {
+  const float tzb = R.dy * aztb;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const float2 dx = h ? hi2(R.dx) : lo2(R.dx);
+    ttb[h] = sel2((fb >> (16 * h)) & 4u, (fb >> (16 * h + 8)) & 4u, __fmul2_rn(dx, dup2(tzb)));
+  }
+}
+// u = (A v) for the four cells of a group: per cell
+//   te (x - xe) + tw (x - xw) + tn (x - xn) + ts (x - xs) + tt (x - xt) + tb (x - xb)
+// summed in that order (mul, then fma).
+__device__ __forceinline__ float4 face_apply2(const float4& c, float left, float right, const float4& s,
+                                              const float4& n, const float4& b, const float4& t, const Faces2& F,
+                                              const float2 (&ttb)[2]) {
+  const float2 x[2] = {lo2(c), hi2(c)};
+  const float2 mid = make_float2(c.y, c.z);
+  const float2 xe[2] = {mid, make_float2(c.w, right)};
+  const float2 xw[2] = {make_float2(left, c.x), mid};
+  const float2 tw[2] = {make_float2(F.te_w, F.te[0].x), make_float2(F.te[0].y, F.te[1].x)};
+  const float2 xn[2] = {lo2(n), hi2(n)}, xs[2] = {lo2(s), hi2(s)}, xt[2] = {lo2(t), hi2(t)}, xb[2] = {lo2(b), hi2(b)};
+  float2 u[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    float2 v = __fmul2_rn(F.te[h], dif2(x[h], xe[h]));
+    v = __ffma2_rn(tw[h], dif2(x[h], xw[h]), v);
+    v = __ffma2_rn(F.tn[h], dif2(x[h], xn[h]), v);
+    v = __ffma2_rn(F.tns[h], dif2(x[h], xs[h]), v);
+    v = __ffma2_rn(F.tt[h], dif2(x[h], xt[h]), v);
+    v = __ffma2_rn(ttb[h], dif2(x[h], xb[h]), v);
+    u[h] = v;
+  }
+  return make_float4(u[0].x, u[0].y, u[1].x, u[1].y);
 }
 
 // Level-0 stencil passes, streamed through shared memory by TMA:
@@ -619,10 +634,15 @@ __global__ void __launch_bounds__(kTThreads, 3)
   const int cx = (ty + 1) * kPW + 4 + 4 * q, cb = (ty + 1) * kPWB + 4 + 4 * q, cc = ty * kTX + 4 * q;
   const Row0 R = row0(O, t);
   Acc2 acc;
+  float2 ttb[2];  // bottom faces of the current plane: the previous plane's top faces
   bool ok = x_ready(k0 - 1) && x_ready(k0);
   if (MODE == kSmooth && ok) {
     prolong(k0 - 1);
     prolong(k0);
+  }
+  {
+    const uint8_t* Bb = smem + kXStage;  // bits of plane k0 - 1 (slot 0)
+    bottom2(R, k0 > 1 ? __ldg(O.azt + k0 - 2) : 0.f, ok ? *reinterpret_cast<const uint32_t*>(Bb + cb) : 0u, ttb);
   }
   int kfail = k0;
   bool failed = false;
@@ -641,7 +661,6 @@ __global__ void __launch_bounds__(kTThreads, 3)
       const float* X0 = reinterpret_cast<const float*>(s0);
       const float* X1 = reinterpret_cast<const float*>(s1);
       const float* X2 = reinterpret_cast<const float*>(s2);
-      const uint8_t* B0 = s0 + kXStage;
       const uint8_t* B1 = s1 + kXStage;
       const float4 pc = *reinterpret_cast<const float4*>(X1 + cx);
       const float4 pb = *reinterpret_cast<const float4*>(X0 + cx);
@@ -649,11 +668,12 @@ __global__ void __launch_bounds__(kTThreads, 3)
       const float4 ps = *reinterpret_cast<const float4*>(X1 + cx - kPW);
       const float4 pn = *reinterpret_cast<const float4*>(X1 + cx + kPW);
       const float left = X1[cx - 1], right = X1[cx + 4];
-      const uchar4 f4 = *reinterpret_cast<const uchar4*>(B1 + cb);
-      const uchar4 fs4 = *reinterpret_cast<const uchar4*>(B1 + cb - kPWB);
-      const uchar4 fbel = *reinterpret_cast<const uchar4*>(B0 + cb);
-      const Faces0 Fc = faces0(O, R, k, f4, fs4, fbel, B1[cb - 1]);
-      const float4 uu = face_apply(pc, left, right, ps, pn, pb, pt, Fc.te, Fc.te_w, Fc.tn, Fc.tns, Fc.tt, Fc.ttb);
+      const uint32_t f4 = *reinterpret_cast<const uint32_t*>(B1 + cb);
+      const uint32_t fs4 = *reinterpret_cast<const uint32_t*>(B1 + cb - kPWB);
+      const Faces2 Fc = faces2(R, __ldg(O.dz + k - 1), __ldg(O.azt + k - 1), f4, fs4, B1[cb - 1]);
+      const float4 uu = face_apply2(pc, left, right, ps, pn, pb, pt, Fc, ttb);
+      ttb[0] = Fc.tt[0];
+      ttb[1] = Fc.tt[1];
       const long long base = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (k - 1));
       if (MODE == kSpmv) {
         st4(out + base, uu);
