@@ -131,85 +131,6 @@ __global__ void k_mg_dinv(MgLevel L) {
   }
 }
 
-// (A x)_c in face form.
-__device__ __forceinline__ float apply_a(const MgLevel& L, const float* __restrict__ x, int i, int j, int k,
-                                        long long c) {
-  const long long sy = L.sy, sz = L.sz;
-  const float xc = x[c];
-  float u = 0.f;
-  if (i + 1 < L.nx) u = fmaf(L.te[c], xc - x[c + 1], u);
-  if (i > 0) u = fmaf(L.te[c - 1], xc - x[c - 1], u);
-  if (j + 1 < L.ny) u = fmaf(L.tn[c], xc - x[c + sy], u);
-  if (j > 0) u = fmaf(L.tn[c - sy], xc - x[c - sy], u);
-  if (k + 1 < L.nz) u = fmaf(L.tt[c], xc - x[c + sz], u);
-  if (k > 0) u = fmaf(L.tt[c - sz], xc - x[c - sz], u);
-  return u;
-}
-
-// xo = (first ? 0 : x) + omega dinv (b - A x)   (first: x is taken as 0)
-__global__ void k_mg_smooth(MgLevel L, Vec4 xv, Vec4 bv, Vec4 xov, float omega, int first, const MgScalars* S,
-                            unsigned mask) {
-  MG_RHS(L);
-  MG_SKIP(mrhs);
-  const float* __restrict__ x = pick(xv.p, mrhs);
-  const float* __restrict__ b = pick(bv.p, mrhs);
-  float* __restrict__ xo = pick(xov.p, mrhs);
-  MG_CELLS(L) {
-    const long long c = ix(L, i, j, k);
-    const float w = omega * L.dinv[c];
-    xo[c] = first ? w * b[c] : fmaf(w, b[c] - apply_a(L, x, i, j, k, c), x[c]);
-  }
-}
-
-// bc = scale x restriction of b - A x: one thread per coarse cell sums the
-// residuals of its (up to 8) fine cells.  scale > 1 over-corrects with the
-// coarse solution (the cycle stays linear and symmetric).
-__global__ void k_mg_resrestrict(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bcv, float scale, const MgScalars* S,
-                                 unsigned mask) {
-  MG_RHS(C);
-  MG_SKIP(mrhs);
-  const float* __restrict__ x = pick(xv.p, mrhs);
-  const float* __restrict__ b = pick(bv.p, mrhs);
-  float* __restrict__ bc = pick(bcv.p, mrhs);
-  MG_CELLS(C) {
-    float s = 0.f;
-    for (int o = 0; o < 8; o++) {
-      const int fi = 2 * i + (o & 1), fj = 2 * j + ((o >> 1) & 1), fk = 2 * k + (o >> 2);
-      if (fi < F.nx && fj < F.ny && fk < F.nz) {
-        const long long c = ix(F, fi, fj, fk);
-        s += b[c] - apply_a(F, x, fi, fj, fk, c);
-      }
-    }
-    bc[ix(C, i, j, k)] = scale * s;
-  }
-}
-
-// xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
-// added on the fly, also at the neighbours): prolongation and the first
-// post-smoothing sweep in one pass.
-__global__ void k_mg_prolong_smooth(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv, Vec4 xov, float omega,
-                                    const MgScalars* S, unsigned mask) {
-  MG_RHS(F);
-  MG_SKIP(mrhs);
-  const float* __restrict__ x = pick(xv.p, mrhs);
-  const float* __restrict__ xcrs = pick(xcv.p, mrhs);
-  const float* __restrict__ b = pick(bv.p, mrhs);
-  float* __restrict__ xo = pick(xov.p, mrhs);
-  const long long sy = F.sy, sz = F.sz, cy = C.sy, cz = C.sz;
-  MG_CELLS(F) {
-    const long long c = ix(F, i, j, k), pc = ix(C, i >> 1, j >> 1, k >> 1);
-    const float yc = x[c] + xcrs[pc];
-    float u = 0.f;
-    if (i + 1 < F.nx) u = fmaf(F.te[c], yc - (x[c + 1] + xcrs[(i & 1) ? pc + 1 : pc]), u);
-    if (i > 0) u = fmaf(F.te[c - 1], yc - (x[c - 1] + xcrs[(i & 1) ? pc : pc - 1]), u);
-    if (j + 1 < F.ny) u = fmaf(F.tn[c], yc - (x[c + sy] + xcrs[(j & 1) ? pc + cy : pc]), u);
-    if (j > 0) u = fmaf(F.tn[c - sy], yc - (x[c - sy] + xcrs[(j & 1) ? pc : pc - cy]), u);
-    if (k + 1 < F.nz) u = fmaf(F.tt[c], yc - (x[c + sz] + xcrs[(k & 1) ? pc + cz : pc]), u);
-    if (k > 0) u = fmaf(F.tt[c - sz], yc - (x[c - sz] + xcrs[(k & 1) ? pc : pc - cz]), u);
-    xo[c] = fmaf(omega * F.dinv[c], b[c] - u, yc);
-  }
-}
-
 // Coarsest level (at most 1024 cells): nsweeps weighted Jacobi sweeps from 0
 // in one block per right-hand side, with the level's operator, right-hand side
 // and iterate in shared memory (compact there, x fastest).
@@ -283,42 +204,6 @@ cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const 
   for (int l = 0; l < H.nlev; l++) {
     k_mg_dinv<<<mg_grid(H.lv[l]), blk, 0, st>>>(H.lv[l]);
     note_launch();
-  }
-  return cudaGetLastError();
-}
-
-// x = V-cycle(b) on level l >= 1 for every right-hand side at once.
-// Smoothing alternates between x and the level's scratch t; the first write
-// goes to t, and 2 nu - 1 sweeps later the result is in x.
-static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsigned mask, cudaStream_t st) {
-  const MgLevel& L = H.lv[l];
-  const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
-  const Vec4 b = vec4(L.b), x = vec4(L.x), t = vec4(L.t);
-  if (l == H.nlev - 1) {
-    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask);
-    note_launch();
-    return cudaGetLastError();
-  }
-  Vec4 cur = t, oth = x;
-  k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, cur, H.omega, 1, S, mask);
-  note_launch();
-  for (int s = 1; s < H.nu; s++) {
-    k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
-    note_launch();
-    std::swap(cur, oth);
-  }
-  const MgLevel& C = H.lv[l + 1];
-  k_mg_resrestrict<<<rhs_grid(C, H.nrhs), blk, 0, st>>>(L, C, cur, b, vec4(C.b), H.cscale, S, mask);
-  note_launch();
-  cudaError_t e = vcycle(H, l + 1, S, mask, st);
-  if (e != cudaSuccess) return e;
-  k_mg_prolong_smooth<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask);
-  note_launch();
-  std::swap(cur, oth);
-  for (int s = 1; s < H.nu; s++) {
-    k_mg_smooth<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
-    note_launch();
-    std::swap(cur, oth);
   }
   return cudaGetLastError();
 }
@@ -485,6 +370,201 @@ __device__ __forceinline__ float4 face_apply2(const float4& c, float left, float
   }
   return make_float4(u[0].x, u[0].y, u[1].x, u[1].y);
 }
+
+// ---------------------------------------------------------------- float4 kernels of the V-cycle
+// Every level's rows start on 16 bytes (level 0: off = 4 + px, levels >= 1:
+// off = 0; sy a multiple of 4), so a thread takes the four cells 4g .. 4g+3
+// of a row on one plane.  Faces outside the grid and at padding cells are
+// zero, so neighbours outside the grid read as zero; outputs at padding
+// cells are written as zero.
+#define MG4_CELLS(L)                                                                        \
+  for (int k = (int)blockIdx.z % (L).zc; k < (L).nz; k += (L).zc)                           \
+    for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < (L).ny; j += gridDim.y * blockDim.y) \
+      for (int g = blockIdx.x * blockDim.x + threadIdx.x; 4 * g < (L).nx; g += gridDim.x * blockDim.x)
+
+struct X4 {  // a group's values and its neighbours' (s, n: rows j -+ 1; b, t: planes k -+ 1; l, r: x)
+  float4 c, s, n, b, t;
+  float l, r;
+};
+__device__ __forceinline__ X4 load_x4(const MgLevel& L, const float* __restrict__ x, int g, int j, int k,
+                                      long long c) {
+  X4 v;
+  v.c = ld4(x + c);
+  v.s = j > 0 ? ld4(x + c - L.sy) : zero4();
+  v.n = j + 1 < L.ny ? ld4(x + c + L.sy) : zero4();
+  v.b = k > 0 ? ld4(x + c - L.sz) : zero4();
+  v.t = k + 1 < L.nz ? ld4(x + c + L.sz) : zero4();
+  v.l = g > 0 ? __ldg(x + c - 1) : 0.f;
+  v.r = 4 * g + 4 < L.nx ? __ldg(x + c + 4) : 0.f;
+  return v;
+}
+// A x for the group from its faces (stored transmissibilities).
+__device__ __forceinline__ float4 apply4(const MgLevel& L, const X4& X, int g, int j, int k, long long c) {
+  const float4 te = ld4(L.te + c), tn = ld4(L.tn + c), tt = ld4(L.tt + c);
+  const float4 tns = j > 0 ? ld4(L.tn + c - L.sy) : zero4();
+  const float4 ttb4 = k > 0 ? ld4(L.tt + c - L.sz) : zero4();
+  Faces2 F;
+  F.te[0] = lo2(te);
+  F.te[1] = hi2(te);
+  F.tn[0] = lo2(tn);
+  F.tn[1] = hi2(tn);
+  F.tns[0] = lo2(tns);
+  F.tns[1] = hi2(tns);
+  F.tt[0] = lo2(tt);
+  F.tt[1] = hi2(tt);
+  F.te_w = g > 0 ? __ldg(L.te + c - 1) : 0.f;
+  const float2 ttb[2] = {lo2(ttb4), hi2(ttb4)};
+  return face_apply2(X.c, X.l, X.r, X.s, X.n, X.b, X.t, F, ttb);
+}
+// out = y + omega dinv (b - u) per cell, zero at padding cells (i >= nx)
+__device__ __forceinline__ float4 smooth_out(const MgLevel& L, int g, const float4& y, const float4& dv,
+                                             const float4& bb, const float4& u, float omega) {
+  float o[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    o[q] = 4 * g + q < L.nx ? fmaf(omega * el(dv, q), el(bb, q) - el(u, q), el(y, q)) : 0.f;
+  return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// xo = (first ? 0 : x) + omega dinv (b - A x)   (first: x is taken as 0)
+__global__ void __launch_bounds__(256) k_mg_smooth4(MgLevel L, Vec4 xv, Vec4 bv, Vec4 xov, float omega, int first,
+                                                    const MgScalars* S, unsigned mask) {
+  MG_RHS(L);
+  MG_SKIP(mrhs);
+  const float* __restrict__ x = pick(xv.p, mrhs);
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ xo = pick(xov.p, mrhs);
+  MG4_CELLS(L) {
+    const long long c = ix(L, 4 * g, j, k);
+    const float4 dv = ld4(L.dinv + c), bb = ld4(b + c);
+    float4 o;
+    if (first) {
+      o = smooth_out(L, g, zero4(), dv, bb, zero4(), omega);
+    } else {
+      const X4 X = load_x4(L, x, g, j, k, c);
+      o = smooth_out(L, g, X.c, dv, bb, apply4(L, X, g, j, k, c), omega);
+    }
+    st4(xo + c, o);
+  }
+}
+
+// bc = scale x restriction of b - A x: a thread takes two coarse cells
+// (cg: 2cg, 2cg+1), i.e. fine group cg on the aggregate's two rows and two
+// planes.  scale > 1 over-corrects with the coarse solution (the cycle stays
+// linear and symmetric).
+__global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bcv,
+                                                         float scale, const MgScalars* S, unsigned mask) {
+  MG_RHS(C);
+  MG_SKIP(mrhs);
+  const float* __restrict__ x = pick(xv.p, mrhs);
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ bc = pick(bcv.p, mrhs);
+  for (int ck = (int)blockIdx.z % C.zc; ck < C.nz; ck += C.zc)
+    for (int cj = blockIdx.y * blockDim.y + threadIdx.y; cj < C.ny; cj += gridDim.y * blockDim.y)
+      for (int cg = blockIdx.x * blockDim.x + threadIdx.x; 2 * cg < C.nx; cg += gridDim.x * blockDim.x) {
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+          const int j = 2 * cj + (o & 1), k = 2 * ck + (o >> 1);
+          if (j < F.ny && k < F.nz) {
+            const long long c = ix(F, 4 * cg, j, k);
+            const X4 X = load_x4(F, x, cg, j, k, c);
+            const float4 u = apply4(F, X, cg, j, k, c), bb = ld4(b + c);
+            s0 += (bb.x - u.x) + (bb.y - u.y);
+            s1 += (bb.z - u.z) + (bb.w - u.w);
+          }
+        }
+        float* o = bc + ix(C, 2 * cg, cj, ck);
+        o[0] = scale * s0;
+        if (2 * cg + 1 < C.nx) o[1] = scale * s1;
+      }
+}
+
+// xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
+// added on the fly, also at the neighbours): prolongation and the first
+// post-smoothing sweep in one pass.  Fine cells 4g .. 4g+3 have the coarse
+// parents 2g, 2g, 2g+1, 2g+1 (a float2 of the coarse row: 2g is even and
+// the row starts on 16 bytes).
+__global__ void __launch_bounds__(256) k_mg_prolong_smooth4(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv,
+                                                            Vec4 xov, float omega, const MgScalars* S,
+                                                            unsigned mask) {
+  MG_RHS(F);
+  MG_SKIP(mrhs);
+  const float* __restrict__ x = pick(xv.p, mrhs);
+  const float* __restrict__ xc = pick(xcv.p, mrhs);
+  const float* __restrict__ b = pick(bv.p, mrhs);
+  float* __restrict__ xo = pick(xov.p, mrhs);
+  auto par = [&](int g, int j, int k) {  // parents of fine group g on row j, plane k
+    const float2 p = __ldg(reinterpret_cast<const float2*>(xc + ix(C, 2 * g, j >> 1, k >> 1)));
+    return make_float4(p.x, p.x, p.y, p.y);
+  };
+  auto add = [](float4& a, const float4& v) {
+    a.x += v.x;
+    a.y += v.y;
+    a.z += v.z;
+    a.w += v.w;
+  };
+  MG4_CELLS(F) {
+    const long long c = ix(F, 4 * g, j, k);
+    X4 X = load_x4(F, x, g, j, k, c);
+    add(X.c, par(g, j, k));
+    if (j > 0) add(X.s, par(g, j - 1, k));
+    if (j + 1 < F.ny) add(X.n, par(g, j + 1, k));
+    if (k > 0) add(X.b, par(g, j, k - 1));
+    if (k + 1 < F.nz) add(X.t, par(g, j, k + 1));
+    if (g > 0) X.l += __ldg(xc + ix(C, 2 * g - 1, j >> 1, k >> 1));
+    if (4 * g + 4 < F.nx) X.r += __ldg(xc + ix(C, 2 * g + 2, j >> 1, k >> 1));
+    const float4 dv = ld4(F.dinv + c), bb = ld4(b + c);
+    st4(xo + c, smooth_out(F, g, X.c, dv, bb, apply4(F, X, g, j, k, c), omega));
+  }
+}
+
+dim3 grid4(const MgLevel& L, int nrhs) {
+  return dim3((unsigned)(((L.nx + 3) / 4 + 31) / 32), (unsigned)((L.ny + 7) / 8), (unsigned)(L.zc * nrhs));
+}
+dim3 grid4r(const MgLevel& C, int nrhs) {  // k_mg_resrestrict4: two coarse cells per thread
+  return dim3((unsigned)(((C.nx + 1) / 2 + 31) / 32), (unsigned)((C.ny + 7) / 8), (unsigned)(C.zc * nrhs));
+}
+
+}  // namespace
+
+// x = V-cycle(b) on level l >= 1 for every right-hand side at once.
+// Smoothing alternates between x and the level's scratch t; the first write
+// goes to t, and 2 nu - 1 sweeps later the result is in x.
+static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsigned mask, cudaStream_t st) {
+  const MgLevel& L = H.lv[l];
+  const dim3 blk(32, 8), g = grid4(L, H.nrhs);
+  const Vec4 b = vec4(L.b), x = vec4(L.x), t = vec4(L.t);
+  if (l == H.nlev - 1) {
+    k_mg_coarse<<<H.nrhs, 1024, 0, st>>>(L, b, x, H.omega, H.coarse_sweeps, S, mask);
+    note_launch();
+    return cudaGetLastError();
+  }
+  Vec4 cur = t, oth = x;
+  k_mg_smooth4<<<g, blk, 0, st>>>(L, cur, b, cur, H.omega, 1, S, mask);
+  note_launch();
+  for (int s = 1; s < H.nu; s++) {
+    k_mg_smooth4<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
+    note_launch();
+    std::swap(cur, oth);
+  }
+  const MgLevel& C = H.lv[l + 1];
+  k_mg_resrestrict4<<<grid4r(C, H.nrhs), blk, 0, st>>>(L, C, cur, b, vec4(C.b), H.cscale, S, mask);
+  note_launch();
+  cudaError_t e = vcycle(H, l + 1, S, mask, st);
+  if (e != cudaSuccess) return e;
+  k_mg_prolong_smooth4<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask);
+  note_launch();
+  std::swap(cur, oth);
+  for (int s = 1; s < H.nu; s++) {
+    k_mg_smooth4<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
+    note_launch();
+    std::swap(cur, oth);
+  }
+  return cudaGetLastError();
+}
+
+namespace {
 
 // Level-0 stencil passes, streamed through shared memory by TMA:
 //   kSpmv      q = A p, pq = p.q, alpha = rz / pq
@@ -896,7 +976,7 @@ cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* sc
   const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
   k_mgp_load<<<g, blk, 0, st>>>(L, rv, scale4(scale, mask), mask, v);
   note_launch();
-  k_mg_smooth<<<g, blk, 0, st>>>(L, vec4(L.t), vec4(v.r), vec4(L.t), H.omega, 1, S, mask);
+  k_mg_smooth4<<<grid4(L, H.nrhs), blk, 0, st>>>(L, vec4(L.t), vec4(v.r), vec4(L.t), H.omega, 1, S, mask);
   note_launch();
   return level0_tail(H, v, S, rb, mask, 1, st);
 }
