@@ -799,10 +799,10 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     L.tn = zeros(L.alloc);
     L.tt = zeros(L.alloc);
     L.dinv = zeros(L.alloc);
-    for (int m = 0; m < nrhs; m++) {
+    for (int m = 0; m < nrhs && H.nlev > 0; m++) {  // level 0 works on the PCG vectors
       L.t[m] = zeros(L.alloc);
-      L.x[m] = H.nlev == 0 ? nullptr : zeros(L.alloc);
-      L.b[m] = H.nlev == 0 ? nullptr : zeros(L.alloc);
+      L.x[m] = zeros(L.alloc);
+      L.b[m] = zeros(L.alloc);
     }
     H.nlev++;
     if (L.n() <= 1024 || H.nlev == kMgMaxLevels) break;
@@ -910,10 +910,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     for (int m = 0; m < nrhs; m++)
       if (live[m] && (!hS[m].active || hS[m].iters >= kMgInnerMax || total >= max_sweeps)) upd |= 1u << m;
     if (!upd) continue;
-    static_assert(offsetof(MgScalars, dir) == offsetof(MgScalars, active) + sizeof(int), "active, dir adjacent");
-    const int zero[2] = {0, 0};
-    for (int m = 0; m < nrhs; m++)  // park them until their restart (active and dir cleared)
-      if ((upd >> m) & 1u) CUDA_TRY(cudaMemcpyAsync(&S[m].active, zero, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    const int zero = 0;
+    for (int m = 0; m < nrhs; m++)  // park them until their restart
+      if ((upd >> m) & 1u) CUDA_TRY(cudaMemcpyAsync(&S[m].active, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(mg_pcg_apply(H, d, v, scale, upd, phis, st));
     unsigned restart = 0;
     for (int m = 0; m < nrhs; m++) {

@@ -249,16 +249,17 @@ struct MgLevel {
   int zc;                      // planes per thread in the one-thread-per-cell kernels: nz / zc
   long long off, sy, sz;       // cell (i, j, k) (0-based) at off + i + sy j + sz k
   long long alloc;             // elements per array
-  float *te, *tn, *tt, *dinv;  // face transmissibilities, inverse diagonal
-  float *x[kMaxRhs], *b[kMaxRhs], *t[kMaxRhs];  // per right-hand side: solution, right-hand side, scratch
+  float *te, *tn, *tt, *dinv;  // face transmissibilities, inverse diagonal (level 0: omega x inverse diagonal)
+  float *x[kMaxRhs], *b[kMaxRhs], *t[kMaxRhs];  // per right-hand side (levels >= 1): solution, right-hand side,
+                                                // scratch
   __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
 };
 constexpr int kMgMaxLevels = 16;
-// Tensor maps of the level-0 TMA passes: the level-0 vectors p, t and r and
-// the level-1 solution x1 of each right-hand side, the level-0 inverse
-// diagonal and the open-face bits.
+// Tensor maps of the level-0 TMA passes: the level-0 vectors z, p and r and
+// the level-1 solution x1 of each right-hand side, level 0's omega D^-1 and
+// the open-face bits.
 struct MgMaps {
-  CUtensorMap p[kMaxRhs], t[kMaxRhs], r[kMaxRhs], x1[kMaxRhs], dinv, fb;
+  CUtensorMap z[kMaxRhs], p[kMaxRhs], r[kMaxRhs], x1[kMaxRhs], dinv, fb;
 };
 struct MgHierarchy {
   int nlev, nrhs;
@@ -285,7 +286,7 @@ struct MgVecs {  // level-0 PCG vectors per right-hand side
 };
 struct MgScalars {  // one per right-hand side
   double rz, rz0, pq, alpha, beta, tol2;
-  int active, dir, iters, pad;
+  int active, pad0, iters, pad;
 };
 // Per-right-hand-side grid reductions: partials holds kMaxRhs x (level-0
 // blocks per right-hand side) doubles, tickets kMaxRhs counters (zero between

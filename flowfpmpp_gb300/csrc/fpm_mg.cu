@@ -123,11 +123,12 @@ __device__ __forceinline__ float face_sum(const MgLevel& L, int i, int j, int k,
   return d;
 }
 
-__global__ void k_mg_dinv(MgLevel L) {
+// dinv = scale / diag (level 0: scale = omega, the smoothing weight folded in)
+__global__ void k_mg_dinv(MgLevel L, float scale) {
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
     const float d = face_sum(L, i, j, k, c);
-    L.dinv[c] = d > 0.f ? 1.f / d : 0.f;
+    L.dinv[c] = d > 0.f ? scale / d : 0.f;
   }
 }
 
@@ -202,7 +203,7 @@ cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const 
     note_launch();
   }
   for (int l = 0; l < H.nlev; l++) {
-    k_mg_dinv<<<mg_grid(H.lv[l]), blk, 0, st>>>(H.lv[l]);
+    k_mg_dinv<<<mg_grid(H.lv[l]), blk, 0, st>>>(H.lv[l], l == 0 ? H.omega : 1.f);
     note_launch();
   }
   return cudaGetLastError();
@@ -566,188 +567,201 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
 
 namespace {
 
-// Level-0 stencil passes, streamed through shared memory by TMA:
-//   kSpmv      q = A p, pq = p.q, alpha = rz / pq
-//   kResidual  b1 = cscale x P^T (r - A t): the residual of the pre-smoothed
-//              iterate, restricted to level 1 on the fly (the two planes of an
-//              aggregate are summed in registers, its two rows through shared
-//              memory; chunks hold whole aggregates)
-//   kSmooth    z = y + omega dinv (r - A y), y = t + P x1 (the pre-smoothed
-//              iterate plus the prolonged level-1 correction), r.z and the PCG
-//              scalar updates (start: rz = rz0; otherwise beta and the stop
-//              test); each operand plane is loaded with the level-1 tile of
-//              its parent plane and turned into y in shared memory when it
-//              lands
+// Level-0 stencil passes, streamed through shared memory by TMA.  Level 0's
+// dinv holds omega D^-1 (wd below).  Each pass loads two operand fields with
+// their x-y halo and turns them into the stencil operand in shared memory
+// when a plane lands:
+//   kSpmv      p = z + beta p_old (the direction update); q = A p, p.q and
+//              alpha = rz / pq.  The new p is written by the update kernel.
+//   kResidual  t = wd r (the first pre-smoothing sweep from zero);
+//              b1 = cscale x P^T (r - A t), the residual restricted to level 1
+//              on the fly (an aggregate's two planes summed in registers, its
+//              two rows through shared memory; chunks hold whole aggregates)
+//   kSmooth    y = wd r + P x1 (the pre-smoothed iterate plus the prolonged
+//              level-1 correction, the level-1 tile of each plane's parents
+//              streamed alongside); z = y + wd (r - A y), r.z and the PCG
+//              scalar updates (start: rz = rz0, beta = 0 and p = 0; otherwise
+//              beta and the stop test)
 // A CTA owns kTX x kTY cells of a plane (a warp per row, four cells per
 // thread) and marches through kc0 planes.  Thread 0 keeps a 4-deep ring of
-// planes of the stencil operand (its tile plus the x-y halo) with their
-// open-face bits in flight, and for kResidual / kSmooth a 3-deep ring of r
-// (and dinv) tiles; every thread reads its seven neighbours from shared
-// memory, so the DRAM stream never waits on a dependent load.
+// planes (both operand tiles, the open-face bits, the level-1 tile) in flight
+// with cp.async.bulk.tensor, completion on mbarriers; every thread reads its
+// seven neighbours from shared memory, so the DRAM stream never waits on a
+// dependent load.  Each thread transforms its own four cells of a landed
+// plane (keeping their raw values for the plane's own step) and threads
+// 0 .. 83 the 84 float4 of the halo.
 //
 // TMA boxes (x coordinates in elements of the MixedGrid row, cell i at 3 + i):
-//   operand  (kTX + 8) x (kTY + 2) floats from (kTX bx, kTY by): cells
+//   operands (kTX + 8) x (kTY + 2) floats from (kTX bx, kTY by): cells
 //            kTX bx - 3 .. kTX bx + kTX + 4, so the tile's cells and both
 //            x neighbours; the x start is a multiple of 4 (16 bytes)
 //   bits     (kTX + 16) x (kTY + 2) bytes from the same corner (x a multiple
 //            of 16 bytes; the bits' row pitch pxb is a multiple of 16)
-//   r, dinv  kTX x kTY floats from (4 + kTX bx, 1 + kTY by): the tile's cells
 //   x1       kCW x kCH floats of level 1 (rows padded to 16 bytes) from
 //            (kTX bx / 2 - 4, kTY by / 2 - 1, parent plane): the parents of
 //            the operand tile's cells
 // Rows and planes outside the grid (plane 0 and nz + 1) read as zero, where
-// the open-face bits are zero as well; the halo cells may pick up a level-1
+// the open-face bits are zero as well; halo cells may pick up a level-1
 // value, which only ever meets a zero face.
 enum { kSpmv = 0, kResidual = 1, kSmooth = 2 };
 constexpr int kTX = 128, kTY = 8, kTThreads = (kTX / 4) * kTY;
 constexpr int kPW = kTX + 8, kPWB = kTX + 16, kPH = kTY + 2;
-constexpr uint32_t kXBytes = kPW * kPH * 4, kBBytes = kPWB * kPH, kCBytes = kTX * kTY * 4;
-constexpr int kCW = kTX / 2 + 8, kCH = kTY / 2 + 2;  // level-1 tile: columns -4 .. kTX/2+3, rows -1 .. kTY/2
-constexpr uint32_t kX1Bytes = kCW * kCH * 4;
+constexpr int kQ = kPW / 4, kHalo4 = 2 * kQ + 2 * kTY;  // float4 per tile row; halo float4 per plane
+constexpr int kCW = kTX / 2 + 8, kCH = kTY / 2 + 2;     // level-1 tile: columns -4 .. kTX/2+3, rows -1 .. kTY/2
+constexpr uint32_t kXBytes = kPW * kPH * 4, kBBytes = kPWB * kPH, kX1Bytes = kCW * kCH * 4;
 constexpr uint32_t kXStage = (kXBytes + 127) / 128 * 128, kBStage = (kBBytes + 127) / 128 * 128,
                    kX1Stage = (kX1Bytes + 127) / 128 * 128;
-constexpr int kXSt = 4, kCSt = 3;
-static_assert((kCW * 4) % 16 == 0, "level-1 box rows are whole 16-byte units");
-static_assert(kPW % 4 == 0 && 2 * (kPW / 4 - 1) + 3 < kCW, "prolongation: float4 rows, parents inside the tile");
+constexpr int kXSt = 4;
 static_assert(kTX % 16 == 0 && kTY % 2 == 0, "tile: bits box start and row pairs");
 static_assert((kPW * 4) % 16 == 0 && kPWB % 16 == 0, "TMA box rows are whole 16-byte units");
+static_assert((kCW * 4) % 16 == 0, "level-1 box rows are whole 16-byte units");
+static_assert(kPW % 4 == 0 && 2 * (kQ - 1) + 3 < kCW, "prolongation: float4 rows, parents inside the tile");
+static_assert(kHalo4 <= kTThreads, "one halo float4 per thread at most");
 
-// Bytes of one operand ring stage (operand, bits, and for kSmooth the level-1 tile).
+// One ring stage: operand A, operand B, bits, and for kSmooth the level-1 tile.
 __host__ __device__ constexpr uint32_t tma_stage(int mode) {
-  return kXStage + kBStage + (mode == kSmooth ? kX1Stage : 0u);
+  return 2 * kXStage + kBStage + (mode == kSmooth ? kX1Stage : 0u);
 }
-__host__ __device__ constexpr uint32_t tma_smem(int mode) {
-  return kXSt * tma_stage(mode) + (mode == kSpmv ? 0u : kCSt * 2 * kCBytes) + 8 * (kXSt + kCSt);
-}
+__host__ __device__ constexpr uint32_t tma_smem(int mode) { return kXSt * tma_stage(mode) + 8 * kXSt; }
 
 template <int MODE>
 __global__ void __launch_bounds__(kTThreads, 3)
     k_mg0_tma(const __grid_constant__ MgMaps M, MixedGrid G, int kc, MgLevel L, MgLevel C, Ops0 O, MgVecs v,
-              float omega, float cscale, MgScalars* S, MgRed rb, unsigned mask, int start) {
+              float cscale, MgScalars* S, MgRed rb, unsigned mask, int start) {
   const int zc = (G.nz + kc - 1) / kc;
   const int m = (int)blockIdx.z / zc;
   MG_SKIP(m);
   if (*reinterpret_cast<volatile int*>(rb.err)) return;  // an earlier wait gave up: the solve is abandoned
   const int k0 = ((int)blockIdx.z - m * zc) * kc + 1;
   const int k1 = min(G.nz, k0 + kc - 1);
-  extern __shared__ __align__(128) unsigned char smem[];
   constexpr uint32_t kStage = tma_stage(MODE);
-  unsigned char* cs = smem + kXSt * kStage;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(cs + (MODE == kSpmv ? 0 : kCSt * 2 * kCBytes));
-  const uint32_t s_base = tma::smem_u32(smem), c_base = tma::smem_u32(cs), bar_base = tma::smem_u32(bars);
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kXSt * kStage);
+  const uint32_t s_base = tma::smem_u32(smem), bar_base = tma::smem_u32(bars);
   const int tid = threadIdx.x, q = tid & 31, ty = tid >> 5;
   const int x0 = kTX * (int)blockIdx.x, y0 = kTY * (int)blockIdx.y;
   P0 t;
   t.g = x0 / 4 + q;
   t.j = y0 + ty + 1;
   t.live = t.g < G.ng && t.j <= G.ny;
-  const CUtensorMap* mx = MODE == kSpmv ? (m == 0 ? &M.p[0] : m == 1 ? &M.p[1] : m == 2 ? &M.p[2] : &M.p[3])
-                                        : (m == 0 ? &M.t[0] : m == 1 ? &M.t[1] : m == 2 ? &M.t[2] : &M.t[3]);
-  const CUtensorMap* mr = m == 0 ? &M.r[0] : m == 1 ? &M.r[1] : m == 2 ? &M.r[2] : &M.r[3];
+  // operand A: z (kSpmv) or r; operand B: p (kSpmv) or wd
+  const CUtensorMap* ma = MODE == kSpmv ? (m == 0 ? &M.z[0] : m == 1 ? &M.z[1] : m == 2 ? &M.z[2] : &M.z[3])
+                                        : (m == 0 ? &M.r[0] : m == 1 ? &M.r[1] : m == 2 ? &M.r[2] : &M.r[3]);
+  const CUtensorMap* mb = MODE == kSpmv ? (m == 0 ? &M.p[0] : m == 1 ? &M.p[1] : m == 2 ? &M.p[2] : &M.p[3])
+                                        : &M.dinv;
   const CUtensorMap* m1 = m == 0 ? &M.x1[0] : m == 1 ? &M.x1[1] : m == 2 ? &M.x1[2] : &M.x1[3];
+  const float beta = MODE == kSpmv ? (float)S[m].beta : 0.f;
   if (tid == 0) {
-    for (int s = 0; s < kXSt + kCSt; s++) tma::mbar_init(bar_base + 8 * s, 1);
+    for (int s = 0; s < kXSt; s++) tma::mbar_init(bar_base + 8 * s, 1);
     tma::mbar_init_fence();
   }
   __syncthreads();
-  // Operand / bits plane p (p = k0 - 1 .. k1 + 1) goes to ring slot
-  // (p - (k0 - 1)) % kXSt, r / dinv plane p (k0 .. k1) to (p - k0) % kCSt; the
-  // n-th use of a slot completes its barrier's phase n.
-  auto issue_x = [&](int p) {
+  // Plane p (p = k0 - 1 .. k1 + 1) goes to ring slot (p - (k0 - 1)) % kXSt;
+  // the n-th use of a slot completes its barrier's phase n.
+  auto issue = [&](int p) {
     const int s = (p - (k0 - 1)) % kXSt;
     const uint32_t bar = bar_base + 8 * s, dst = s_base + s * kStage;
-    tma::mbar_expect_tx(bar, kXBytes + kBBytes + (MODE == kSmooth ? kX1Bytes : 0u));
-    tma::load_3d(dst, mx, x0, y0, p - 1, bar);
-    tma::load_3d(dst + kXStage, &M.fb, x0, y0, p - 1, bar);
-    if (MODE == kSmooth) tma::load_3d(dst + kXStage + kBStage, m1, x0 / 2 - 4, y0 / 2 - 1, (p - 1) >> 1, bar);
+    tma::mbar_expect_tx(bar, 2 * kXBytes + kBBytes + (MODE == kSmooth ? kX1Bytes : 0u));
+    tma::load_3d(dst, ma, x0, y0, p - 1, bar);
+    tma::load_3d(dst + kXStage, mb, x0, y0, p - 1, bar);
+    tma::load_3d(dst + 2 * kXStage, &M.fb, x0, y0, p - 1, bar);
+    if (MODE == kSmooth) tma::load_3d(dst + 2 * kXStage + kBStage, m1, x0 / 2 - 4, y0 / 2 - 1, (p - 1) >> 1, bar);
   };
-  // kSmooth: operand plane p (just landed) += its cells' level-1 parents.
-  // Columns 4a .. 4a+3 of a tile row have the parents 2a+2, 2a+2, 2a+3, 2a+3
-  // of the level-1 tile; tile row r has the parent row ((r - 1) >> 1) + 1.
-  auto prolong = [&](int p) {
-    if (MODE != kSmooth) return;
-    unsigned char* st = smem + ((p - (k0 - 1)) % kXSt) * kStage;
-    float* X = reinterpret_cast<float*>(st);
-    const float* X1 = reinterpret_cast<const float*>(st + kXStage + kBStage);
-    constexpr int kQ = kPW / 4;  // float4 per tile row
-    for (int e = tid; e < kPH * kQ; e += kTThreads) {
-      const int r = e / kQ, a = e - r * kQ;
-      float4* x4 = reinterpret_cast<float4*>(X + r * kPW) + a;
-      const float2 c = *reinterpret_cast<const float2*>(X1 + (((r - 1) >> 1) + 1) * kCW + 2 * a + 2);
-      float4 v4 = *x4;
-      v4.x += c.x;
-      v4.y += c.x;
-      v4.z += c.y;
-      v4.w += c.y;
-      *x4 = v4;
-    }
-  };
-  auto issue_c = [&](int p) {
-    const int s = (p - k0) % kCSt;
-    const uint32_t bar = bar_base + 8 * (kXSt + s), dst = c_base + s * 2 * kCBytes;
-    tma::mbar_expect_tx(bar, (MODE == kSmooth ? 2 : 1) * kCBytes);
-    tma::load_3d(dst, mr, 4 + x0, y0 + 1, p - 1, bar);
-    if (MODE == kSmooth) tma::load_3d(dst + kCBytes, &M.dinv, 4 + x0, y0 + 1, p - 1, bar);
-  };
-  auto x_ready = [&](int p) {
+  auto ready = [&](int p) {
     const int u = p - (k0 - 1);
     return tma::mbar_wait(bar_base + 8 * (u % kXSt), (uint32_t)((u / kXSt) & 1));
   };
-  auto c_ready = [&](int p) {
-    const int u = p - k0;
-    return tma::mbar_wait(bar_base + 8 * (kXSt + u % kCSt), (uint32_t)((u / kCSt) & 1));
+  // The stencil operand of plane p: kResidual keeps it in B's place, the
+  // others in A's.
+  auto operand = [&](int p) {
+    return reinterpret_cast<float*>(smem + ((p - (k0 - 1)) % kXSt) * kStage + (MODE == kResidual ? kXStage : 0));
   };
-  int next_x = k0 - 1, next_c = k0;
-  if (tid == 0) {
-    for (; next_x <= k0 + 2 && next_x <= k1 + 1; next_x++) issue_x(next_x);
-    if (MODE != kSpmv)
-      for (; next_c <= k0 + 2 && next_c <= k1; next_c++) issue_c(next_c);
-  }
+  const int oc = (ty + 1) * kPW + 4 + 4 * q;  // this thread's four cells in a tile plane
+  // Turn plane p into the stencil operand; own_a / own_b: the raw A and B
+  // values of this thread's cells.
+  auto transform = [&](int p, float4& own_a, float4& own_b) {
+    unsigned char* st = smem + ((p - (k0 - 1)) % kXSt) * kStage;
+    float* A = reinterpret_cast<float*>(st);
+    float* B = reinterpret_cast<float*>(st + kXStage);
+    const float* X1 = reinterpret_cast<const float*>(st + 2 * kXStage + kBStage);
+    auto one = [&](int e, int r, int a4, float4& ra, float4& rb4) {  // float4 e = (row r, column 4 a4)
+      ra = *reinterpret_cast<const float4*>(A + e);
+      rb4 = *reinterpret_cast<const float4*>(B + e);
+      const float2 a0 = lo2(ra), a1 = hi2(ra), b0 = lo2(rb4), b1 = hi2(rb4);
+      float2 r0, r1;
+      if (MODE == kSpmv) {  // p = z + beta p_old
+        r0 = __ffma2_rn(dup2(beta), b0, a0);
+        r1 = __ffma2_rn(dup2(beta), b1, a1);
+      } else if (MODE == kResidual) {  // t = wd r
+        r0 = __fmul2_rn(b0, a0);
+        r1 = __fmul2_rn(b1, a1);
+      } else {  // y = wd r + parent (columns 4a4, 4a4+1 -> 2a4+2; 4a4+2, 4a4+3 -> 2a4+3)
+        const float2 c = *reinterpret_cast<const float2*>(X1 + (((r - 1) >> 1) + 1) * kCW + 2 * a4 + 2);
+        r0 = __ffma2_rn(b0, a0, dup2(c.x));
+        r1 = __ffma2_rn(b1, a1, dup2(c.y));
+      }
+      *reinterpret_cast<float4*>((MODE == kResidual ? B : A) + e) = make_float4(r0.x, r0.y, r1.x, r1.y);
+    };
+    one(oc, ty + 1, q + 1, own_a, own_b);
+    if (tid < kHalo4) {
+      int r, a4;
+      if (tid < kQ) {
+        r = 0;
+        a4 = tid;
+      } else if (tid < 2 * kQ) {
+        r = kPH - 1;
+        a4 = tid - kQ;
+      } else {
+        r = 1 + ((tid - 2 * kQ) >> 1);
+        a4 = ((tid - 2 * kQ) & 1) ? kQ - 1 : 0;
+      }
+      float4 da, db;
+      one(r * kPW + 4 * a4, r, a4, da, db);
+    }
+  };
+  int next = k0 - 1;
+  if (tid == 0)
+    for (; next <= k0 + 2 && next <= k1 + 1; next++) issue(next);
 
   float* __restrict__ out = MODE == kSpmv ? v.q[m] : (MODE == kResidual ? C.b[m] : v.z[m]);
   // kResidual: the odd rows' aggregate sums, double-buffered by aggregate
   // plane (with an odd nz the last two planes complete aggregates in
   // consecutive steps)
   __shared__ float2 pair_sum[2][kTY / 2][32];
-  float2 agg = make_float2(0.f, 0.f);        // kResidual: this row's sums of the group's two aggregates
-  const int i0 = 4 * t.g;                    // first cell of the group (0-based)
-  const int cx = (ty + 1) * kPW + 4 + 4 * q, cb = (ty + 1) * kPWB + 4 + 4 * q, cc = ty * kTX + 4 * q;
+  float2 agg = make_float2(0.f, 0.f);  // kResidual: this row's sums of the group's two aggregates
+  const int i0 = 4 * t.g;              // first cell of the group (0-based)
+  const int cb = (ty + 1) * kPWB + 4 + 4 * q;
   const Row0 R = row0(O, t);
   Acc2 acc;
   float2 ttb[2];  // bottom faces of the current plane: the previous plane's top faces
-  bool ok = x_ready(k0 - 1) && x_ready(k0);
-  if (MODE == kSmooth && ok) {
-    prolong(k0 - 1);
-    prolong(k0);
+  float4 cur_a = zero4(), cur_b = zero4(), nxt_a = zero4(), nxt_b = zero4();
+  bool ok = ready(k0 - 1) && ready(k0);
+  if (ok) {
+    transform(k0 - 1, nxt_a, nxt_b);
+    transform(k0, cur_a, cur_b);
   }
   {
-    const uint8_t* Bb = smem + kXStage;  // bits of plane k0 - 1 (slot 0)
+    const uint8_t* Bb = smem + 2 * kXStage;  // bits of plane k0 - 1 (slot 0)
     bottom2(R, k0 > 1 ? __ldg(O.azt + k0 - 2) : 0.f, ok ? *reinterpret_cast<const uint32_t*>(Bb + cb) : 0u, ttb);
   }
   int kfail = k0;
   bool failed = false;
   for (int k = k0; k <= k1; k++) {
-    ok = ok && x_ready(k + 1) && (MODE == kSpmv || c_ready(k));
-    if (MODE == kSmooth) {
-      if (ok) prolong(k + 1);
-      __syncthreads();
-    }
+    ok = ok && ready(k + 1);
+    if (ok) transform(k + 1, nxt_a, nxt_b);
+    __syncthreads();
     const bool pair_done = MODE == kResidual && (((k - 1) & 1) || k == G.nz);
     if (ok && t.live) {
-      const int u = k - k0;  // plane k - 1 is in slot u % kXSt
-      const unsigned char* s0 = smem + (u % kXSt) * kStage;
-      const unsigned char* s1 = smem + ((u + 1) % kXSt) * kStage;
-      const unsigned char* s2 = smem + ((u + 2) % kXSt) * kStage;
-      const float* X0 = reinterpret_cast<const float*>(s0);
-      const float* X1 = reinterpret_cast<const float*>(s1);
-      const float* X2 = reinterpret_cast<const float*>(s2);
-      const uint8_t* B1 = s1 + kXStage;
-      const float4 pc = *reinterpret_cast<const float4*>(X1 + cx);
-      const float4 pb = *reinterpret_cast<const float4*>(X0 + cx);
-      const float4 pt = *reinterpret_cast<const float4*>(X2 + cx);
-      const float4 ps = *reinterpret_cast<const float4*>(X1 + cx - kPW);
-      const float4 pn = *reinterpret_cast<const float4*>(X1 + cx + kPW);
-      const float left = X1[cx - 1], right = X1[cx + 4];
+      const float* X0 = operand(k - 1);
+      const float* X1p = operand(k);
+      const float* X2 = operand(k + 1);
+      const uint8_t* B1 = smem + ((k - (k0 - 1)) % kXSt) * kStage + 2 * kXStage;
+      const float4 pc = *reinterpret_cast<const float4*>(X1p + oc);
+      const float4 pb = *reinterpret_cast<const float4*>(X0 + oc);
+      const float4 pt = *reinterpret_cast<const float4*>(X2 + oc);
+      const float4 ps = *reinterpret_cast<const float4*>(X1p + oc - kPW);
+      const float4 pn = *reinterpret_cast<const float4*>(X1p + oc + kPW);
+      const float left = X1p[oc - 1], right = X1p[oc + 4];
       const uint32_t f4 = *reinterpret_cast<const uint32_t*>(B1 + cb);
       const uint32_t fs4 = *reinterpret_cast<const uint32_t*>(B1 + cb - kPWB);
       const Faces2 Fc = faces2(R, __ldg(O.dz + k - 1), __ldg(O.azt + k - 1), f4, fs4, B1[cb - 1]);
@@ -758,22 +772,20 @@ __global__ void __launch_bounds__(kTThreads, 3)
       if (MODE == kSpmv) {
         st4(out + base, uu);
         acc.add4(pc, uu);
+      } else if (MODE == kResidual) {
+        const float4& rr = cur_a;
+        agg.x += (rr.x - uu.x) + (rr.y - uu.y);
+        agg.y += (rr.z - uu.z) + (rr.w - uu.w);
       } else {
-        const float* Rt = reinterpret_cast<const float*>(cs + (u % kCSt) * 2 * kCBytes);
-        const float4 rr = *reinterpret_cast<const float4*>(Rt + cc);
-        if (MODE == kResidual) {
-          agg.x += (rr.x - uu.x) + (rr.y - uu.y);
-          agg.y += (rr.z - uu.z) + (rr.w - uu.w);
-        } else {
-          const float4 dv = *reinterpret_cast<const float4*>(Rt + kTX * kTY + cc);
-          float zz[4];
+        const float4 &rr = cur_a, &wd = cur_b;
+        float zz[4];
 #pragma unroll
-          for (int n = 0; n < 4; n++)
-            zz[n] = i0 + n < L.nx ? fmaf(omega * el(dv, n), el(rr, n) - el(uu, n), el(pc, n)) : 0.f;
-          const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
-          st4(out + base, z4);
-          acc.add4(rr, z4);
-        }
+        for (int n = 0; n < 4; n++)
+          zz[n] = i0 + n < L.nx ? fmaf(el(wd, n), el(rr, n) - el(uu, n), el(pc, n)) : 0.f;
+        const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
+        st4(out + base, z4);
+        if (start) st4(v.p[m] + base, zero4());  // the first direction is z itself
+        acc.add4(rr, z4);
       }
     }
     // rows 2c and 2c+1 (0-based) of an aggregate are warps ty = 2h and 2h+1
@@ -793,17 +805,13 @@ __global__ void __launch_bounds__(kTThreads, 3)
       }
       agg = make_float2(0.f, 0.f);
     }
-    if (tid == 0) {
-      if (next_x <= k1 + 1) issue_x(next_x++);
-      if (MODE != kSpmv && next_c <= k1) issue_c(next_c++);
-    }
+    cur_a = nxt_a;
+    cur_b = nxt_b;
+    if (tid == 0 && next <= k1 + 1) issue(next++);
   }
   if (failed && tid == 0) {
     atomicExch(rb.err, 1);
-    // drain the copies still in flight (bounded) before the CTA exits
-    for (int p = kfail - 1; p < next_x; p++) x_ready(p);
-    if (MODE != kSpmv)
-      for (int p = kfail; p < next_c; p++) c_ready(p);
+    for (int p = kfail - 1; p < next; p++) ready(p);  // drain the copies still in flight (bounded)
   }
   if (MODE == kResidual) return;
   // every block of the right-hand side takes part, also after a failure
@@ -826,64 +834,41 @@ __global__ void __launch_bounds__(kTThreads, 3)
     Q.rz0 = rz;
     Q.beta = 0.0;
     Q.active = rz > 0 ? 1 : 0;
-    Q.dir = Q.active;
     return;
   }
   Q.iters += 1;
   if (!(rz >= 0)) {
     Q.active = 0;
-    Q.dir = 0;
     return;
   }
   Q.beta = rz / Q.rz;
   Q.rz = rz;
-  Q.dir = 1;
   if (rz <= Q.tol2 * Q.rz0) Q.active = 0;
 }
 
-// e += alpha p; r -= alpha q; t = omega dinv r (the V-cycle's first
-// pre-smoothing sweep from zero)
-__global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgLevel L, MgVecs v, float omega, const MgScalars* S,
-                                                    unsigned mask) {
+// p = z + beta p (the direction the spmv pass used), e += alpha p,
+// r -= alpha q: pointwise, so p is updated in place.
+__global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgVecs v, const MgScalars* S, unsigned mask) {
   const P0 t = p0_pos(G);
   MG_SKIP(t.m);
   if (!t.live) return;
-  const float a = (float)S[t.m].alpha;
-  const float* __restrict__ p = pick(v.p, t.m);
+  const float a = (float)S[t.m].alpha, bt = (float)S[t.m].beta;
+  const float* __restrict__ z = pick(v.z, t.m);
   const float* __restrict__ q = pick(v.q, t.m);
+  float* __restrict__ p = pick(v.p, t.m);
   float* __restrict__ e = pick(v.e, t.m);
   float* __restrict__ r = pick(v.r, t.m);
-  float* __restrict__ tt = pick(L.t, t.m);
   long long base = t.base;
   for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
-    const float4 pp = ld4(p + base), qq = ld4(q + base), dv = ld4(L.dinv + base);
-    float4 ee = *reinterpret_cast<const float4*>(e + base), rr = *reinterpret_cast<const float4*>(r + base);
+    const float4 zz = ld4(z + base), qq = ld4(q + base);
+    float4 pp = *reinterpret_cast<const float4*>(p + base), ee = *reinterpret_cast<const float4*>(e + base),
+           rr = *reinterpret_cast<const float4*>(r + base);
+    pp = make_float4(fmaf(bt, pp.x, zz.x), fmaf(bt, pp.y, zz.y), fmaf(bt, pp.z, zz.z), fmaf(bt, pp.w, zz.w));
     ee = make_float4(fmaf(a, pp.x, ee.x), fmaf(a, pp.y, ee.y), fmaf(a, pp.z, ee.z), fmaf(a, pp.w, ee.w));
     rr = make_float4(fmaf(-a, qq.x, rr.x), fmaf(-a, qq.y, rr.y), fmaf(-a, qq.z, rr.z), fmaf(-a, qq.w, rr.w));
+    st4(p + base, pp);
     st4(e + base, ee);
     st4(r + base, rr);
-    st4(tt + base, make_float4(omega * dv.x * rr.x, omega * dv.y * rr.y, omega * dv.z * rr.z, omega * dv.w * rr.w));
-  }
-}
-
-// p = z + beta p (start: p = z).  dir stays set once a right-hand side has
-// stopped, so later launches of the same chunk may rescale its p again; the
-// next start overwrites p, so that direction is never used.
-__global__ void __launch_bounds__(128) k_mg0_direction(MixedGrid G, MgVecs v, const MgScalars* S, unsigned mask,
-                                                       int start) {
-  const P0 t = p0_pos(G);
-  if (!((mask >> t.m) & 1u) || !(start || S[t.m].dir)) return;
-  if (!t.live) return;
-  const float b = start ? 0.f : (float)S[t.m].beta;
-  const float* __restrict__ z = pick(v.z, t.m);
-  float* __restrict__ p = pick(v.p, t.m);
-  long long base = t.base;
-  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
-    const float4 zz = ld4(z + base);
-    const float4 pp = *reinterpret_cast<const float4*>(p + base);
-    st4(p + base, start ? zz
-                        : make_float4(fmaf(b, pp.x, zz.x), fmaf(b, pp.y, zz.y), fmaf(b, pp.z, zz.z),
-                                      fmaf(b, pp.w, zz.w)));
   }
 }
 
@@ -949,23 +934,21 @@ Scale4 scale4(const double* s, unsigned mask) {
 
 }  // namespace
 
-// Level-0 V-cycle tail shared by start and iteration: restriction of
-// r - A t, the coarse cycle (which adds its prolonged correction to t), and
-// the post-smoothing + r.z pass.
+// Level-0 V-cycle tail shared by start and iteration: the residual of the
+// first smoothing sweep restricted to level 1, the coarse cycle, and the
+// post-smoothing + r.z pass.
 static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, unsigned mask,
                                int start, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const MgLevel& C = H.lv[1];
-  const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4), gt = tma_grid(H);
-  k_mg0_tma<kResidual><<<gt, kTThreads, tma_smem(kResidual), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.omega,
-                                                                   H.cscale, S, rb, mask, start);
+  const dim3 gt = tma_grid(H);
+  k_mg0_tma<kResidual><<<gt, kTThreads, tma_smem(kResidual), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.cscale,
+                                                                   S, rb, mask, start);
   note_launch();
   cudaError_t e = vcycle(H, 1, S, mask, st);
   if (e != cudaSuccess) return e;
-  k_mg0_tma<kSmooth><<<gt, kTThreads, tma_smem(kSmooth), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.omega,
-                                                                 H.cscale, S, rb, mask, start);
-  note_launch();
-  k_mg0_direction<<<g0, b0, 0, st>>>(H.g0, v, S, mask, start);
+  k_mg0_tma<kSmooth><<<gt, kTThreads, tma_smem(kSmooth), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.cscale, S,
+                                                                 rb, mask, start);
   note_launch();
   return cudaGetLastError();
 }
@@ -973,22 +956,19 @@ static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, co
 cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* scale, unsigned mask, MgVecs& v,
                          MgScalars* S, const MgRed& rb, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
-  const dim3 blk(32, 8), g = rhs_grid(L, H.nrhs);
-  k_mgp_load<<<g, blk, 0, st>>>(L, rv, scale4(scale, mask), mask, v);
-  note_launch();
-  k_mg_smooth4<<<grid4(L, H.nrhs), blk, 0, st>>>(L, vec4(L.t), vec4(v.r), vec4(L.t), H.omega, 1, S, mask);
+  k_mgp_load<<<rhs_grid(L, H.nrhs), dim3(32, 8), 0, st>>>(L, rv, scale4(scale, mask), mask, v);
   note_launch();
   return level0_tail(H, v, S, rb, mask, 1, st);
 }
 
+// One PCG iteration: direction + q = A p, the PCG update, the V-cycle.
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
   const unsigned all = (1u << H.nrhs) - 1u;
-  const dim3 g0 = g0_grid(H.g0, H.nrhs), b0(32, 4);
   k_mg0_tma<kSpmv><<<tma_grid(H), kTThreads, tma_smem(kSpmv), st>>>(H.maps, H.g0, H.kc0, L, H.lv[1], ops0(H), v,
-                                                                     H.omega, H.cscale, S, rb, all, 0);
+                                                                     H.cscale, S, rb, all, 0);
   note_launch();
-  k_mg0_update<<<g0, b0, 0, st>>>(H.g0, L, v, H.omega, S, all);
+  k_mg0_update<<<g0_grid(H.g0, H.nrhs), dim3(32, 4), 0, st>>>(H.g0, v, S, all);
   note_launch();
   return level0_tail(H, v, S, rb, all, 0, st);
 }
@@ -1014,14 +994,14 @@ cudaError_t mg_encode(MgHierarchy& H, const MgVecs& v) {
   };
   bool ok = true;
   for (int m = 0; m < H.nrhs; m++) {
-    ok = ok && f32(&H.maps.p[m], v.p[m], kPW, kPH) && f32(&H.maps.t[m], H.lv[0].t[m], kPW, kPH) &&
-         f32(&H.maps.r[m], v.r[m], kTX, kTY);
+    ok = ok && f32(&H.maps.z[m], v.z[m], kPW, kPH) && f32(&H.maps.p[m], v.p[m], kPW, kPH) &&
+         f32(&H.maps.r[m], v.r[m], kPW, kPH);
   }
   const MgLevel& L1 = H.lv[1];
   for (int m = 0; m < H.nrhs; m++)
     ok = ok && tma_encode_3d(&H.maps.x1[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, L1.x[m], (uint64_t)L1.sy,
                              (uint64_t)L1.ny, (uint64_t)L1.nz, 4ULL * L1.sy, 4ULL * L1.sz, kCW, kCH);
-  ok = ok && f32(&H.maps.dinv, H.lv[0].dinv, kTX, kTY) &&
+  ok = ok && f32(&H.maps.dinv, H.lv[0].dinv, kPW, kPH) &&
        tma_encode_3d(&H.maps.fb, CU_TENSOR_MAP_DATA_TYPE_UINT8, H.fb0, (uint64_t)H.pxb, rows, G.nz, (uint64_t)H.pxb,
                      (uint64_t)H.pxb * rows, kPWB, kPH);
   if (!ok) return cudaErrorInvalidValue;
