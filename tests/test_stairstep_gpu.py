@@ -258,18 +258,14 @@ def test_pcg_mixed_matches_fp64_oracle(gpu_lib, method):
     assert ge["res"] <= 2e-10 and errors[0] < 1e-9 and errors[1] < 1e-9 and errors[3] == 0 and ierr < 1e-10
 
 
-@pytest.mark.parametrize("method", [0, 3, 4])
-def test_multi_rhs_three_influence_fields(gpu_lib, method):
-    """phi_x, phi_y, phi_z of a stretched-grid sphere in one call (FP64 one
-    after the other, mixed precision batched, or multigrid-preconditioned FP32)
-    against the FP64 oracle."""
-    import torch
+def _multi_rhs_vs_oracle(gpu_lib, f, method, axes=(0, 1, 2)):
+    """Potentials for the body moving along each of axes, solved in one call,
+    against the FP64 oracle one by one."""
     from flowfpmpp_gb300 import stairstep as ss
-    from flowfpmpp_gb300 import workloads
-    f = workloads.sphere_c1(nx=40, ny=36, nz=24)
     nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    n = len(axes)
     phis, rhss, faces_dev, bgs, refs = [], [], [], [], []
-    for axis in range(3):
+    for axis in axes:
         body = np.zeros(3)
         body[axis] = 1.0
         faces = [x.copy(order="F") for x in f["faces"]]
@@ -284,16 +280,38 @@ def test_multi_rhs_three_influence_fields(gpu_lib, method):
         bgs.append(body)
     dax = [to_dev(f[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
     VP = ctypes.c_void_p
-    phi_arr = (VP * 3)(*[t.data_ptr() for t in phis])
-    rhs_arr = (VP * 3)(*[t.data_ptr() for t in rhss])
-    face_arr = (VP * 18)(*[t.data_ptr() for t in faces_dev])
+    phi_arr = (VP * n)(*[t.data_ptr() for t in phis])
+    rhs_arr = (VP * n)(*[t.data_ptr() for t in rhss])
+    face_arr = (VP * (6 * n))(*[t.data_ptr() for t in faces_dev])
     bg = np.ascontiguousarray(np.concatenate(bgs))
-    sweeps = (I * 3)()
-    res = (D * 3)()
-    rc = gpu_lib.fpm_solve_stairstep_multi_dev(3, phi_arr, rhs_arr, ptr(to_dev(f["solid"])),
+    sweeps = (I * n)()
+    res = (D * n)()
+    rc = gpu_lib.fpm_solve_stairstep_multi_dev(n, phi_arr, rhs_arr, ptr(to_dev(f["solid"])),
                                                bg.ctypes.data_as(VP), face_arr, *[ptr(x) for x in dax], nx, ny, nz,
                                                D(1e-10), 100000, 50, method, sweeps, res, stream_ptr())
     assert rc == 0, gpu_lib.fpm_last_error()
-    for m in range(3):
+    for m in range(n):
         assert res[m] <= 2e-10
         assert rel_linf(from_dev(phis[m], refs[m].shape), refs[m]) <= 1e-9
+
+
+@pytest.mark.parametrize("method", [0, 3, 4])
+def test_multi_rhs_three_influence_fields(gpu_lib, method):
+    """phi_x, phi_y, phi_z of a stretched-grid sphere in one call (FP64 one
+    after the other, mixed precision batched, or multigrid-preconditioned FP32)
+    against the FP64 oracle."""
+    from flowfpmpp_gb300 import workloads
+    _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_c1(nx=40, ny=36, nz=24), method)
+
+
+@pytest.mark.parametrize("dims,kchunk,axes", [((37, 29, 11), 16, (0, 1, 2)), ((133, 21, 37), 16, (0, 2)),
+                                              ((150, 17, 6), 2, (1,)), ((64, 12, 33), 4, (2, 0, 1)),
+                                              ((259, 9, 5), 6, (0, 1))])
+def test_multigrid_tile_edges(gpu_lib, monkeypatch, dims, kchunk, axes):
+    """The multigrid path on shapes that end level-0 TMA tiles mid-tile in x
+    (nx not a multiple of 4 or of 128) and y (ny not a multiple of 8), chunks
+    mid-aggregate in z (odd nz, several chunks, chunks of 2 planes), with one
+    to three right-hand sides: potentials within 1e-9 of the FP64 oracle."""
+    from flowfpmpp_gb300 import workloads
+    monkeypatch.setenv("FPM_MG_KCHUNK", str(kchunk))
+    _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_c1(*dims), 4, axes)
