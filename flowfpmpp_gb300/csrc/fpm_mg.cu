@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, V
 // post-smoothing sweep in one pass.  Fine cells 4g .. 4g+3 have the coarse
 // parents 2g, 2g, 2g+1, 2g+1 (a float2 of the coarse row: 2g is even and
 // the row starts on 16 bytes).
-__global__ void __launch_bounds__(256) k_mg_prolong_smooth4(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv,
+__global__ void __launch_bounds__(256, 3) k_mg_prolong_smooth4(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv,
                                                             Vec4 xov, float omega, const MgScalars* S,
                                                             unsigned mask) {
   MG_RHS(F);
@@ -587,9 +587,12 @@ namespace {
 // planes (both operand tiles, the open-face bits, the level-1 tile) in flight
 // with cp.async.bulk.tensor, completion on mbarriers; every thread reads its
 // seven neighbours from shared memory, so the DRAM stream never waits on a
-// dependent load.  Each thread transforms its own four cells of a landed
-// plane (keeping their raw values for the plane's own step) and threads
-// 0 .. 83 the 84 float4 of the halo.
+// dependent load.  Each
+// thread transforms its own four cells of a landed plane (keeping their raw
+// values for the plane's own step) and threads 0 .. 83 the 84 float4 of the
+// halo, one step ahead of the plane's use as the top neighbour.  (Transforming
+// two steps ahead saves a barrier per plane but shortens the TMA prefetch
+// distance; measured slower.)
 //
 // TMA boxes (x coordinates in elements of the MixedGrid row, cell i at 3 + i):
 //   operands (kTX + 8) x (kTY + 2) floats from (kTX bx, kTY by): cells
@@ -611,7 +614,7 @@ constexpr int kCW = kTX / 2 + 8, kCH = kTY / 2 + 2;     // level-1 tile: columns
 constexpr uint32_t kXBytes = kPW * kPH * 4, kBBytes = kPWB * kPH, kX1Bytes = kCW * kCH * 4;
 constexpr uint32_t kXStage = (kXBytes + 127) / 128 * 128, kBStage = (kBBytes + 127) / 128 * 128,
                    kX1Stage = (kX1Bytes + 127) / 128 * 128;
-constexpr int kXSt = 4;
+constexpr int kXSt = 4;  // planes k-1 .. k+1 in use, k+2 in flight
 static_assert(kTX % 16 == 0 && kTY % 2 == 0, "tile: bits box start and row pairs");
 static_assert((kPW * 4) % 16 == 0 && kPWB % 16 == 0, "TMA box rows are whole 16-byte units");
 static_assert((kCW * 4) % 16 == 0, "level-1 box rows are whole 16-byte units");
@@ -721,7 +724,7 @@ __global__ void __launch_bounds__(kTThreads, 3)
   };
   int next = k0 - 1;
   if (tid == 0)
-    for (; next <= k0 + 2 && next <= k1 + 1; next++) issue(next);
+    for (; next <= k0 + kXSt - 2 && next <= k1 + 1; next++) issue(next);
 
   float* __restrict__ out = MODE == kSpmv ? v.q[m] : (MODE == kResidual ? C.b[m] : v.z[m]);
   // kResidual: the odd rows' aggregate sums, double-buffered by aggregate
@@ -734,6 +737,7 @@ __global__ void __launch_bounds__(kTThreads, 3)
   const Row0 R = row0(O, t);
   Acc2 acc;
   float2 ttb[2];  // bottom faces of the current plane: the previous plane's top faces
+  // raw A / B values of this thread's cells: plane k (cur), k + 1 (nxt)
   float4 cur_a = zero4(), cur_b = zero4(), nxt_a = zero4(), nxt_b = zero4();
   bool ok = ready(k0 - 1) && ready(k0);
   if (ok) {
@@ -755,13 +759,14 @@ __global__ void __launch_bounds__(kTThreads, 3)
       const float* X0 = operand(k - 1);
       const float* X1p = operand(k);
       const float* X2 = operand(k + 1);
-      const uint8_t* B1 = smem + ((k - (k0 - 1)) % kXSt) * kStage + 2 * kXStage;
       const float4 pc = *reinterpret_cast<const float4*>(X1p + oc);
+      // (x neighbours from the adjacent lanes by shuffles measured slower)
+      const float left = X1p[oc - 1], right = X1p[oc + 4];
+      const uint8_t* B1 = smem + ((k - (k0 - 1)) % kXSt) * kStage + 2 * kXStage;
       const float4 pb = *reinterpret_cast<const float4*>(X0 + oc);
       const float4 pt = *reinterpret_cast<const float4*>(X2 + oc);
       const float4 ps = *reinterpret_cast<const float4*>(X1p + oc - kPW);
       const float4 pn = *reinterpret_cast<const float4*>(X1p + oc + kPW);
-      const float left = X1p[oc - 1], right = X1p[oc + 4];
       const uint32_t f4 = *reinterpret_cast<const uint32_t*>(B1 + cb);
       const uint32_t fs4 = *reinterpret_cast<const uint32_t*>(B1 + cb - kPWB);
       const Faces2 Fc = faces2(R, __ldg(O.dz + k - 1), __ldg(O.azt + k - 1), f4, fs4, B1[cb - 1]);
