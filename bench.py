@@ -22,13 +22,14 @@ workload: the oracle is the reference arm because the reference itself is
 Fortran/OpenACC and no Fortran compiler is available.
 
 Other workloads (one GPU, a JSON line each):
-  pcg_c1, pcg_c3  phi_x, phi_y, phi_z to a 1e-10 max-norm residual with plain
-                  FP64 PCG, FP32 PCG in FP64 refinement (diagonal and multigrid
-                  preconditioners) and the learned initial guess; value is the
-                  multigrid arm's solve time
-  frames_c4       256 uneven 2-D foil frames, two potentials and the four
+  pcg_sphere      sphere on 64x64x32 and
+  pcg_ellipsoids  3 ellipsoids on 384x384x192: phi_x, phi_y, phi_z to a 1e-10
+                  max-norm residual with plain FP64 PCG, FP32 PCG in FP64
+                  refinement (diagonal and multigrid preconditioners) and the
+                  learned initial guess; value is the multigrid arm's solve time
+  foil_frames     256 uneven 2-D foil frames, two potentials and the four
                   partition terms each
-  learned_c5      the trained network as initial guess on unseen bodies
+  learned_guess   the trained network as initial guess on unseen bodies
 
 Multi-GPU: replicas only (each rank solves its own copy; no collective on the
 data path); value is the sum over ranks divided by the slowest rank's time.
@@ -63,19 +64,19 @@ def parse():
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
-                    help="pcg_c3 only: a smaller grid of the same generator (profiling runs)")
+                    help="pcg_ellipsoids only: a smaller grid of the same generator (profiling runs)")
     ap.add_argument("--arms", default="fp64,mixed,mg,learned_mixed,learned_mg",
-                    help="pcg_c1 / pcg_c3: comma-separated solver arms to time (profiling runs take one)")
-    ap.add_argument("--workload", choices=["jacobi256", "pcg_c1", "pcg_c3", "frames_c4", "learned_c5"],
+                    help="pcg_sphere / pcg_ellipsoids: comma-separated solver arms to time (profiling runs take one)")
+    ap.add_argument("--workload", choices=["jacobi256", "pcg_sphere", "pcg_ellipsoids", "foil_frames", "learned_guess"],
                     default="jacobi256",
-                    help="jacobi256: the headline bandwidth benchmark; pcg_c1 / pcg_c3: three-potential PCG "
+                    help="jacobi256: the headline bandwidth benchmark; pcg_sphere / pcg_ellipsoids: three-potential PCG "
                          "time to 1e-10 (plain FP64 vs mixed precision)")
     return ap.parse_args()
 
 
 def workload(n):
     from flowfpmpp_gb300 import workloads
-    return workloads.boxes_c2(n=n)
+    return workloads.boxes_grid(n=n)
 
 
 def config(n):
@@ -222,15 +223,15 @@ def run_pcg(args):
     from flowfpmpp_gb300 import stairstep as ss
     from flowfpmpp_gb300 import workloads
     lib = flowfpmpp_gb300.lib()
-    if args.workload == "pcg_c1":
-        f = workloads.sphere_c1()
-        name = "C1 64x64x32 sphere, ratio 1.03"
+    if args.workload == "pcg_sphere":
+        f = workloads.sphere_grid()
+        name = "sphere 64x64x32, ratio 1.03"
     elif args.grid:
-        f = workloads.ellipsoids_c3(*args.grid)
-        name = "C3 generator at %dx%dx%d, 3 ellipsoids, ratio 1.02" % tuple(args.grid)
+        f = workloads.ellipsoids_grid(*args.grid)
+        name = "3 ellipsoids %dx%dx%d, ratio 1.02" % tuple(args.grid)
     else:
-        f = workloads.ellipsoids_c3()
-        name = "C3 384x384x192, 3 ellipsoids, ratio 1.02"
+        f = workloads.ellipsoids_grid()
+        name = "3 ellipsoids 384x384x192, ratio 1.02"
     nx, ny, nz = f["nx"], f["ny"], f["nz"]
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
     faces_dev, bgs, rhss = [], [], []
@@ -312,7 +313,7 @@ def run_pcg(args):
 
 
 def run_learned(args):
-    """Config 5: the committed trained network as initial guess on unseen
+    """The committed trained network as initial guess on unseen
     random bodies at 256x256x128 (the training set was 128x128x64), FP64 PCG
     to 1e-10 from phi = 0 and from the learned guess; iterations, time and
     fallbacks over `steps` bodies (after `warmup` bodies)."""
@@ -343,7 +344,7 @@ def run_learned(args):
     line = {"metric": "FP64 PCG solve time to 1e-10 with the learned initial guess vs from phi = 0",
             "value": float(a[:, 4].mean()), "unit": "s per body", "higher_is_better": False, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded random bodies)",
-            "config": {"workload": "C5 unseen bodies 256x256x128, network trained on 2000 bodies at 128x128x64",
+            "config": {"workload": "unseen bodies 256x256x128, network trained on 2000 bodies at 128x128x64",
                        "tolerance": 1e-10, "bodies": len(rows)},
             "plain": {"seconds": float(a[:, 1].mean()), "iterations": float(a[:, 0].mean())},
             "learned": {"seconds": float(a[:, 4].mean()), "iterations": float(a[:, 3].mean()),
@@ -354,7 +355,7 @@ def run_learned(args):
 
 
 def run_frames(args):
-    """Config 4: 256 uneven 2-D foil frames (96^2..512^2 cells), phi_x and
+    """256 uneven 2-D foil frames (96^2..512^2 cells), phi_x and
     phi_y to a 1e-10 max-norm residual and the four partition terms for both,
     all frames batched; host arrays in and out (the C ABI call a user makes)."""
     import torch
@@ -362,7 +363,7 @@ def run_frames(args):
     fbuild.build()
     from flowfpmpp_gb300 import partition as pt
     from flowfpmpp_gb300 import workloads
-    frames = workloads.foil_frames_c4()
+    frames = workloads.foil_frames()
     cells = sum(f["nx"] * f["ny"] for f in frames)
     for _ in range(args.warmup):
         pt.partition_frames_2d(frames, tolerance=1e-10)
@@ -374,7 +375,7 @@ def run_frames(args):
     line = {"metric": "batched 2-D frames: phi_x, phi_y to 1e-10 and the four FPM terms",
             "value": len(frames) / el, "unit": "frames/s", "higher_is_better": True, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "seconds_per_batch": el, "data": "synthetic (seeded)",
-            "config": {"workload": "C4 256 foil frames 96^2..512^2, ratio 1.02", "frames": len(frames),
+            "config": {"workload": "256 foil frames 96^2..512^2, ratio 1.02", "frames": len(frames),
                        "cells_2d": int(cells), "tolerance": 1e-10},
             "cell_potentials_per_s": 2 * cells / el, "max_residual": float(np.max(res)),
             "fp32_iterations": {"max": int(sweeps.max()), "mean": float(sweeps.mean())},
@@ -395,13 +396,13 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
-    if args.workload == "learned_c5":
+    if args.workload == "learned_guess":
         if rank == 0:
             run_learned(args)
         return
     if args.workload != "jacobi256":
         if rank == 0:
-            run_frames(args) if args.workload == "frames_c4" else run_pcg(args)
+            run_frames(args) if args.workload == "foil_frames" else run_pcg(args)
         return
     dist = None
     if world > 1:

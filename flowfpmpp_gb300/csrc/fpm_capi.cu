@@ -769,7 +769,9 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   // compact; the level-0 passes take an even number of planes per chunk (whole
   // aggregates)
   H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk() + (mixed_kchunk() & 1));
-  H.kc0 = (int)env_double("FPM_MG_KCHUNK", 24);  // C3: 16 -> 0.726 s, 24 -> 0.716 s, 48 -> 0.715 s
+  // planes per CTA of the level-0 TMA passes (three potentials on 384 x 384 x 192:
+  // 16 -> 0.726 s, 24 -> 0.716 s, 48 -> 0.715 s)
+  H.kc0 = (int)env_double("FPM_MG_KCHUNK", 24);
   H.kc0 = H.kc0 < 2 ? 2 : H.kc0 + (H.kc0 & 1);
   H.pxb = (H.g0.px + 15) / 16 * 16;
   auto zeros = [&](long long n) {

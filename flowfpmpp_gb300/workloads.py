@@ -75,8 +75,8 @@ def _frame(nx, ny, nz, ax, ay, az, solid_interior, axis):
                 phi=np.zeros((nx + 2, ny + 2, nz), order="F"), body=body, faces=_empty_faces(nx, ny, nz))
 
 
-def boxes_c2(n=256, seed=2025, ratio=1.01, half=4.0, nboxes=4):
-    """Config 2: n^3 grid, four axis-aligned boxes of 8-40 cells per side at
+def boxes_grid(n=256, seed=2025, ratio=1.01, half=4.0, nboxes=4):
+    """Weighted-Jacobi bandwidth case: n^3 grid, four axis-aligned boxes of 8-40 cells per side at
     seeded positions, the first one touching the outer boundary (x = -half)."""
     rng = np.random.default_rng(seed)
     ax = geometric_axis(n, -half, half, ratio)
@@ -92,8 +92,8 @@ def boxes_c2(n=256, seed=2025, ratio=1.01, half=4.0, nboxes=4):
     return _frame(n, n, n, ax, ax, ax, solid, 0)
 
 
-def sphere_c1(nx=64, ny=64, nz=32, ratio=1.03, radius=0.5, axis=0):
-    """Config 1: stretched grid on [-4,4]^2 x [-2,2], sphere at the origin."""
+def sphere_grid(nx=64, ny=64, nz=32, ratio=1.03, radius=0.5, axis=0):
+    """Plain-PCG case: stretched grid on [-4,4]^2 x [-2,2], sphere at the origin."""
     ax = geometric_axis(nx, -4.0, 4.0, ratio)
     ay = geometric_axis(ny, -4.0, 4.0, ratio)
     az = geometric_axis(nz, -2.0, 2.0, ratio)
@@ -113,8 +113,8 @@ def _rotation(rng):
                      [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
 
 
-def ellipsoids_c3(nx=384, ny=384, nz=192, ratio=1.02, seed=3, count=3, axis=0, w0=0.01):
-    """Config 3: union of `count` random ellipsoids (semi-axes 0.3-1.0, random
+def ellipsoids_grid(nx=384, ny=384, nz=192, ratio=1.02, seed=3, count=3, axis=0, w0=0.01):
+    """Three-potential PCG case: union of `count` random ellipsoids (semi-axes 0.3-1.0, random
     orientation, centres within 1.0 of the origin, 0.5 in z) on axes of
     smallest cell w0 (at least [-2,2] in z)."""
     rng = np.random.default_rng(seed)
@@ -179,9 +179,9 @@ def flow_c1(frame, seed=11, ntubes=8, core=0.2, nmodes=6):
     return dict(u=F(u), v=F(v), w=F(w), ox=F(ox), oy=F(oy), oz=F(oz), ax=F(acc[0]), ay=F(acc[1]), az=F(acc[2]))
 
 
-def foil_frames_c4(nframes=256, seed=4, nmin=96, nmax=512, ratio=1.02, half_x=4.0, half_y=4.0, nvort=12,
+def foil_frames(nframes=256, seed=4, nmin=96, nmax=512, ratio=1.02, half_x=4.0, half_y=4.0, nvort=12,
                    dt=0.4, nu=1e-4, w0=0.01):
-    """Config 4: uneven 2-D frames in the fpm_partition_2d form.  Each frame:
+    """Batched-frames case: uneven 2-D frames in the fpm_partition_2d form.  Each frame:
     nx, ny ~ U[nmin, nmax], geometric stretching `ratio` away from the centre
     lines from a smallest cell w0, the domain at least [-half_x, half_x] x
     [-half_y, half_y]; vortex centres lie in that box; an elliptic foil (chord 1, thickness 0.12) at pitch U[-30, 30]

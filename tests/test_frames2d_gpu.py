@@ -35,7 +35,7 @@ def oracle_frame(fr, tol):
 def test_batched_frames_match_oracle(gpu_lib):
     from flowfpmpp_gb300 import partition as pt
     from flowfpmpp_gb300 import workloads
-    frames = workloads.foil_frames_c4(nframes=5, seed=21, nmin=40, nmax=90)
+    frames = workloads.foil_frames(nframes=5, seed=21, nmin=40, nmax=90)
     tol = 1e-11
     terms, sweeps, res, phis = pt.partition_frames_2d(frames, tolerance=tol, return_phi=True)
     assert np.all(res <= 2 * tol), res

@@ -301,7 +301,7 @@ def test_multi_rhs_three_influence_fields(gpu_lib, method):
     after the other, mixed precision batched, or multigrid-preconditioned FP32)
     against the FP64 oracle."""
     from flowfpmpp_gb300 import workloads
-    _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_c1(nx=40, ny=36, nz=24), method)
+    _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_grid(nx=40, ny=36, nz=24), method)
 
 
 @pytest.mark.parametrize("dims,kchunk,axes", [((37, 29, 11), 16, (0, 1, 2)), ((133, 21, 37), 16, (0, 2)),
@@ -314,4 +314,4 @@ def test_multigrid_tile_edges(gpu_lib, monkeypatch, dims, kchunk, axes):
     to three right-hand sides: potentials within 1e-9 of the FP64 oracle."""
     from flowfpmpp_gb300 import workloads
     monkeypatch.setenv("FPM_MG_KCHUNK", str(kchunk))
-    _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_c1(*dims), 4, axes)
+    _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_grid(*dims), 4, axes)
