@@ -1,7 +1,7 @@
 """ctypes bindings for the CPU oracle (``fpm_oracle.c``).
 
 Test infrastructure only: tests, ``__graft_entry__.smoke()`` and ``bench.py``'s
-CPU-baseline leg use this package as the checker.  The product library
+CPU-baseline leg use this package to check and time results.  The product library
 (``flowfpmpp_gb300``) never imports it.
 
 Arrays follow the reference's Fortran layout, held in numpy arrays with

@@ -1,6 +1,6 @@
 /*
- * fpm_oracle.c -- CPU restatement of FlowFPM++'s hot path, used ONLY as a
- * parity checker and as the timed CPU baseline (test infrastructure: nothing
+ * fpm_oracle.c -- CPU restatement of FlowFPM++'s hot path, used ONLY as the
+ * parity oracle and as the timed CPU baseline (test infrastructure: nothing
  * in the product library links or calls this file).
  *
  * Each function follows the reference Fortran routine named in its comment,
