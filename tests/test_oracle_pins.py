@@ -1,6 +1,6 @@
 """Pins the CPU oracle against every known answer the reference's own tests
 and README hold for this path.  CPU only (no GPU): these decide whether the
-oracle can be trusted as the checker of the CUDA kernels.
+oracle can be trusted as the reference for the CUDA kernels' results.
 
 Sources (reference repository):
   tests/test_stairstep_exact_3d.f90  thresholds :46-48, :68-70; README.md:114-119
