@@ -955,7 +955,92 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
 // solve them one after the other; FPM_METHOD_PCG_MIXED solves them together.
 static bool valid_method(int m) {
   return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED ||
-         m == FPM_METHOD_PCG_MG;
+         m == FPM_METHOD_PCG_MG || m == FPM_METHOD_FCG_LEARNED;
+}
+
+// FPM_METHOD_FCG_LEARNED: FP64 flexible CG (Notay's FCG(1): the Polak-Ribiere
+// beta = z_k.(r_k - r_{k-1}) / z_{k-1}.r_{k-1} keeps the method a CG for a
+// preconditioner that changes between applications) with z = M(r) the
+// network-based preconditioner of launch_fcg_precond.  The true residual
+// replaces the recursive one every check_interval iterations, convergence is
+// the reference's max-norm test, and the loop stops after the same number of
+// checks without a 1 % improvement as the FP64 PCG (the caller then finishes
+// with FP64 PCG).  Returns the max-norm residual.
+static double fcg_learned_loop(void* net, const SolveArgs& a, const Dims& d, double* p, const double* src,
+                               const double* diag, const double* rdiag, const Coefs& c, Scratch& A, Common& cm,
+                               int* sweeps, cudaStream_t st) {
+  const long long nc = d.ncell();
+  double* r = A.get<double>(nc);
+  double* q = A.get<double>(nc);
+  double* z = A.get<double>(nc);
+  double* rprev = A.get<double>(nc);
+  CUDA_TRY(cudaMemsetAsync(rprev, 0, nc * sizeof(double), st));
+  FcgWork w;
+  w.fluid = A.get<uint8_t>(nc);
+  w.mx = A.get<float>(d.nx);
+  w.my = A.get<float>(d.ny);
+  w.mz = A.get<float>(d.nz);
+  w.b = A.get<float>(nc);
+  w.y = A.get<float>(nc);
+  w.ay = A.get<double>(nc);
+  w.sc = A.get<double>(8);
+  // fluid flags and metric channels (b is refilled from r before every use)
+  CUDA_TRY(launch_learn_inputs(d, src, diag, a.ax, w.fluid, w.mx, w.my, w.mz, w.b, w.sc, cm.rb, st));
+  CUDA_TRY(launch_true_residual(d, a.phi, src, diag, rdiag, r, p, c, a.ax, 0, cm.S, cm.rb, st));
+  double res = read_scalars(cm.S, st).res, best = res;
+  const int ci = a.ci < 1 ? 1 : a.ci;
+  const int max_stalled = stall_checks();
+  int it = 0, stalled = 0, restarts = 0;
+  double zr_prev = 0.0;
+  bool restart = true;
+  double h[2];
+  const int zero = 0;
+  while (it < a.max_sweeps && res > a.tol) {
+    std::string err;
+    int status = 0;
+    CUDA_TRY(launch_fcg_precond(d, net, r, rprev, diag, rdiag, c, a.ax, w, z, cm.rb, st, &err, &status));
+    if (status != FPM_OK) throw Error{status, err};
+    CUDA_TRY(cudaMemcpyAsync(h, w.sc + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const double zr = h[0];
+    if (!(zr > 0)) {  // the preconditioned residual lost positivity: restart, give up on the second time
+      if (++restarts > 1) break;
+      restart = true;
+      CUDA_TRY(launch_true_residual(d, a.phi, src, diag, rdiag, r, p, c, a.ax, 0, cm.S, cm.rb, st));
+      res = read_scalars(cm.S, st).res;
+      continue;
+    }
+    const double beta = restart || !(zr_prev > 0) ? 0.0 : (zr - h[1]) / zr_prev;
+    CUDA_TRY(launch_fcg_direction(d, z, p, beta, st));
+    CUDA_TRY(cudaMemcpyAsync(&cm.S->rz, &zr, sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&cm.S->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(launch_pcg_spmv(d, p, q, diag, c, a.ax, cm.S, cm.rb, st));
+    CUDA_TRY(launch_fcg_update(d, a.phi, p, q, r, rprev, cm.S, st));
+    zr_prev = zr;
+    restart = false;
+    it++;
+    if (it % ci == 0 || it >= a.max_sweeps) {
+      const SolveScalars& hs = read_scalars(cm.S, st);
+      if (hs.halt) {  // p.q <= 0: restart from the true residual
+        if (++restarts > 1) break;
+        restart = true;
+      } else {
+        restarts = 0;
+      }
+      CUDA_TRY(launch_true_residual(d, a.phi, src, diag, rdiag, r, p, c, a.ax, 0, cm.S, cm.rb, st));
+      res = read_scalars(cm.S, st).res;
+      if (verbose()) std::fprintf(stderr, "fpm fcg_learned: iterations %d residual %.3e\n", it, res);
+      if (res < 0.99 * best) {
+        best = res;
+        stalled = 0;
+      } else {
+        stalled++;
+      }
+      if (stalled >= max_stalled || !(res == res)) break;
+    }
+  }
+  *sweeps = it;
+  return res;
 }
 
 // Learned initial guess for every right-hand side (see fpm_learned.cu): the
@@ -1049,7 +1134,18 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
         sweeps[m] += extra;
       }
     };
-    if (a0.method == FPM_METHOD_PCG_MG) {
+    if (a0.method == FPM_METHOD_FCG_LEARNED) {
+      if (!net) throw Error{FPM_E_METHOD, "the learned flexible CG needs the network (fpm_solve_stairstep_learned_dev)"};
+      int to64[kMaxRhs] = {};
+      for (int m = 0; m < nrhs; m++) {
+        const SolveArgs& a = args[m];
+        CUDA_TRY(launch_init_fields(d, a.solid, a.phi, next, st));
+        CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
+        const double res = fcg_learned_loop(net, a, d, next, src[m], diag, rdiag, c, A, cm, &sweeps[m], st);
+        to64[m] = res > a.tol ? 1 : 0;
+      }
+      finish_fp64(to64);
+    } else if (a0.method == FPM_METHOD_PCG_MG) {
       double* phis[kMaxRhs] = {};
       for (int m = 0; m < nrhs; m++) phis[m] = args[m].phi;
       int to64[kMaxRhs] = {};

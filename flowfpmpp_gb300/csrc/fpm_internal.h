@@ -321,6 +321,22 @@ cudaError_t launch_learn_apply(const Dims& d, const float* y, const double* src,
                                const Axes& ax, double* phi, double* dots, const RedBuf& rb, cudaStream_t st);
 cudaError_t launch_energy(const Dims& d, const double* phi, const double* src, const double* diag, const Coefs& c,
                           const Axes& ax, double* out2, const RedBuf& rb, cudaStream_t st);
+// Learned flexible CG: work arrays of the preconditioner (compact cell order).
+struct FcgWork {
+  uint8_t* fluid;            // network inputs prepared once per solve
+  float *mx, *my, *mz;
+  float *b, *y;              // network input channel (r / max |r|) and output
+  double* ay;                // A y_f
+  double* sc;                // [0] max |r|, [2..3] (y.r, y.Ay), [4..5] (z.r, z.r_prev)
+};
+cudaError_t launch_fcg_precond(const Dims& d, void* net, const double* r, const double* rprev, const double* diag,
+                               const double* rdiag, const Coefs& c, const Axes& ax, const FcgWork& w, double* z,
+                               const RedBuf& rb, cudaStream_t st, std::string* err, int* status);
+cudaError_t launch_fcg_direction(const Dims& d, const double* z, double* p, double beta, cudaStream_t st);
+cudaError_t launch_fcg_update(const Dims& d, double* phi, const double* p, const double* q, double* r, double* rprev,
+                              const SolveScalars* S, cudaStream_t st);
+cudaError_t launch_pcg_spmv(const Dims& d, const double* p, double* q, const double* diag, const Coefs& c,
+                            const Axes& ax, SolveScalars* S, const RedBuf& rb, cudaStream_t st);
 namespace net {
 // Network forward pass into out (FP32, one value per cell); returns an FPM_*
 // status and fills *err on failure.

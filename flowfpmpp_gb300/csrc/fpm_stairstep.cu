@@ -345,6 +345,12 @@ __global__ void k_pcg_direction(Dims d, double* __restrict__ p, const double* __
   CELL_LOOP_END
   if (lin_bid() == 0 && lin_tid() == 0) S->iters += 1;
 }
+cudaError_t launch_pcg_spmv(const Dims& d, const double* p, double* q, const double* diag, const Coefs& c,
+                            const Axes& ax, SolveScalars* S, const RedBuf& rb, cudaStream_t st) {
+  Launch L = cells_launch(d);
+  k_pcg_spmv<<<L.grid, L.block, 0, st>>>(d, p, q, diag, c, ax, S, rb); note_launch();
+  return cudaGetLastError();
+}
 cudaError_t launch_pcg_iteration(const Dims& d, double* phi, double* p, double* q, double* r, const double* diag,
                                  const double* rdiag, const Coefs& c, const Axes& ax, SolveScalars* S,
                                  const RedBuf& rb, cudaStream_t st) {

@@ -19,7 +19,7 @@ import numpy as np
 
 from ._lib import check, lib
 
-METHODS = {"pcg": 0, "jacobi": 1, "jacobi_df": 2, "pcg_mixed": 3, "pcg_mg": 4}
+METHODS = {"pcg": 0, "jacobi": 1, "jacobi_df": 2, "pcg_mixed": 3, "pcg_mg": 4, "fcg_learned": 5}
 
 _D = ctypes.c_double
 _I = ctypes.c_int

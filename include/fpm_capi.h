@@ -62,6 +62,9 @@ extern "C" {
                                    around FP32 diagonal PCG; max_sweeps caps the FP32 iterations */
 #define FPM_METHOD_PCG_MG 4     /* the refinement of FPM_METHOD_PCG_MIXED around FP32 PCG preconditioned by an
                                    aggregation multigrid V-cycle (no reference counterpart) */
+#define FPM_METHOD_FCG_LEARNED 5 /* FP64 flexible CG with the learned network as preconditioner (one diagonal
+                                    step on what the network leaves); FP64 PCG finishes if it stalls.  Only
+                                    through fpm_solve_stairstep_learned_dev (it needs the network) */
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char* fpm_last_error(void);

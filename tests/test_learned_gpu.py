@@ -102,6 +102,26 @@ def test_learned_solve_matches_plain_solve(gpu_lib):
         assert fb in (0, 1)
 
 
+def test_learned_flexible_cg(gpu_lib):
+    """The flexible CG with the network as preconditioner reaches the
+    tolerance and the plain FP64 PCG potential (1e-9 relative), with an
+    untrained network as well (the diagonal step keeps the preconditioner
+    useful; a stalled run is finished by FP64 PCG); without the network the
+    method is refused."""
+    from flowfpmpp_gb300 import FpmError
+    from flowfpmpp_gb300.learned import LearnedGuess
+    p = _problem(32, 32, 16, seed=8, axis=1)
+    ref, sw0, r0, _ = p.solve("pcg", tol=1e-10)
+    ref = ref.cpu().numpy()
+    for net in (LearnedGuess(seed=4), LearnedGuess(seed=9)):
+        phi, sw1, r1, _ = p.solve("fcg_learned", tol=1e-10, net=net)
+        print(f"fcg_learned: {sw1} iterations (plain PCG {sw0}), residual {r1:.2e}")
+        assert r1 <= 1e-10
+        assert np.abs(phi.cpu().numpy() - ref).max() <= 1e-9 * np.abs(ref).max()
+    with pytest.raises(FpmError):
+        p.solve("fcg_learned", tol=1e-10)
+
+
 def test_trained_network_guess(gpu_lib):
     """What the committed trained network gains, on unseen bodies at the
     training size: its output is within 50 % (relative L2 over fluid cells,
@@ -126,7 +146,12 @@ def test_trained_network_guess(gpu_lib):
         yc, tc = y[f] - y[f].mean(), phi[f] - phi[f].mean()
         rel = np.linalg.norm(tc - (yc @ tc) / (yc @ yc) * yc) / np.linalg.norm(tc)
         _, sw1, r1, fb = p.solve("pcg", tol=1e-10, net=net)
-        print(f"body {seed}: guess error {rel:.3f}, PCG iterations {sw0} -> {sw1}")
+        msg = f"body {seed}: guess error {rel:.3f}, PCG iterations {sw0} -> {sw1}"
+        if seed == 1001:  # the flexible CG with the network, once (it is slow)
+            _, sw2, r2, _ = p.solve("fcg_learned", tol=1e-10, net=net)
+            msg += f", flexible CG with the network {sw2}"
+            assert r2 <= 1e-10
+        print(msg)
         assert rel < 0.5, rel
         assert r1 <= 1e-10 and fb == 0
         assert sw1 <= 1.1 * sw0, (sw0, sw1)
