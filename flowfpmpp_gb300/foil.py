@@ -35,9 +35,12 @@ def frame_axes(fr):
     return dx, dy, xc, yc
 
 
-def partition_frame(fr, method="pcg", tolerance=1e-10, nu=1.0 / RE):
+def partition_frame(fr, method="pcg", tolerance=1e-10, nu=1.0 / RE, phi0=None):
     """Returns dict(terms (2,4), sweeps (2,), residual (2,), phi (2,nx,ny),
-    vif (2,nx,ny), omega (nx,ny), seconds)."""
+    vif (2,nx,ny), omega (nx,ny), seconds, phi3 (the two padded 3-D
+    potentials)).  phi0: the padded potentials to start from (the solver's
+    initial guess, src/fpm_stairstep_mpi_3d.f90:110), e.g. the previous
+    frame's phi3; default zero."""
     nx, ny, nz = fr["nx"], fr["ny"], 2
     dx, dy, xc, yc = frame_axes(fr)
     dz = np.array([0.5, 0.5])
@@ -47,14 +50,14 @@ def partition_frame(fr, method="pcg", tolerance=1e-10, nu=1.0 / RE):
         solid[1:nx + 1, 1:ny + 1, k] = fr["solid"]
     rhs = np.zeros((nx, ny, nz), order="F")
     out = dict(terms=np.zeros((2, 4)), sweeps=np.zeros(2, dtype=int), residual=np.zeros(2),
-               phi=np.zeros((2, nx, ny)), vif=np.zeros((2, nx, ny)))
+               phi=np.zeros((2, nx, ny)), vif=np.zeros((2, nx, ny)), phi3=[None, None])
     t0 = time.perf_counter()
     for d in range(2):
         body = np.zeros(3)
         body[d] = 1.0
         faces = [np.zeros(s, order="F") for s in ((ny, nz), (ny, nz), (nx, nz), (nx, nz), (nx, ny), (nx, ny))]
         ss.enforce_stairstep_compatibility_3d(rhs, solid, body, *faces, dx, dy, dz)
-        phi = np.zeros((nx + 2, ny + 2, nz), order="F")
+        phi = np.zeros((nx + 2, ny + 2, nz), order="F") if phi0 is None else np.array(phi0[d], order="F")
         sw, res = ss.solve_stairstep_poisson_3d(phi, rhs, solid, body, *faces, xc, yc, zc, dx, dy, dz, tolerance,
                                                 2000000, 50, method)
         p2 = np.asfortranarray(phi[1:nx + 1, 1:ny + 1, 0])
@@ -62,8 +65,45 @@ def partition_frame(fr, method="pcg", tolerance=1e-10, nu=1.0 / RE):
                                                       fr["yf"], fr["kin"], fr["ring"], fr["dt"], nu)
         out["terms"][d], out["sweeps"][d], out["residual"][d] = terms, sw, res
         out["phi"][d], out["vif"][d] = p2, vif
+        out["phi3"][d] = phi
         out["omega"] = omega
     out["seconds"] = time.perf_counter() - t0
+    return out
+
+
+def ring_from_neighbours(prev, nxt):
+    """The F_BOUND ring of a frame from its neighbouring dumps: u and v in the
+    outer-boundary cells (west column, east column, south row, north row) of
+    the dump before and the dump after, and dt half their time distance
+    (the layout of the FFPM2D02 ring, src/fpm_partition_2d.f90:84-87)."""
+    nx, ny = prev["nx"], prev["ny"]
+    ring = np.zeros((2 * nx + 2 * ny, 2, 2), order="F")
+    for t, fr in ((0, prev), (1, nxt)):
+        for comp, key in ((0, "u"), (1, "v")):
+            a = fr[key]
+            ring[:, comp, t] = np.concatenate([a[0, :], a[nx - 1, :], a[:, 0], a[:, ny - 1]])
+    return ring, 0.5 * (nxt["time"] - prev["time"])
+
+
+def partition_series(frames, method="pcg_mg", tolerance=1e-10, nu=1.0 / RE, warm=True, ring="file"):
+    """Force partition of a time series of dumps on one grid: each frame as
+    partition_frame, its potentials started from the previous frame's when
+    `warm` (the solver takes phi as its initial guess; cells that turned solid
+    are zeroed by the solver), and with ring="neighbours" the F_BOUND ring of
+    the interior frames taken from the dumps before and after
+    (ring_from_neighbours; the first and last frames keep their own).
+    Returns the list of partition_frame results."""
+    out, prev = [], None
+    for k, fr in enumerate(frames):
+        if prev is not None and (fr["nx"], fr["ny"]) != (frames[k - 1]["nx"], frames[k - 1]["ny"]):
+            raise ValueError("a series must stay on one grid")
+        f = fr
+        if ring == "neighbours" and 0 < k < len(frames) - 1:
+            r, dt = ring_from_neighbours(frames[k - 1], frames[k + 1])
+            f = dict(fr, ring=r, dt=dt)
+        res = partition_frame(f, method, tolerance, nu, phi0=prev["phi3"] if (warm and prev is not None) else None)
+        out.append(res)
+        prev = res
     return out
 
 

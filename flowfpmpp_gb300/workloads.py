@@ -229,6 +229,72 @@ def foil_frames(nframes=256, seed=4, nmin=96, nmax=512, ratio=1.02, half_x=4.0, 
     return frames
 
 
+def foil_series(nframes=6, nx=192, ny=160, seed=7, ratio=1.02, half_x=4.0, half_y=4.0, nvort=8, dt=0.05,
+                period=2.0, w0=0.01):
+    """A time series of 2-D dumps on one grid (FFPM2D02 frame dicts with
+    `time`): an elliptic foil (chord 1, thickness 0.12) pitching 20 deg sin(w t)
+    and heaving 0.3 sin(w t + 1) (w = 2 pi / period), velocity U = 1 plus
+    `nvort` Lamb-Oseen vortices carried downstream at U = 1; dumps every dt,
+    each frame's outer ring holding the boundary cells' u, v of the same field
+    at t -/+ dt (so interior frames' rings equal their neighbours' boundary
+    cells); kin from the analytic rigid-body motion."""
+    rng = np.random.default_rng(seed)
+    xf, xc, dx = geometric_axis_w0(nx, w0, ratio, half_x)
+    yf, yc, dy = geometric_axis_w0(ny, w0, ratio, half_y)
+    X = xc[1:nx + 1][:, None] * np.ones((nx, ny))
+    Y = yc[1:ny + 1][None, :] * np.ones((nx, ny))
+    vort = [(rng.uniform(-half_x, half_x), rng.uniform(-half_y, half_y), rng.standard_normal(), rng.uniform(0.05, 0.2))
+            for _ in range(nvort)]
+    w = 2 * math.pi / period
+    amp_p, amp_h = math.radians(20.0), 0.3
+
+    def motion(t):  # pitch, heave and their first two time derivatives
+        return (amp_p * math.sin(w * t), amp_p * w * math.cos(w * t), -amp_p * w * w * math.sin(w * t),
+                amp_h * math.sin(w * t + 1), amp_h * w * math.cos(w * t + 1), -amp_h * w * w * math.sin(w * t + 1))
+
+    def solid_at(t):
+        pitch, _, _, heave, _, _ = motion(t)
+        cp, sp = math.cos(pitch), math.sin(pitch)
+        xr = cp * X + sp * (Y - heave)
+        yr = -sp * X + cp * (Y - heave)
+        return ((xr / 0.5) ** 2 + (yr / 0.06) ** 2 < 1.0).astype(np.uint8)
+
+    def field(t, solid):
+        u = np.ones((nx, ny))
+        v = np.zeros((nx, ny))
+        for x0, y0, gam, rc in vort:
+            r2 = (X - x0 - t) ** 2 + (Y - y0) ** 2
+            fac = np.where(r2 > 0, gam / (2 * math.pi) * (1 - np.exp(-r2 / rc ** 2)) / np.where(r2 > 0, r2, 1.0), 0.0)
+            u -= fac * (Y - y0)
+            v += fac * (X - x0 - t)
+        fluid = solid == 0
+        return u * fluid, v * fluid
+
+    def boundary(a):
+        return np.concatenate([a[0, :], a[nx - 1, :], a[:, 0], a[:, ny - 1]])
+
+    frames = []
+    for k in range(nframes):
+        t = k * dt
+        solid = solid_at(t)
+        u, v = field(t, solid)
+        ring = np.zeros((2 * nx + 2 * ny, 2, 2), order="F")
+        for tt, ts in ((0, t - dt), (1, t + dt)):
+            ub, vb = field(ts, solid_at(ts))
+            ring[:, 0, tt] = boundary(ub)
+            ring[:, 1, tt] = boundary(vb)
+        pitch, dp, ddp, heave, dh, ddh = motion(t)
+        # rotation by the pitch about (0, heave): with U_B = (k1 - k3 y, k2 + k3 x)
+        # and a_B = (k4 - k6 y - k3^2 x, k5 + k6 x - k3^2 y), k3 = d(pitch)/dt,
+        # k6 = its derivative, k1 = k3 heave, k2 = d(heave)/dt, k4 = k6 heave,
+        # k5 = d2(heave)/dt2 + k3^2 heave
+        kin = np.array([dp * heave, dh, dp, ddp * heave, ddh + dp * dp * heave, ddp])
+        frames.append(dict(nx=nx, ny=ny, xf=xf, yf=yf, xc=xc, yc=yc, dx=dx, dy=dy,
+                           solid=np.asfortranarray(solid), u=np.asfortranarray(u), v=np.asfortranarray(v),
+                           ring=ring, kin=kin, dt=dt, time=t))
+    return frames
+
+
 def frame_as_stairstep(fr):
     """The reference's 2-D use of the 3-D solver (examples/flapping_foil_fpm.f90:
     nz = 2, dz = 0.5, zero z-face data): padded solid, axes and zero faces."""
