@@ -276,7 +276,9 @@ struct MgHierarchy {
   float *aex, *dxr;   // row layout (index 3 + i, i 1-based), zero outside
   float *dy, *ayn;    // index j - 1
   float *dz, *azt;    // index k - 1
-  int nu;             // pre- and post-smoothing sweeps
+  int nu;             // pre- and post-smoothing sweeps (one)
+  int gamma;          // cycles on the next coarser problem for the levels l < gamma_depth (1: V-cycle)
+  int gamma_depth;
   int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block per right-hand side)
   float omega;        // Jacobi weight
   float cscale;       // coarse-correction scale (1 = plain Galerkin correction)

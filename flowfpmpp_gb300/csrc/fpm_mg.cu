@@ -529,10 +529,19 @@ dim3 grid4r(const MgLevel& C, int nrhs) {  // k_mg_resrestrict4: two coarse cell
 
 }  // namespace
 
-// x = V-cycle(b) on level l >= 1 for every right-hand side at once.
-// Smoothing alternates between x and the level's scratch t; the first write
-// goes to t, and 2 nu - 1 sweeps later the result is in x.
-static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsigned mask, cudaStream_t st) {
+// Cycles on the level-(l+1) problem asked for by level l: gamma on the first
+// gamma_depth levels (W-like there), one below; the coarsest level is solved
+// (from zero) once.
+static int coarse_cycles(const MgHierarchy& H, int l) {
+  if (l + 1 == H.nlev - 1) return 1;
+  return l < H.gamma_depth ? H.gamma : 1;
+}
+
+// x = cycle(b) on level l >= 1 for every right-hand side at once, from x = 0,
+// or from the current x when warm.  Smoothing writes the level's scratch t,
+// the prolongation + post-smoothing pass writes x (one sweep each way).
+static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsigned mask, cudaStream_t st,
+                          bool warm = false) {
   const MgLevel& L = H.lv[l];
   const dim3 blk(32, 8), g = grid4(L, H.nrhs);
   const Vec4 b = vec4(L.b), x = vec4(L.x), t = vec4(L.t);
@@ -541,27 +550,17 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
     note_launch();
     return cudaGetLastError();
   }
-  Vec4 cur = t, oth = x;
-  k_mg_smooth4<<<g, blk, 0, st>>>(L, cur, b, cur, H.omega, 1, S, mask);
+  k_mg_smooth4<<<g, blk, 0, st>>>(L, warm ? x : t, b, t, H.omega, warm ? 0 : 1, S, mask);
   note_launch();
-  for (int s = 1; s < H.nu; s++) {
-    k_mg_smooth4<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
-    note_launch();
-    std::swap(cur, oth);
-  }
   const MgLevel& C = H.lv[l + 1];
-  k_mg_resrestrict4<<<grid4r(C, H.nrhs), blk, 0, st>>>(L, C, cur, b, vec4(C.b), H.cscale, S, mask);
+  k_mg_resrestrict4<<<grid4r(C, H.nrhs), blk, 0, st>>>(L, C, t, b, vec4(C.b), H.cscale, S, mask);
   note_launch();
-  cudaError_t e = vcycle(H, l + 1, S, mask, st);
-  if (e != cudaSuccess) return e;
-  k_mg_prolong_smooth4<<<g, blk, 0, st>>>(L, C, cur, vec4(C.x), b, oth, H.omega, S, mask);
-  note_launch();
-  std::swap(cur, oth);
-  for (int s = 1; s < H.nu; s++) {
-    k_mg_smooth4<<<g, blk, 0, st>>>(L, cur, b, oth, H.omega, 0, S, mask);
-    note_launch();
-    std::swap(cur, oth);
+  for (int c = 0; c < coarse_cycles(H, l); c++) {
+    cudaError_t e = vcycle(H, l + 1, S, mask, st, c > 0);
+    if (e != cudaSuccess) return e;
   }
+  k_mg_prolong_smooth4<<<g, blk, 0, st>>>(L, C, t, vec4(C.x), b, x, H.omega, S, mask);
+  note_launch();
   return cudaGetLastError();
 }
 
@@ -950,8 +949,10 @@ static cudaError_t level0_tail(const MgHierarchy& H, MgVecs& v, MgScalars* S, co
   k_mg0_tma<kResidual><<<gt, kTThreads, tma_smem(kResidual), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.cscale,
                                                                    S, rb, mask, start);
   note_launch();
-  cudaError_t e = vcycle(H, 1, S, mask, st);
-  if (e != cudaSuccess) return e;
+  for (int cy = 0; cy < coarse_cycles(H, 0); cy++) {
+    cudaError_t e = vcycle(H, 1, S, mask, st, cy > 0);
+    if (e != cudaSuccess) return e;
+  }
   k_mg0_tma<kSmooth><<<gt, kTThreads, tma_smem(kSmooth), st>>>(H.maps, H.g0, H.kc0, L, C, ops0(H), v, H.cscale, S,
                                                                  rb, mask, start);
   note_launch();
