@@ -399,6 +399,27 @@ __device__ __forceinline__ X4 load_x4(const MgLevel& L, const float* __restrict_
   v.r = 4 * g + 4 < L.nx ? __ldg(x + c + 4) : 0.f;
   return v;
 }
+// The first smoothing sweep from zero, t = omega dinv b, at the group and
+// its neighbours (the layout of load_x4), for passes that rebuild t instead
+// of reading it.
+__device__ __forceinline__ X4 load_t4(const MgLevel& L, const float* __restrict__ b, float omega, int g, int j,
+                                      int k, long long c) {
+  auto t4 = [&](long long o) {
+    const float4 bb = ld4(b + o), dv = ld4(L.dinv + o);
+    return make_float4(omega * dv.x * bb.x, omega * dv.y * bb.y, omega * dv.z * bb.z, omega * dv.w * bb.w);
+  };
+  auto t1 = [&](long long o) { return omega * __ldg(L.dinv + o) * __ldg(b + o); };
+  X4 v;
+  v.c = t4(c);
+  v.s = j > 0 ? t4(c - L.sy) : zero4();
+  v.n = j + 1 < L.ny ? t4(c + L.sy) : zero4();
+  v.b = k > 0 ? t4(c - L.sz) : zero4();
+  v.t = k + 1 < L.nz ? t4(c + L.sz) : zero4();
+  v.l = g > 0 ? t1(c - 1) : 0.f;
+  v.r = 4 * g + 4 < L.nx ? t1(c + 4) : 0.f;
+  return v;
+}
+
 // A x for the group from its faces (stored transmissibilities).
 __device__ __forceinline__ float4 apply4(const MgLevel& L, const X4& X, int g, int j, int k, long long c) {
   const float4 te = ld4(L.te + c), tn = ld4(L.tn + c), tt = ld4(L.tt + c);
@@ -451,10 +472,13 @@ __global__ void __launch_bounds__(256) k_mg_smooth4(MgLevel L, Vec4 xv, Vec4 bv,
 
 // bc = scale x restriction of b - A x: a thread takes two coarse cells
 // (cg: 2cg, 2cg+1), i.e. fine group cg on the aggregate's two rows and two
-// planes.  scale > 1 over-corrects with the coarse solution (the cycle stays
-// linear and symmetric).
+// planes.  first: x is the first smoothing sweep from zero, rebuilt as
+// omega dinv b.  scale > 1 over-corrects with the coarse solution (the
+// cycle stays linear and symmetric).
+template <bool FIRST>
 __global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bcv,
-                                                         float scale, const MgScalars* S, unsigned mask) {
+                                                         float scale, const MgScalars* S, unsigned mask,
+                                                         float omega) {
   MG_RHS(C);
   MG_SKIP(mrhs);
   const float* __restrict__ x = pick(xv.p, mrhs);
@@ -469,7 +493,7 @@ __global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, V
           const int j = 2 * cj + (o & 1), k = 2 * ck + (o >> 1);
           if (j < F.ny && k < F.nz) {
             const long long c = ix(F, 4 * cg, j, k);
-            const X4 X = load_x4(F, x, cg, j, k, c);
+            const X4 X = FIRST ? load_t4(F, b, omega, cg, j, k, c) : load_x4(F, x, cg, j, k, c);
             const float4 u = apply4(F, X, cg, j, k, c), bb = ld4(b + c);
             s0 += (bb.x - u.x) + (bb.y - u.y);
             s1 += (bb.z - u.z) + (bb.w - u.w);
@@ -483,9 +507,11 @@ __global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, V
 
 // xo = y + omega dinv (b - A y) with y = x + P xc (the prolonged correction is
 // added on the fly, also at the neighbours): prolongation and the first
-// post-smoothing sweep in one pass.  Fine cells 4g .. 4g+3 have the coarse
+// post-smoothing sweep in one pass (first: x rebuilt as omega dinv b, as in
+// k_mg_resrestrict4).  Fine cells 4g .. 4g+3 have the coarse
 // parents 2g, 2g, 2g+1, 2g+1 (a float2 of the coarse row: 2g is even and
 // the row starts on 16 bytes).
+template <bool FIRST>
 __global__ void __launch_bounds__(256, 3) k_mg_prolong_smooth4(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv,
                                                             Vec4 xov, float omega, const MgScalars* S,
                                                             unsigned mask) {
@@ -507,7 +533,7 @@ __global__ void __launch_bounds__(256, 3) k_mg_prolong_smooth4(MgLevel F, MgLeve
   };
   MG4_CELLS(F) {
     const long long c = ix(F, 4 * g, j, k);
-    X4 X = load_x4(F, x, g, j, k, c);
+    X4 X = FIRST ? load_t4(F, b, omega, g, j, k, c) : load_x4(F, x, g, j, k, c);
     add(X.c, par(g, j, k));
     if (j > 0) add(X.s, par(g, j - 1, k));
     if (j + 1 < F.ny) add(X.n, par(g, j + 1, k));
@@ -538,8 +564,8 @@ static int coarse_cycles(const MgHierarchy& H, int l) {
 }
 
 // x = cycle(b) on level l >= 1 for every right-hand side at once, from x = 0,
-// or from the current x when warm.  Smoothing writes the level's scratch t,
-// the prolongation + post-smoothing pass writes x (one sweep each way).
+// or from the current x when warm (one smoothing sweep each way; the
+// prolongation + post-smoothing pass writes x).
 static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsigned mask, cudaStream_t st,
                           bool warm = false) {
   const MgLevel& L = H.lv[l];
@@ -550,16 +576,26 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
     note_launch();
     return cudaGetLastError();
   }
-  k_mg_smooth4<<<g, blk, 0, st>>>(L, warm ? x : t, b, t, H.omega, warm ? 0 : 1, S, mask);
-  note_launch();
+  // cold cycles rebuild the first sweep (t = omega dinv b) inside the next
+  // two passes; warm ones smooth from x into t
+  if (warm) {
+    k_mg_smooth4<<<g, blk, 0, st>>>(L, x, b, t, H.omega, 0, S, mask);
+    note_launch();
+  }
   const MgLevel& C = H.lv[l + 1];
-  k_mg_resrestrict4<<<grid4r(C, H.nrhs), blk, 0, st>>>(L, C, t, b, vec4(C.b), H.cscale, S, mask);
+  if (warm)
+    k_mg_resrestrict4<false><<<grid4r(C, H.nrhs), blk, 0, st>>>(L, C, t, b, vec4(C.b), H.cscale, S, mask, H.omega);
+  else
+    k_mg_resrestrict4<true><<<grid4r(C, H.nrhs), blk, 0, st>>>(L, C, t, b, vec4(C.b), H.cscale, S, mask, H.omega);
   note_launch();
   for (int c = 0; c < coarse_cycles(H, l); c++) {
     cudaError_t e = vcycle(H, l + 1, S, mask, st, c > 0);
     if (e != cudaSuccess) return e;
   }
-  k_mg_prolong_smooth4<<<g, blk, 0, st>>>(L, C, t, vec4(C.x), b, x, H.omega, S, mask);
+  if (warm)
+    k_mg_prolong_smooth4<false><<<g, blk, 0, st>>>(L, C, t, vec4(C.x), b, x, H.omega, S, mask);
+  else
+    k_mg_prolong_smooth4<true><<<g, blk, 0, st>>>(L, C, t, vec4(C.x), b, x, H.omega, S, mask);
   note_launch();
   return cudaGetLastError();
 }
