@@ -434,17 +434,31 @@ static void df_choose(JacobiDfPlan& pl, cudaStream_t st) {
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
     float best_ms = 1e30f;
+    int sms = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     for (int s = 0; s < jacobi_df_num_shapes(); s++) {
-      const int cands[5] = {default_kchunk(d, s), 8, 16, 32, 64};
-      for (int c = 0; c < 5; c++) {
-        const int kc = cands[c];
-        if (kc > d.nz || (c > 0 && kc == cands[0])) continue;
+      // planes per CTA: the default, fixed lengths, and lengths that make the
+      // CTA count a whole number (2..8) of waves at this shape's occupancy
+      std::vector<int> cands = {default_kchunk(d, s), 8, 16, 32, 64};
+      int tx, ty;
+      jacobi_df_shape(s, &tx, &ty);
+      const long long tiles = (long long)((d.nx + tx - 1) / tx) * ((d.ny + ty - 1) / ty);
+      const long long slots = (long long)sms * jacobi_df_ctas_per_sm(s);
+      for (int w = 2; w <= 8; w++) {
+        const long long nch = w * slots / tiles;
+        if (nch < 1 || nch > d.nz) continue;
+        cands.push_back((int)((d.nz + nch - 1) / nch));
+      }
+      std::sort(cands.begin(), cands.end());
+      cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+      for (const int kc : cands) {
+        if (kc < 2 || kc > d.nz) continue;
         pl.shape = s;
         pl.kchunk = kc;
         CUDA_TRY(jacobi_df_encode(pl));
         CUDA_TRY(jacobi_df_sweep(pl, pl.a, pl.b, st));
         CUDA_TRY(cudaEventRecord(e0, st));
-        for (int r = 0; r < 3; r++) CUDA_TRY(jacobi_df_sweep(pl, pl.a, pl.b, st));
+        for (int r = 0; r < 5; r++) CUDA_TRY(jacobi_df_sweep(pl, pl.a, pl.b, st));
         CUDA_TRY(cudaEventRecord(e1, st));
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;

@@ -99,6 +99,7 @@ struct JacobiDfPlan {
   CUtensorMap tm_a, tm_b, tm_sr;
 };
 int jacobi_df_num_shapes();
+int jacobi_df_ctas_per_sm(int shape);
 cudaError_t jacobi_df_pack(JacobiDfPlan& pl, const double* phi, const double* src, const double* rdiag,
                            const double* coef64, cudaStream_t st);
 cudaError_t jacobi_df_encode(JacobiDfPlan& pl);

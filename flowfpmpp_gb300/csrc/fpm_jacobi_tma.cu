@@ -309,6 +309,32 @@ cudaError_t jacobi_df_sweep(const JacobiDfPlan& pl, const float2* src_phi, float
 
 int jacobi_df_num_shapes() { return kNumShapes; }
 
+// Resident CTAs per SM of a tile shape's sweep kernel (shared memory and
+// registers), for wave-aligned chunk choices.
+template <int TX, int TYB, int CY>
+static int shape_occupancy() {
+  const size_t smem = shape_smem<TX, TYB, CY>();
+  if (cudaFuncSetAttribute(k_jacobi_df_tma<TX, TYB, CY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_jacobi_df_tma<TX, TYB, CY>, TX * TYB, smem) != cudaSuccess)
+    return 1;
+  return n < 1 ? 1 : n;
+}
+int jacobi_df_ctas_per_sm(int shape) {
+  switch (shape) {
+    case 0: return shape_occupancy<64, 4, 2>();
+    case 1: return shape_occupancy<32, 8, 2>();
+    case 2: return shape_occupancy<64, 2, 4>();
+    case 3: return shape_occupancy<32, 4, 4>();
+    case 4: return shape_occupancy<128, 2, 2>();
+    case 5: return shape_occupancy<64, 4, 1>();
+    case 6: return shape_occupancy<32, 8, 1>();
+    default: return shape_occupancy<64, 8, 1>();
+  }
+}
+
 // Packs FP64 phi / src / rdiag / coefficients into the internal double-float
 // arrays.  a/b/sr/coef/err are allocated by the caller: a and b hold
 // px*(ny+2)*nz float2, sr nx*ny*nz float4, coef 2(nx+ny+nz) float2.
