@@ -784,7 +784,6 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   MgHierarchy H;
   std::memset(&H, 0, sizeof(H));
   H.nrhs = nrhs;
-  H.nu = (int)env_double("FPM_MG_NU", 1);
   // Two cycles on the level-1 problem per level-0 cycle where level 1 is
   // large enough for the extra launches to pay (three potentials on
   // 384 x 384 x 192: 20 % fewer iterations, 12 % less time); small grids are
@@ -846,7 +845,6 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     throw Error{FPM_E_LIMIT, "grid too small or too large for the multigrid hierarchy"};
   if ((d.ny + 3) / 4 > 65535 || (long long)((d.nz + H.g0.kc - 1) / H.g0.kc) * nrhs > 65535)
     throw Error{FPM_E_LIMIT, "grid too large for the multigrid launch geometry"};
-  if (H.nu != 1) throw Error{FPM_E_ARG, "the multigrid cycle uses one smoothing sweep on level 0"};
   const long long fb_size = H.pxb * (d.ny + 2) * (long long)d.nz;
   H.fb0 = A.get<uint8_t>(fb_size);
   CUDA_TRY(cudaMemsetAsync(H.fb0, 0, fb_size, st));

@@ -277,7 +277,7 @@ struct MgHierarchy {
   float *aex, *dxr;   // row layout (index 3 + i, i 1-based), zero outside
   float *dy, *ayn;    // index j - 1
   float *dz, *azt;    // index k - 1
-  int nu;             // pre- and post-smoothing sweeps (one)
+  // one weighted-Jacobi sweep before and one after each coarse correction
   int gamma;          // cycles on the next coarser problem for the levels l < gamma_depth (1: V-cycle)
   int gamma_depth;
   int coarse_sweeps;  // Jacobi sweeps on the coarsest level (one block per right-hand side)

@@ -448,8 +448,9 @@ __device__ __forceinline__ float4 smooth_out(const MgLevel& L, int g, const floa
   return make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// xo = (first ? 0 : x) + omega dinv (b - A x)   (first: x is taken as 0)
-__global__ void __launch_bounds__(256) k_mg_smooth4(MgLevel L, Vec4 xv, Vec4 bv, Vec4 xov, float omega, int first,
+// xo = x + omega dinv (b - A x): the smoothing sweep of a warm cycle (cold
+// cycles fold their sweep from zero into the next two passes)
+__global__ void __launch_bounds__(256) k_mg_smooth4(MgLevel L, Vec4 xv, Vec4 bv, Vec4 xov, float omega,
                                                     const MgScalars* S, unsigned mask) {
   MG_RHS(L);
   MG_SKIP(mrhs);
@@ -459,14 +460,8 @@ __global__ void __launch_bounds__(256) k_mg_smooth4(MgLevel L, Vec4 xv, Vec4 bv,
   MG4_CELLS(L) {
     const long long c = ix(L, 4 * g, j, k);
     const float4 dv = ld4(L.dinv + c), bb = ld4(b + c);
-    float4 o;
-    if (first) {
-      o = smooth_out(L, g, zero4(), dv, bb, zero4(), omega);
-    } else {
-      const X4 X = load_x4(L, x, g, j, k, c);
-      o = smooth_out(L, g, X.c, dv, bb, apply4(L, X, g, j, k, c), omega);
-    }
-    st4(xo + c, o);
+    const X4 X = load_x4(L, x, g, j, k, c);
+    st4(xo + c, smooth_out(L, g, X.c, dv, bb, apply4(L, X, g, j, k, c), omega));
   }
 }
 
@@ -579,7 +574,7 @@ static cudaError_t vcycle(const MgHierarchy& H, int l, const MgScalars* S, unsig
   // cold cycles rebuild the first sweep (t = omega dinv b) inside the next
   // two passes; warm ones smooth from x into t
   if (warm) {
-    k_mg_smooth4<<<g, blk, 0, st>>>(L, x, b, t, H.omega, 0, S, mask);
+    k_mg_smooth4<<<g, blk, 0, st>>>(L, x, b, t, H.omega, S, mask);
     note_launch();
   }
   const MgLevel& C = H.lv[l + 1];
