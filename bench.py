@@ -419,21 +419,9 @@ def main():
         if rank == 0:
             run_frames(args) if args.workload == "foil_frames" else run_pcg(args)
         return
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    from flowfpmpp_gb300.replicas import Replicas
+    reps = Replicas(world=world, rank=rank)  # replicas only: no collective on the data path
+    barrier, max_over_ranks = reps.barrier, reps.max
 
     from flowfpmpp_gb300 import build as fbuild
     fbuild.build()
@@ -524,8 +512,7 @@ def main():
     for x in [p0] + [x[1] for x in h_in]:
         lib.fpm_host_free(ctypes.c_void_p(x))
 
-    if dist is not None:
-        dist.destroy_process_group()
+    reps.close()
     if rank != 0:
         return
     peaks = {}
