@@ -767,7 +767,7 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
 // FP64 and recomputes the true residual; convergence is the reference's
 // max-norm test.  All right-hand sides iterate in the same launches; each
 // has its own outer steps.
-constexpr double kMgDrop = 1e-4;
+static const double kMgDrop = env_double("FPM_MG_DROP", 1e-4);
 constexpr int kMgInnerMax = 400;
 
 static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
