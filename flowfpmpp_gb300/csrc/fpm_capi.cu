@@ -173,7 +173,7 @@ struct TimedRun {
 
 // ---------------------------------------------------------------- options
 // FPM_VERBOSE=1 prints one line per convergence check of every solver loop
-// to stderr.  FPM_PCG_STALL_CHECKS overrides the number of checks without a
+// to stderr; FPM_VERBOSE=2 adds the Jacobi autotuner's timings.  FPM_PCG_STALL_CHECKS overrides the number of checks without a
 // 1% improvement after which PCG stops (50, src/fpm_stairstep_mpi_3d.f90:288).
 static int verbose_level() {
   static int v = -1;
@@ -463,6 +463,9 @@ static void df_choose(JacobiDfPlan& pl, cudaStream_t st) {
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
         CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (verbose_level() >= 2)
+          std::fprintf(stderr, "fpm df autotune: shape %d tile %dx%d planes %d: %.1f us per sweep\n", s, tx, ty, kc,
+                       200.f * ms);
         if (ms < best_ms) {
           best_ms = ms;
           best = DfChoice{s, kc};

@@ -24,8 +24,6 @@ namespace fpm {
 
 namespace {
 
-constexpr int kPhiStages = 4;
-constexpr int kSrStages = 3;
 using tma::mbar_expect_tx;
 using tma::mbar_init;
 using tma::mbar_wait;
@@ -79,11 +77,128 @@ __device__ __forceinline__ float2 df_jacobi_finish(float2 a, float2 rd, float2 s
   return make_float2(h, e - (h - u));
 }
 
+// Packed FP32x2 form of the same arithmetic for two cells at once (lane 0 and
+// lane 1 are two rows of one column).  Each packed instruction rounds every
+// lane like its scalar FP32 counterpart, so a lane computes exactly what the
+// scalar TwoProd / TwoSum sequence computes without FMA contraction.  The
+// product error is carried negated (fma with -c against +p), which avoids a
+// separate negation of p and leaves every rounding unchanged.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+// A double-float coefficient pair: high parts, and both parts negated.
+struct DfCoef2 {
+  float2 h, nh, nl;
+};
+__device__ __forceinline__ DfCoef2 coef2(float2 c0, float2 c1) {
+  return DfCoef2{make_float2(c0.x, c1.x), make_float2(-c0.x, -c1.x), make_float2(-c0.y, -c1.y)};
+}
+struct DfAcc2 {
+  float2 s, e;
+};
+// A += c * a for lane-wise double-float c and a = (ah, al).
+__device__ __forceinline__ void acc_prod2(DfAcc2& A, const DfCoef2& c, float2 ah, float2 al) {
+  const float2 p = __fmul2_rn(c.h, ah);
+  float2 npe = __ffma2_rn(c.nh, ah, p);
+  npe = __ffma2_rn(c.nh, al, npe);
+  npe = __ffma2_rn(c.nl, ah, npe);
+  const float2 s = add2(A.s, p);
+  const float2 bb = sub2(s, A.s);
+  const float2 t = add2(sub2(A.s, sub2(s, bb)), sub2(p, bb));
+  A.s = s;
+  A.e = add2(A.e, sub2(t, npe));
+}
+// b = 0.2 a + rd * s, lane-wise; returns (hi, lo) pairs in *bh, *bl.
+__device__ __forceinline__ void df_jacobi_finish2(float2 ah, float2 al, float2 rdh, float2 rdl, const DfAcc2& A,
+                                                  float2* bh, float2* bl) {
+  const float2 P2 = DF_POINT2;
+  const float2 sh = add2(A.s, A.e);
+  const float2 sl = sub2(A.e, sub2(sh, A.s));
+  const float2 p = __fmul2_rn(make_float2(P2.x, P2.x), ah);
+  float2 npe = __ffma2_rn(make_float2(-P2.x, -P2.x), ah, p);
+  npe = __ffma2_rn(make_float2(-P2.x, -P2.x), al, npe);
+  npe = __ffma2_rn(make_float2(-P2.y, -P2.y), ah, npe);
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 q = __fmul2_rn(rdh, sh);
+  float2 nqe = __ffma2_rn(__fmul2_rn(rdh, m1), sh, q);
+  nqe = __ffma2_rn(__fmul2_rn(rdh, m1), sl, nqe);
+  nqe = __ffma2_rn(__fmul2_rn(rdl, m1), sh, nqe);
+  const float2 u = add2(p, q);
+  const float2 bb = sub2(u, p);
+  const float2 t = add2(sub2(p, sub2(u, bb)), sub2(q, bb));
+  const float2 e = sub2(t, add2(npe, nqe));
+  const float2 h = add2(u, e);
+  *bh = h;
+  *bl = sub2(e, sub2(h, u));
+}
+
+// One plane of a thread's column: rows jbase + r*TYB (r < CY) of column i,
+// from the phi planes k-1 (pm), k (pc), k+1 (pp) and the (src, rdiag) plane in
+// shared memory; writes phi' at outp + px * r*TYB.
+template <int TX, int TYB, int CY>
+__device__ __forceinline__ void df_plane(const float2* pm, const float2* pc, const float2* pp, const float4* srp,
+                                         float2* outp, long long px, int tx, int tyb, int jbase, int ny, float2 cwi,
+                                         float2 cei, const float2 (&csj)[CY], const float2 (&cnj)[CY], float2 cbk,
+                                         float2 ctk) {
+  constexpr int PW = TX + 2;
+  if constexpr (CY % 2 == 0) {
+    // Rows r and r+1 of the column share one packed computation.
+    const DfCoef2 CW = coef2(cwi, cwi), CE = coef2(cei, cei), CB = coef2(cbk, cbk), CT = coef2(ctk, ctk);
+#pragma unroll
+    for (int r = 0; r < CY; r += 2) {
+      const int j = jbase + r * TYB;
+      if (j <= ny) {
+        const int c0 = (tx + 1) + PW * (tyb + r * TYB + 1), c1 = c0 + PW * TYB;
+        const float4 s0 = srp[tx + TX * (tyb + r * TYB)], s1 = srp[tx + TX * (tyb + (r + 1) * TYB)];
+        const float2 a0 = pc[c0], a1 = pc[c1];
+        DfAcc2 A{make_float2(s0.x, s1.x), make_float2(s0.y, s1.y)};
+        float2 v0 = pc[c0 - 1], v1 = pc[c1 - 1];
+        acc_prod2(A, CW, make_float2(v0.x, v1.x), make_float2(v0.y, v1.y));
+        v0 = pc[c0 + 1], v1 = pc[c1 + 1];
+        acc_prod2(A, CE, make_float2(v0.x, v1.x), make_float2(v0.y, v1.y));
+        v0 = pc[c0 - PW], v1 = pc[c1 - PW];
+        acc_prod2(A, coef2(csj[r], csj[r + 1]), make_float2(v0.x, v1.x), make_float2(v0.y, v1.y));
+        v0 = pc[c0 + PW], v1 = pc[c1 + PW];
+        acc_prod2(A, coef2(cnj[r], cnj[r + 1]), make_float2(v0.x, v1.x), make_float2(v0.y, v1.y));
+        v0 = pm[c0], v1 = pm[c1];
+        acc_prod2(A, CB, make_float2(v0.x, v1.x), make_float2(v0.y, v1.y));
+        v0 = pp[c0], v1 = pp[c1];
+        acc_prod2(A, CT, make_float2(v0.x, v1.x), make_float2(v0.y, v1.y));
+        float2 bh, bl;
+        df_jacobi_finish2(make_float2(a0.x, a1.x), make_float2(a0.y, a1.y), make_float2(s0.z, s1.z),
+                          make_float2(s0.w, s1.w), A, &bh, &bl);
+        outp[px * (r * TYB)] = make_float2(bh.x, bl.x);
+        if (j + TYB <= ny) outp[px * ((r + 1) * TYB)] = make_float2(bh.y, bl.y);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < CY; r++) {
+      const int j = jbase + r * TYB;
+      if (j <= ny) {
+        const int c0 = (tx + 1) + PW * (tyb + r * TYB + 1);
+        const float4 sr = srp[tx + TX * (tyb + r * TYB)];
+        const float2 ac = pc[c0];
+        DfAcc A{sr.x, sr.y};
+        acc_prod(A, cwi, pc[c0 - 1]);
+        acc_prod(A, cei, pc[c0 + 1]);
+        acc_prod(A, csj[r], pc[c0 - PW]);
+        acc_prod(A, cnj[r], pc[c0 + PW]);
+        acc_prod(A, cbk, pm[c0]);
+        acc_prod(A, ctk, pp[c0]);
+        outp[px * (r * TYB)] = df_jacobi_finish(ac, make_float2(sr.z, sr.w), acc_norm(A));
+      }
+    }
+  }
+}
+
 // One CTA: TX x (TYB*CY) interior cells; thread (tx, tyb) owns rows
 // tyb + r*TYB (r < CY) of its column, so a warp reads contiguous rows of the
-// shared-memory plane.
-template <int TX, int TYB, int CY>
-__global__ void __launch_bounds__(TX* TYB, 2) k_jacobi_df_tma(const __grid_constant__ CUtensorMap tm_phi,
+// shared-memory plane.  kPhiStages / kSrStages are the ring depths: planes in
+// flight ahead of the compute are kPhiStages - 2 of phi and kSrStages - 1 of
+// (src, rdiag).
+template <int TX, int TYB, int CY, int kPhiStages, int kSrStages>
+__global__ void __launch_bounds__(TX* TYB, 1024 / (TX * TYB)) k_jacobi_df_tma(const __grid_constant__ CUtensorMap tm_phi,
                                                              const __grid_constant__ CUtensorMap tm_sr,
                                                              float2* __restrict__ out,
                                                              const float2* __restrict__ coef, int nx, int ny, int nz,
@@ -109,8 +224,9 @@ __global__ void __launch_bounds__(TX* TYB, 2) k_jacobi_df_tma(const __grid_const
   }
   __syncthreads();
 
-  // Plane p of phi goes to ring slot (p - (k0-1)) % 4; its n-th use of the
-  // slot completes phase n.  (src, rdiag) plane p goes to slot (p - k0) % 3.
+  // Plane p of phi goes to ring slot (p - (k0-1)) % kPhiStages; its n-th use
+  // of the slot completes phase n.  (src, rdiag) plane p goes to slot
+  // (p - k0) % kSrStages.
   auto issue_phi = [&](int p) {
     const int u = p - (k0 - 1), s = u % kPhiStages;
     const uint32_t bar = bar_base + 8 * s;
@@ -134,8 +250,8 @@ __global__ void __launch_bounds__(TX* TYB, 2) k_jacobi_df_tma(const __grid_const
 
   int next_phi = k0 - 1, next_sr = k0;
   if (tid == 0) {
-    for (; next_phi <= k0 + 2 && next_phi <= k1 + 1; next_phi++) issue_phi(next_phi);
-    for (; next_sr <= k0 + 2 && next_sr <= k1; next_sr++) issue_sr(next_sr);
+    for (; next_phi <= k0 + kPhiStages - 2 && next_phi <= k1 + 1; next_phi++) issue_phi(next_phi);
+    for (; next_sr <= k0 + kSrStages - 1 && next_sr <= k1; next_sr++) issue_sr(next_sr);
   }
 
   const bool col = i <= nx;
@@ -169,24 +285,7 @@ __global__ void __launch_bounds__(TX* TYB, 2) k_jacobi_df_tma(const __grid_const
       const float4* srp = sr_s + ((k - k0) % kSrStages) * (TX * TY);
       // z neighbours clamp at the domain ends like a(i,j,max(k-1,1)); there
       // cb(1) = ct(nz) = 0, so reading the zero-filled plane gives the same sum.
-      const float2 cbk = cb[k - 1], ctk = ct[k - 1];
-#pragma unroll
-      for (int r = 0; r < CY; r++) {
-        const int j = jbase + r * TYB;
-        if (j <= ny) {
-          const int c0 = (tx + 1) + PW * (tyb + r * TYB + 1);
-          const float4 sr = srp[tx + TX * (tyb + r * TYB)];
-          const float2 ac = pc[c0];
-          DfAcc A{sr.x, sr.y};
-          acc_prod(A, cwi, pc[c0 - 1]);
-          acc_prod(A, cei, pc[c0 + 1]);
-          acc_prod(A, csj[r], pc[c0 - PW]);
-          acc_prod(A, cnj[r], pc[c0 + PW]);
-          acc_prod(A, cbk, pm[c0]);
-          acc_prod(A, ctk, pp[c0]);
-          outp[px * (r * TYB)] = df_jacobi_finish(ac, make_float2(sr.z, sr.w), acc_norm(A));
-        }
-      }
+      df_plane<TX, TYB, CY>(pm, pc, pp, srp, outp, px, tx, tyb, jbase, ny, cwi, cei, csj, cnj, cb[k - 1], ct[k - 1]);
     }
     outp += plane;
     if (__syncthreads_or(!ok)) {
@@ -262,77 +361,89 @@ static bool encode_3d(CUtensorMap* map, void* base, uint64_t d0, uint64_t d1, ui
   return tma_encode_3d(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, base, d0, d1, d2, stride1_bytes, stride2_bytes, b0, b1);
 }
 
+// Tile shapes the autotuner chooses from: (id, TX, TYB, CY, phi ring depth,
+// (src, rdiag) ring depth).
+#define FPM_DF_SHAPES(X)  \
+  X(0, 64, 4, 2, 4, 3)    \
+  X(1, 32, 8, 2, 4, 3)    \
+  X(2, 64, 2, 4, 4, 3)    \
+  X(3, 32, 4, 4, 4, 3)    \
+  X(4, 128, 2, 2, 4, 3)   \
+  X(5, 64, 4, 1, 4, 3)    \
+  X(6, 32, 8, 1, 4, 3)    \
+  X(7, 64, 8, 1, 4, 3)    \
+  X(8, 32, 4, 2, 4, 3)    \
+  X(9, 64, 2, 2, 4, 3)    \
+  X(10, 32, 2, 4, 4, 3)
+
 struct TileShape {
   int tx, tyb, cy;  // tile = tx x (tyb*cy); threads = tx*tyb
 };
-static const TileShape kShapes[] = {{64, 4, 2}, {32, 8, 2}, {64, 2, 4}, {32, 4, 4}, {128, 2, 2},
-                                    {64, 4, 1}, {32, 8, 1}, {64, 8, 1}};
+#define FPM_DF_SHAPE_ROW(id, tx, tyb, cy, ps, ss) {tx, tyb, cy},
+static const TileShape kShapes[] = {FPM_DF_SHAPES(FPM_DF_SHAPE_ROW)};
+#undef FPM_DF_SHAPE_ROW
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <int TX, int TYB, int CY>
+template <int TX, int TYB, int CY, int PS, int SS>
 static size_t shape_smem() {
   constexpr size_t ty = TYB * CY;
   constexpr size_t phi = ((TX + 2) * (ty + 2) * 8 + 127) / 128 * 128;
-  return kPhiStages * phi + kSrStages * (size_t)TX * ty * 16 + (kPhiStages + kSrStages) * 8;
+  return PS * phi + SS * (size_t)TX * ty * 16 + (PS + SS) * 8;
 }
 
-template <int TX, int TYB, int CY>
+// Resident CTAs per SM of a tile shape's sweep kernel (shared memory and
+// registers), for wave-aligned chunk choices.
+template <int TX, int TYB, int CY, int PS, int SS>
+static int shape_occupancy() {
+  const size_t smem = shape_smem<TX, TYB, CY, PS, SS>();
+  if (cudaFuncSetAttribute(k_jacobi_df_tma<TX, TYB, CY, PS, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_jacobi_df_tma<TX, TYB, CY, PS, SS>, TX * TYB, smem) !=
+      cudaSuccess)
+    return 1;
+  return n < 1 ? 1 : n;
+}
+
+template <int TX, int TYB, int CY, int PS, int SS>
 static cudaError_t launch_shape(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st) {
   const CUtensorMap& tm = (src_phi == pl.a) ? pl.tm_a : pl.tm_b;
-  const size_t smem = shape_smem<TX, TYB, CY>();
+  const size_t smem = shape_smem<TX, TYB, CY, PS, SS>();
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_jacobi_df_tma<TX, TYB, CY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_jacobi_df_tma<TX, TYB, CY, PS, SS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   constexpr int TY = TYB * CY;
   dim3 grid((pl.nx + TX - 1) / TX, (pl.ny + TY - 1) / TY, (pl.nz + pl.kchunk - 1) / pl.kchunk);
-  k_jacobi_df_tma<TX, TYB, CY><<<grid, TX * TYB, smem, st>>>(tm, pl.tm_sr, dst_phi, pl.coef, pl.nx, pl.ny, pl.nz,
-                                                             pl.px, pl.kchunk, pl.err); note_launch();
+  k_jacobi_df_tma<TX, TYB, CY, PS, SS><<<grid, TX * TYB, smem, st>>>(tm, pl.tm_sr, dst_phi, pl.coef, pl.nx, pl.ny,
+                                                                     pl.nz, pl.px, pl.kchunk, pl.err); note_launch();
   return cudaGetLastError();
 }
 
 cudaError_t jacobi_df_sweep(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st) {
+#define FPM_DF_LAUNCH(id, tx, tyb, cy, ps, ss) \
+  case id: return launch_shape<tx, tyb, cy, ps, ss>(pl, src_phi, dst_phi, st);
   switch (pl.shape) {
-    case 0: return launch_shape<64, 4, 2>(pl, src_phi, dst_phi, st);
-    case 1: return launch_shape<32, 8, 2>(pl, src_phi, dst_phi, st);
-    case 2: return launch_shape<64, 2, 4>(pl, src_phi, dst_phi, st);
-    case 3: return launch_shape<32, 4, 4>(pl, src_phi, dst_phi, st);
-    case 4: return launch_shape<128, 2, 2>(pl, src_phi, dst_phi, st);
-    case 5: return launch_shape<64, 4, 1>(pl, src_phi, dst_phi, st);
-    case 6: return launch_shape<32, 8, 1>(pl, src_phi, dst_phi, st);
-    default: return launch_shape<64, 8, 1>(pl, src_phi, dst_phi, st);
+    FPM_DF_SHAPES(FPM_DF_LAUNCH)
+    default: return cudaErrorInvalidValue;
   }
+#undef FPM_DF_LAUNCH
 }
 
 int jacobi_df_num_shapes() { return kNumShapes; }
 
-// Resident CTAs per SM of a tile shape's sweep kernel (shared memory and
-// registers), for wave-aligned chunk choices.
-template <int TX, int TYB, int CY>
-static int shape_occupancy() {
-  const size_t smem = shape_smem<TX, TYB, CY>();
-  if (cudaFuncSetAttribute(k_jacobi_df_tma<TX, TYB, CY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_jacobi_df_tma<TX, TYB, CY>, TX * TYB, smem) != cudaSuccess)
-    return 1;
-  return n < 1 ? 1 : n;
-}
 int jacobi_df_ctas_per_sm(int shape) {
+#define FPM_DF_OCC(id, tx, tyb, cy, ps, ss) \
+  case id: return shape_occupancy<tx, tyb, cy, ps, ss>();
   switch (shape) {
-    case 0: return shape_occupancy<64, 4, 2>();
-    case 1: return shape_occupancy<32, 8, 2>();
-    case 2: return shape_occupancy<64, 2, 4>();
-    case 3: return shape_occupancy<32, 4, 4>();
-    case 4: return shape_occupancy<128, 2, 2>();
-    case 5: return shape_occupancy<64, 4, 1>();
-    case 6: return shape_occupancy<32, 8, 1>();
-    default: return shape_occupancy<64, 8, 1>();
+    FPM_DF_SHAPES(FPM_DF_OCC)
+    default: return 1;
   }
+#undef FPM_DF_OCC
 }
 
 // Packs FP64 phi / src / rdiag / coefficients into the internal double-float

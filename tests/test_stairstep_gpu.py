@@ -203,7 +203,7 @@ def test_errors_mirror_reference_error_stops(gpu_lib):
     assert e.value.code == 3
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("shape", range(11))
 @pytest.mark.parametrize("dims,kchunk", [((37, 29, 11), 3), ((130, 70, 20), 8)])
 def test_df_tma_tile_shapes_match_fp64(gpu_lib, monkeypatch, shape, dims, kchunk):
     """Every TMA tile shape and a ragged z-chunk, on grids that are not
