@@ -262,6 +262,21 @@ class ChunkGraphs {
     CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
     note_launches(it->second.launches);
   }
+  // Runs `launch_one` n times as a sum of power-of-two graphs, so chunks of
+  // any length reuse at most log2(n)+1 captured graphs.
+  template <class F>
+  void run_pow2(int n, cudaStream_t st, F&& launch_one) {
+    for (int p = 1 << 20; p >= 1; p >>= 1)
+      if (n & p) run(p, st, launch_one);
+  }
+  // Runs `launch_one` n times as repeats of one graph of `unit` iterations
+  // (plus power-of-two graphs for the remainder).
+  template <class F>
+  void run_units(int n, int unit, cudaStream_t st, F&& launch_one) {
+    if (unit < 1) unit = 1;
+    for (int i = 0; i < n / unit; i++) run(unit, st, launch_one);
+    run_pow2(n % unit, st, launch_one);
+  }
 
  private:
   static cudaStream_t capture_stream() {
@@ -769,9 +784,19 @@ static void mixed_solve(const Dims& d, int nrhs, double* const phi[], const doub
 // by kMgDrop^2 (or kMgInnerMax iterations), adds the correction to phi in
 // FP64 and recomputes the true residual; convergence is the reference's
 // max-norm test.  All right-hand sides iterate in the same launches; each
-// has its own outer steps.
+// has its own outer steps.  The host looks at the device scalars after each
+// chunk of iterations; a chunk runs until every live right-hand side is
+// predicted to have finished its inner solve (its previous inner count + 1;
+// for the first inner solve kMgFirstChunk, then doubling), so that on small
+// grids (cells x right-hand sides below kMgAdaptCells), where an iteration
+// costs little more than its launches, few iterations run after an inner
+// solve has converged on the device.  Larger grids run fixed chunks of
+// check_interval (at most 50) iterations.
 static const double kMgDrop = env_double("FPM_MG_DROP", 1e-4);
 constexpr int kMgInnerMax = 400;
+constexpr int kMgFirstChunk = 8;
+constexpr double kMgAdaptCells = 4194304.0;
+constexpr int kMgMinChunk = 2;
 
 static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double* const src[], const double* diag,
                      const double* rdiag, const int32_t* solid, const Axes& ax, const Coefs& c, double tol,
@@ -800,11 +825,28 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   // level 0 in the mixed solver's FP32 layout (zero halo), coarse levels
   // compact; the level-0 passes take an even number of planes per chunk (whole
   // aggregates)
-  H.g0 = mixed_grid(d.nx, d.ny, d.nz, mixed_kchunk() + (mixed_kchunk() & 1));
-  // planes per CTA of the level-0 TMA passes (three potentials on 384 x 384 x 192:
-  // 16 -> 0.726 s, 24 -> 0.716 s, 48 -> 0.715 s)
+  // Planes per CTA: the level-0 passes march kc planes per CTA, so on a small
+  // grid a long chunk leaves most SMs idle and the pass waits on one CTA's
+  // serial plane loads.  Each chunk length is the largest even value up to its
+  // default that still gives at least one CTA per SM (three potentials on a
+  // 64 x 64 x 32 sphere grid: TMA chunk 24 -> 6.2 ms, 4 -> 4.3 ms per solve).
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  auto fill_chunk = [&](int kc, long long ctas_per_chunk_row) {
+    kc = kc < 2 ? 2 : kc + (kc & 1);
+    while (kc > 2 && ctas_per_chunk_row * ((d.nz + kc - 1) / kc) < sms) kc -= 2;
+    return kc;
+  };
+  const bool kc_pinned = std::getenv("FPM_MIXED_KCHUNK") != nullptr;
+  int kcm = mixed_kchunk() + (mixed_kchunk() & 1);
+  if (!kc_pinned) kcm = fill_chunk(kcm, (long long)((d.nx + 3) / 4 + 31) / 32 * ((d.ny + 3) / 4) * nrhs);
+  H.g0 = mixed_grid(d.nx, d.ny, d.nz, kcm);
+  // level-0 TMA passes (three potentials on 384 x 384 x 192: 16 -> 0.726 s,
+  // 24 -> 0.716 s, 48 -> 0.715 s)
   H.kc0 = (int)env_double("FPM_MG_KCHUNK", 24);
   H.kc0 = H.kc0 < 2 ? 2 : H.kc0 + (H.kc0 & 1);
+  if (!std::getenv("FPM_MG_KCHUNK")) H.kc0 = fill_chunk(H.kc0, mg_tma_ctas_per_chunk(H.g0, nrhs));
   H.pxb = (H.g0.px + 15) / 16 * 16;
   auto zeros = [&](long long n) {
     float* x = A.get<float>(n);
@@ -897,6 +939,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   };
   double res[kMaxRhs] = {}, best[kMaxRhs] = {}, scale[kMaxRhs] = {};
   int stall[kMaxRhs] = {}, iters[kMaxRhs] = {};
+  int done[kMaxRhs] = {}, est[kMaxRhs] = {};  // inner iterations so far / of the last inner solve
   bool live[kMaxRhs] = {};
   // (Re)start the inner PCG of the right-hand sides in set from their
   // current true residuals: drop by kMgDrop, or just far enough for the
@@ -913,6 +956,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
       h0.tol2 = drop * drop;
       h0.active = 1;
       CUDA_TRY(cudaMemcpyAsync(S + m, &h0, sizeof(MgScalars), cudaMemcpyHostToDevice, st));
+      done[m] = 0;
     }
     CUDA_TRY(mg_pcg_start(H, r64, scale, set, v, S, rb, st));
   };
@@ -926,18 +970,35 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
   const int chunk_len = ci < 1 ? 1 : (ci > 50 ? 50 : ci);
   int total = 0;
   ChunkGraphs graphs;
+  // Adaptive chunks only where an iteration is cheap next to its launches
+  // (measured: three potentials on 64 x 64 x 32, 8.1 -> 6.7 ms per solve);
+  // on 384 x 384 x 192 fixed chunks are faster (0.665 s vs 0.681 s).
+  const bool adapt = (double)d.ncell() * nrhs < kMgAdaptCells;
   while (set && total < max_sweeps) {
-    int chunk = chunk_len;
+    int chunk = adapt ? kMgMinChunk : chunk_len;
+    for (int m = 0; m < nrhs && adapt; m++) {
+      if (!((set >> m) & 1u)) continue;
+      int pred;
+      if (est[m] > 0)
+        pred = est[m] >= done[m] ? est[m] + 1 - done[m] : est[m] / 8;
+      else
+        pred = done[m] > kMgFirstChunk ? done[m] : kMgFirstChunk;
+      if (pred > chunk) chunk = pred;
+    }
+    if (chunk > chunk_len) chunk = chunk_len;
     if (chunk > max_sweeps - total) chunk = max_sweeps - total;
     {
       TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
-      graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
+      // one captured iteration, replayed: chunks of any length share it
+      graphs.run_units(chunk, 1, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
     }
     total += chunk;
     CUDA_TRY(cudaMemcpyAsync(hS, S, kMaxRhs * sizeof(MgScalars), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(herr, rb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     if (*herr) throw Error{FPM_E_TIMEOUT, "multigrid: a bounded wait for a TMA copy gave up"};
+    for (int m = 0; m < nrhs; m++)
+      if ((set >> m) & 1u) done[m] = hS[m].iters;
     // Which right-hand sides have finished an outer step?
     unsigned upd = 0;
     for (int m = 0; m < nrhs; m++)
@@ -952,6 +1013,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
       if (!((upd >> m) & 1u)) continue;
       const int inner = hS[m].iters;
       iters[m] += inner;
+      est[m] = inner;
       const double prev = res[m];
       res[m] = true_res(m);
       if (verbose())

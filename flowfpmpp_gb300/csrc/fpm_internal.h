@@ -300,6 +300,8 @@ struct MgRed {
   int* err;  // set when a bounded TMA wait gave up
 };
 long long mg_red_partials(const MgHierarchy& H);
+// CTAs of one z-chunk of the level-0 TMA passes (all right-hand sides).
+long long mg_tma_ctas_per_chunk(const MixedGrid& G, int nrhs);
 // Tensor maps of the level-0 passes (after the level-0 vectors exist).
 cudaError_t mg_encode(MgHierarchy& H, const MgVecs& v);
 // A launch covers the right-hand sides whose bit is set in mask and whose

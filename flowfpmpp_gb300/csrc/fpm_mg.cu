@@ -969,6 +969,11 @@ Scale4 scale4(const double* s, unsigned mask) {
 
 }  // namespace
 
+// CTAs of one z-chunk of the level-0 TMA passes (all right-hand sides).
+long long mg_tma_ctas_per_chunk(const MixedGrid& G, int nrhs) {
+  return (long long)((G.ng + kTX / 4 - 1) / (kTX / 4)) * ((G.ny + kTY - 1) / kTY) * nrhs;
+}
+
 // Level-0 V-cycle tail shared by start and iteration: the residual of the
 // first smoothing sweep restricted to level 1, the coarse cycle, and the
 // post-smoothing + r.z pass.
