@@ -262,21 +262,6 @@ class ChunkGraphs {
     CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
     note_launches(it->second.launches);
   }
-  // Runs `launch_one` n times as a sum of power-of-two graphs, so chunks of
-  // any length reuse at most log2(n)+1 captured graphs.
-  template <class F>
-  void run_pow2(int n, cudaStream_t st, F&& launch_one) {
-    for (int p = 1 << 20; p >= 1; p >>= 1)
-      if (n & p) run(p, st, launch_one);
-  }
-  // Runs `launch_one` n times as repeats of one graph of `unit` iterations
-  // (plus power-of-two graphs for the remainder).
-  template <class F>
-  void run_units(int n, int unit, cudaStream_t st, F&& launch_one) {
-    if (unit < 1) unit = 1;
-    for (int i = 0; i < n / unit; i++) run(unit, st, launch_one);
-    run_pow2(n % unit, st, launch_one);
-  }
 
  private:
   static cudaStream_t capture_stream() {
@@ -990,7 +975,8 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     {
       TimedRun t(FPM_TIMER_PCG_MIXED_ITER, chunk, st);
       // one captured iteration, replayed: chunks of any length share it
-      graphs.run_units(chunk, 1, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
+      for (int i = 0; i < chunk; i++)
+        graphs.run(1, st, [&](cudaStream_t s2) { CUDA_TRY(mg_pcg_iteration(H, v, S, rb, s2)); });
     }
     total += chunk;
     CUDA_TRY(cudaMemcpyAsync(hS, S, kMaxRhs * sizeof(MgScalars), cudaMemcpyDeviceToHost, st));
