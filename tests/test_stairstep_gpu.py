@@ -307,13 +307,18 @@ def test_multi_rhs_three_influence_fields(gpu_lib, method):
 @pytest.mark.parametrize("dims,kchunk,axes", [((37, 29, 11), 16, (0, 1, 2)), ((133, 21, 37), 16, (0, 2)),
                                               ((150, 17, 6), 2, (1,)), ((64, 12, 33), 4, (2, 0, 1)),
                                               ((259, 9, 5), 6, (0, 1)),
-                                              ((20, 18, 6), 2, (0, 1, 2, 0))])
+                                              ((20, 18, 6), 2, (0, 1, 2, 0)),
+                                              ((70, 45, 29), None, (0, 1, 2))])
 def test_multigrid_tile_edges(gpu_lib, monkeypatch, dims, kchunk, axes):
     """The multigrid path on shapes that end level-0 TMA tiles mid-tile in x
     (nx not a multiple of 4 or of 128) and y (ny not a multiple of 8), chunks
     mid-aggregate in z (odd nz, several chunks, chunks of 2 planes), with one
-    to four right-hand sides (the last case: level 1 is already the
-    coarsest): potentials within 1e-9 of the FP64 oracle."""
+    to four right-hand sides (the fifth case: level 1 is already the
+    coarsest; the last: plane chunks chosen by the library to fill the SMs):
+    potentials within 1e-9 of the FP64 oracle."""
     from flowfpmpp_gb300 import workloads
-    monkeypatch.setenv("FPM_MG_KCHUNK", str(kchunk))
+    if kchunk is None:
+        monkeypatch.delenv("FPM_MG_KCHUNK", raising=False)
+    else:
+        monkeypatch.setenv("FPM_MG_KCHUNK", str(kchunk))
     _multi_rhs_vs_oracle(gpu_lib, workloads.sphere_grid(*dims), 4, axes)
