@@ -77,12 +77,13 @@ def _frame(nx, ny, nz, ax, ay, az, solid_interior, axis):
 
 def boxes_grid(n=256, seed=2025, ratio=1.01, half=4.0, nboxes=4):
     """Weighted-Jacobi bandwidth case: n^3 grid, four axis-aligned boxes of 8-40 cells per side at
-    seeded positions, the first one touching the outer boundary (x = -half)."""
+    seeded positions, the first one touching the outer boundary (x = -half).  On grids below 160
+    cells per side the sides are capped at n/4 so that every box fits."""
     rng = np.random.default_rng(seed)
     ax = geometric_axis(n, -half, half, ratio)
     solid = np.zeros((n, n, n), dtype=np.int32)
     for b in range(nboxes):
-        size = rng.integers(8, 41, size=3)
+        size = np.minimum(rng.integers(8, 41, size=3), max(1, n // 4))
         lo = np.array([rng.integers(0, n - s + 1) for s in size])
         if b == 0:
             lo[0] = 0  # touches the west boundary
