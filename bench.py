@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-densities", action="store_true",
+                    help="pcg_sphere / pcg_ellipsoids: skip the force densities on the solved potentials")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="pcg_ellipsoids only: a smaller grid of the same generator (profiling runs)")
     ap.add_argument("--arms", default="fp64,mixed,mg,learned_mixed,learned_mg",
@@ -310,7 +312,78 @@ def run_pcg(args):
             line[label]["vs_fp64_rel_linf"] = max(
                 float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
                 for a, b in zip(lm["phi"], out["fp64"]["phi"]))
+    if not args.no_densities:
+        line["densities"] = densities(args, lib, f, out, head, dsolid, dax, faces_dev, bgs, stream)
+        for label, errs in line["densities"].pop("terms_vs_fp64").items():
+            line[label]["terms_vs_fp64"] = errs
     print(json.dumps(line), flush=True)
+
+
+def densities(args, lib, f, out, head, dsolid, dax, faces_dev, bgs, stream):
+    """The force densities of every arm's three potentials in the C1 flow
+    (U = 1 plus 8 Gaussian z-tubes, acceleration of 6 Fourier modes):
+    -(omega x u).grad(phi_i), -a.grad(phi_i) and their integrals through
+    fpm_compute_stairstep_fpm_terms_3d_dev, the call timed on the head arm's
+    potentials (124 bytes per cell and potential: phi, nine flow fields and
+    the solid flag read, five fields written), and each arm's integrals and
+    density fields against the FP64 arm's."""
+    import torch
+    from flowfpmpp_gb300 import workloads
+    VP = ctypes.c_void_p
+    nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    fl = workloads.flow_c1(f)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    dflow = [dev(fl[k]) for k in ("u", "v", "w", "ox", "oy", "oz", "ax", "ay", "az")]
+    n3 = nx * ny * nz
+    outs = [torch.empty(n3, dtype=torch.float64, device="cuda") for _ in range(5)]
+    bounds = np.array([-1e300, 1e300] * 3)
+
+    def terms(phi_t, axis):
+        tot = (ctypes.c_double * 2)()
+        bg = np.ascontiguousarray(bgs[axis], dtype=np.float64)
+        rc = lib.fpm_compute_stairstep_fpm_terms_3d_dev(
+            VP(phi_t.data_ptr()), *[VP(t.data_ptr()) for t in dflow], VP(dsolid.data_ptr()), bg.ctypes.data_as(VP),
+            *[VP(t.data_ptr()) for t in dax], *[VP(t.data_ptr()) for t in faces_dev[6 * axis:6 * axis + 6]],
+            bounds.ctypes.data_as(VP), *[VP(o.data_ptr()) for o in outs], tot, nx, ny, nz, VP(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+        return [tot[0], tot[1]]
+
+    ref, errs, head_totals, seconds = None, {}, None, None
+    order = sorted(out, key=lambda lb: lb != "fp64")  # the FP64 arm first: the others are compared with it
+    for label in order:
+        phis = [torch.from_numpy(p).cuda() for p in out[label]["phi"]]
+        r = []
+        for axis in range(3):
+            tot = terms(phis[axis], axis)
+            r.append((tot, outs[3].cpu().numpy(), outs[4].cpu().numpy()))
+        if label == "fp64":
+            ref = r
+        elif ref is not None:
+            # integrals relative to the largest FP64 integral (some are zero by symmetry)
+            scale = max(max(abs(x) for x in t0) for t0, _, _ in ref) or 1e-300
+            tot_rel, field_rel = 0.0, 0.0
+            for (t, vo, ad), (t0, vo0, ad0) in zip(r, ref):
+                for a, b in zip(t, t0):
+                    tot_rel = max(tot_rel, abs(a - b) / scale)
+                for a, b in ((vo, vo0), (ad, ad0)):
+                    field_rel = max(field_rel, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+            errs[label] = {"integrals_rel": tot_rel, "densities_rel_linf": field_rel}
+        if label == head:
+            head_totals = [x[0] for x in r]
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 5
+            e0.record(stream)
+            for _ in range(reps):
+                for axis in range(3):
+                    terms(phis[axis], axis)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            seconds = e0.elapsed_time(e1) / reps / 1e3
+    gbs = 124.0 * n3 * 3 / seconds / 1e9
+    return {"kernel": "k_terms", "seconds_three_potentials": seconds, "gbs": gbs, "bytes_per_cell_potential": 124,
+            "integrals_head": head_totals, "terms_vs_fp64": errs}
 
 
 def run_learned(args):
