@@ -1624,7 +1624,8 @@ int fpm_compute_stairstep_fpm_terms_3d_dev(const double* phi, const double* u, c
     Faces f{const_cast<double*>(xlo), const_cast<double*>(xhi), const_cast<double*>(ylo),
             const_cast<double*>(yhi), const_cast<double*>(zlo), const_cast<double*>(zhi)};
     TermsOut o{gx, gy, gz, vortex, advection};
-    CUDA_TRY(launch_terms(d, phi, fl, solid, body_grad, axes, f, bounds, o, cm.S, cm.rb, st));
+    double* rcp = A.get<double>((long long)(nx + 2) + (ny + 2) + nz);
+    CUDA_TRY(launch_terms(d, phi, fl, solid, body_grad, axes, f, bounds, o, rcp, cm.S, cm.rb, st));
     const SolveScalars& h = read_scalars(cm.S, st);
     totals[0] = h.red[0];
     totals[1] = h.red[1];

@@ -79,9 +79,10 @@ struct Flow {
 struct TermsOut {
   double *gx, *gy, *gz, *vortex, *advection;
 };
+// rcp: scratch for (nx+2) + (ny+2) + nz spacing reciprocals.
 cudaError_t launch_terms(const Dims& d, const double* phi, const Flow& fl, const int32_t* solid, const double bg[3],
-                         const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o, SolveScalars* S,
-                         const RedBuf& rb, cudaStream_t st);
+                         const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o, double* rcp,
+                         SolveScalars* S, const RedBuf& rb, cudaStream_t st);
 
 // FP64 -> double-float conversion (fpm_stairstep_df.cu).
 cudaError_t launch_to_df(const double* x, float2* y, long long n, cudaStream_t st);

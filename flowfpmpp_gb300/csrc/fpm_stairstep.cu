@@ -483,6 +483,49 @@ __device__ __forceinline__ void face_gradients(const Dims& d, const double* __re
   else g[5] = ddiv(dsub(phi[p + pl], pc), dsub(ax.zc[k], ax.zc[k - 1]));
 }
 
+// a / b from y = RN(1/b), correctly rounded: Markstein's correction step
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990): q0 = RN(a y), the remainder
+// r = a - b q0 is exact with one FMA, and RN(q0 + r y) is the IEEE quotient
+// when y is the correctly rounded reciprocal and no underflow occurs.  Three
+// FP64 instructions instead of a full division; the per-cell parity tests
+// compare the densities bit for bit with the oracle's IEEE divisions.
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  const double q0 = __dmul_rn(a, y);
+  const double r = __fma_rn(-b, q0, a);
+  return __fma_rn(r, y, q0);
+}
+
+// face_gradients with the spacing reciprocals rx[i] = 1 / (xc[i] - xc[i-1]),
+// ry[j] likewise, rz[k] = 1 / (zc[k] - zc[k-1]) (zc 0-based).
+__device__ __forceinline__ void face_gradients_rcp(const Dims& d, const double* __restrict__ phi,
+                                                   const int32_t* __restrict__ solid, const Bg& bg, const Faces& f,
+                                                   const Axes& ax, const double* __restrict__ rx,
+                                                   const double* __restrict__ ry, const double* __restrict__ rz,
+                                                   int i, int j, int k, double g[6]) {
+  const long long p = d.ph(i, j, k), px = d.nx + 2, pl = d.plane();
+  const double* xc = ax.xc;
+  const double* yc = ax.yc;
+  const double pc = phi[p];
+  if (i == 1) g[0] = f.xlo[d.xf(j, k)];
+  else if (solid[p - 1] != 0) g[0] = bg.x;
+  else g[0] = div_rcp(dsub(pc, phi[p - 1]), dsub(xc[i], xc[i - 1]), rx[i]);
+  if (i == d.nx) g[1] = f.xhi[d.xf(j, k)];
+  else if (solid[p + 1] != 0) g[1] = bg.x;
+  else g[1] = div_rcp(dsub(phi[p + 1], pc), dsub(xc[i + 1], xc[i]), rx[i + 1]);
+  if (j == 1) g[2] = f.ylo[d.yf(i, k)];
+  else if (solid[p - px] != 0) g[2] = bg.y;
+  else g[2] = div_rcp(dsub(pc, phi[p - px]), dsub(yc[j], yc[j - 1]), ry[j]);
+  if (j == d.ny) g[3] = f.yhi[d.yf(i, k)];
+  else if (solid[p + px] != 0) g[3] = bg.y;
+  else g[3] = div_rcp(dsub(phi[p + px], pc), dsub(yc[j + 1], yc[j]), ry[j + 1]);
+  if (k == 1) g[4] = f.zlo[d.zf(i, j)];
+  else if (solid[p - pl] != 0) g[4] = bg.z;
+  else g[4] = div_rcp(dsub(pc, phi[p - pl]), dsub(ax.zc[k - 1], ax.zc[k - 2]), rz[k - 1]);
+  if (k == d.nz) g[5] = f.zhi[d.zf(i, j)];
+  else if (solid[p + pl] != 0) g[5] = bg.z;
+  else g[5] = div_rcp(dsub(phi[p + pl], pc), dsub(ax.zc[k], ax.zc[k - 1]), rz[k]);
+}
+
 // stairstep_residual_3d, src/fpm_stairstep_mpi_3d.f90:403-419 -> S->res.
 __global__ void k_face_residual(Dims d, const double* __restrict__ phi, const double* __restrict__ rhs,
                                 const int32_t* __restrict__ solid, Bg bg, Faces f, Axes ax, SolveScalars* S,
@@ -517,12 +560,13 @@ cudaError_t launch_face_residual(const Dims& d, const double* phi, const double*
 // lie strictly inside bounds -> S->red[0..1].
 __global__ void k_terms(Dims d, const double* __restrict__ phi, Flow fl, const int32_t* __restrict__ solid, Bg bg,
                         Axes ax, Faces f, double b0, double b1, double b2, double b3, double b4, double b5,
-                        TermsOut o, SolveScalars* S, RedBuf rb) {
+                        TermsOut o, const double* __restrict__ rx, const double* __restrict__ ry,
+                        const double* __restrict__ rz, SolveScalars* S, RedBuf rb) {
   double s[2] = {0.0, 0.0}, m[1] = {0.0};
   CELL_LOOP_BEGIN
   const long long cc = d.in(i, j, k);
   double g[6];
-  face_gradients(d, phi, solid, bg, f, ax, ax.xc, ax.yc, i, j, k, g);
+  face_gradients_rcp(d, phi, solid, bg, f, ax, rx, ry, rz, i, j, k, g);
   const double mask = solid[d.ph(i, j, k)] == 0 ? 1.0 : 0.0;
   const double hm = dmul(mask, 0.5);
   const double gx = dmul(hm, dadd(g[0], g[1]));
@@ -553,12 +597,36 @@ __global__ void k_terms(Dims d, const double* __restrict__ phi, Flow fl, const i
     }
   }
 }
+// Spacing reciprocals for face_gradients_rcp: rx[i] = 1 / (xc[i] - xc[i-1])
+// for i = 1 .. nx+1, ry likewise, rz[k] = 1 / (zc[k] - zc[k-1]) for
+// k = 1 .. nz-1 (IEEE divisions; entry 0 unused).
+__global__ void k_spacing_rcp(Dims d, Axes ax, double* rx, double* ry, double* rz) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < (d.nx + 2) + (d.ny + 2) + d.nz;
+       t += gridDim.x * blockDim.x) {
+    if (t < d.nx + 2) {
+      rx[t] = t >= 1 ? ddiv(1.0, dsub(ax.xc[t], ax.xc[t - 1])) : 0.0;
+    } else if (t < d.nx + 2 + d.ny + 2) {
+      const int j = t - (d.nx + 2);
+      ry[j] = j >= 1 ? ddiv(1.0, dsub(ax.yc[j], ax.yc[j - 1])) : 0.0;
+    } else {
+      const int k = t - (d.nx + 2) - (d.ny + 2);
+      rz[k] = k >= 1 ? ddiv(1.0, dsub(ax.zc[k], ax.zc[k - 1])) : 0.0;
+    }
+  }
+}
+
 cudaError_t launch_terms(const Dims& d, const double* phi, const Flow& fl, const int32_t* solid, const double bg[3],
-                         const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o, SolveScalars* S,
-                         const RedBuf& rb, cudaStream_t st) {
+                         const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o, double* rcp,
+                         SolveScalars* S, const RedBuf& rb, cudaStream_t st) {
+  double* rx = rcp;
+  double* ry = rx + (d.nx + 2);
+  double* rz = ry + (d.ny + 2);
+  const int nr = (d.nx + 2) + (d.ny + 2) + d.nz;
+  k_spacing_rcp<<<(nr + 255) / 256, 256, 0, st>>>(d, ax, rx, ry, rz); note_launch();
   Launch L = cells_launch(d);
   k_terms<<<L.grid, L.block, 0, st>>>(d, phi, fl, solid, Bg{bg[0], bg[1], bg[2]}, ax, f, bounds[0], bounds[1],
-                                      bounds[2], bounds[3], bounds[4], bounds[5], o, S, rb); note_launch();
+                                      bounds[2], bounds[3], bounds[4], bounds[5], o, rx, ry, rz, S, rb);
+  note_launch();
   return cudaGetLastError();
 }
 
