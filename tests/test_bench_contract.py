@@ -1,7 +1,6 @@
-"""bench.py's reference arm on the CPU: the JSON line the harness
-parses (metric, value, unit, impl, cpu_baseline, e2e with zero transfer
-bytes) on a small grid, and the silent exit of the non-zero ranks under a
-multi-rank launch."""
+"""bench.py's reference arm on the CPU: its one JSON line (metric, value,
+unit, impl, cpu_baseline, e2e with zero transfer bytes) on a small grid, and
+the silent exit of the non-zero ranks under a multi-rank launch."""
 import json
 import os
 import subprocess
