@@ -612,6 +612,10 @@ def main():
         gbs, cores, nsw, el = cpu_sample(n)
         cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
                "sample": f"{nsw} weighted-Jacobi sweeps of the {n}^3 operator in {el:.1f} s (oracle, OpenMP)"}
+        # the reference's serial order on one core, beside the all-cores figure
+        g1, _, n1, e1 = cpu_sample(n, budget_s=4.0, threads=1)
+        cpu["single_core"] = {"value": g1, "unit": "GB/s", "cores": 1,
+                              "sample": f"{n1} sweeps of the same operator in {e1:.1f} s (oracle, one thread)"}
     cfg = config(n)
     cfg["parallelism"] = f"replicas x{world}"
     cfg["autotuned"] = tuned
