@@ -2,12 +2,15 @@
 // double-float arithmetic, streamed through shared memory by TMA.
 //
 // Each CTA owns a TX x TY column of interior cells and marches k through a
-// chunk of planes.  One elected thread keeps a 4-deep ring of phi planes
-// (tile plus one-cell x-y halo) and a 3-deep ring of (src, rdiag) planes in
+// chunk of planes.  One elected thread keeps a ring of phi planes (tile plus
+// one-cell x-y halo; 4 deep) and a ring of (src, rdiag) planes (3 deep) in
 // flight with cp.async.bulk.tensor, completion tracked by mbarriers; every
 // thread reads its seven phi values and its src/rdiag from shared memory, so
 // global memory sees each field once per sweep (the x-y halo re-reads hit L2)
-// and the DRAM stream never waits on a dependent load.
+// and the DRAM stream never waits on a dependent load.  A thread owns CY rows
+// of its column; with CY even, row pairs run through the packed FP32x2
+// instructions.  Tile shape, ring depths and planes per CTA are template and
+// launch parameters chosen by the host autotuner.
 //
 // Internal layout (owned by this module, not the caller's):
 //   phi   float2 (hi, lo), padded (0:nx+1, 0:ny+1, 1:nz) with x pitch PX even
