@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--method", choices=["jacobi_fma", "jacobi", "jacobi_df"], default="jacobi_fma",
+                    help="jacobi256: the sweep timed as the headline (the others are timed as secondary keys)")
+    ap.add_argument("--head-only", action="store_true", help="jacobi256: time only the headline method")
+    ap.add_argument("--no-pcg", action="store_true",
+                    help="jacobi256: skip the three-potential PCG measurement on the 384x384x192 grid")
     ap.add_argument("--no-densities", action="store_true",
                     help="pcg_sphere / pcg_ellipsoids: skip the force densities on the solved potentials")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
@@ -82,9 +87,9 @@ def workload(n):
     return workloads.boxes_grid(n=n)
 
 
-def config(n):
+def config(n, method="jacobi_fma"):
     return {"workload": f"stair-step weighted Jacobi {n}^3, 4 boxes, phi_x, {SWEEPS} sweeps",
-            "grid": [n, n, n], "sweeps": SWEEPS, "method": "jacobi_df", "stretch_ratio": 1.01,
+            "grid": [n, n, n], "sweeps": SWEEPS, "method": method, "stretch_ratio": 1.01,
             "l2_policy": "inputs larger than L2 (phi, src, rdiag, phi' = 4 x 134 MB per sweep)"}
 
 
@@ -471,7 +476,191 @@ def run_frames(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- C3 inside the default line
+C3_FIXTURE = os.path.join(ROOT, "tests", "golden", "c3_phix_oracle.npz")
+MG_LEVEL0_BYTES = 68   # multigrid level 0, per cell, right-hand side and iteration (spmv, update, residual, smoothing)
+FP64_PCG_BYTES = 112   # the reference's FP64 PCG iteration, per cell (14 fields)
+
+
+def fixture_error(phi_padded, nx, ny, fx):
+    """Relative max-norm error of phi_x at the oracle fixture's sampled cells
+    (normalised by the oracle field's max |phi|) and of the whole-field sum."""
+    interior = np.asarray(phi_padded).reshape((nx + 2, ny + 2, -1), order="F")[1:nx + 1, 1:ny + 1, :]
+    flat = interior.ravel(order="F")
+    samp = flat[::int(fx["stride"])]
+    ref = fx["sample"]
+    scale = float(fx["checksum"][2])
+    return {"rel_linf_sampled": float(np.abs(samp - ref).max() / scale), "cells_compared": int(ref.size),
+            "sum_rel": float(abs(flat.sum() - fx["checksum"][0]) / float(fx["checksum"][1]))}
+
+
+def oracle_pcg_iteration_s(f, body, faces, threads):
+    """Seconds per FP64 PCG iteration of the oracle on the host cores: two
+    bounded solves (10 and 30 iterations from phi = 0) differenced, so the
+    operator build, the true residuals and the gauge cancel."""
+    import oracle as orc
+    orc.build()
+    orc.set_threads(threads)
+    times = []
+    for its in (10, 30):
+        phi = f["phi"].copy(order="F")
+        t0 = time.perf_counter()
+        orc.solve_stairstep_poisson_3d(phi, f["rhs"], f["solid"], body, *faces, f["xc"], f["yc"], f["zc"], f["dx"],
+                                       f["dy"], f["dz"], 1e-300, its, 1000000, "pcg")
+        times.append(time.perf_counter() - t0)
+    orc.set_threads(1)
+    return (times[1] - times[0]) / 20.0
+
+
+def pcg_c3(args, lib):
+    """The PCG half of the metric on the three-ellipsoid 384x384x192 grid:
+    phi_x, phi_y, phi_z to a 1e-10 max-norm residual with the multigrid-
+    preconditioned FP32 PCG in FP64 refinement (all three per launch, timed
+    over solves) and with plain FP64 PCG (one solve of the three), phi_x of
+    both against the oracle's FP64 PCG fixture, and the oracle's per-iteration
+    time on the host cores times the FP64 iteration count as the CPU figure."""
+    import torch
+    from flowfpmpp_gb300 import stairstep as ss
+    from flowfpmpp_gb300 import workloads
+    f = workloads.ellipsoids_grid()
+    nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    n3 = nx * ny * nz
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    faces_host, faces_dev, bgs, rhss = [], [], [], []
+    for axis in range(3):
+        body = np.zeros(3)
+        body[axis] = 1.0
+        faces = [x.copy(order="F") for x in f["faces"]]
+        ss.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], body, *faces, f["dx"], f["dy"], f["dz"])
+        faces_host.append(faces)
+        faces_dev += [dev(x) for x in faces]
+        bgs.append(body)
+        rhss.append(dev(f["rhs"]))
+    phis = [dev(f["phi"]) for _ in range(3)]
+    dsolid = dev(f["solid"])
+    dax = [dev(f[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    VP = ctypes.c_void_p
+    bg = np.ascontiguousarray(np.concatenate(bgs))
+    stream = torch.cuda.current_stream()
+
+    def solve(method):
+        for t in phis:
+            t.zero_()
+        sweeps = (ctypes.c_int * 3)()
+        res = (ctypes.c_double * 3)()
+        rc = lib.fpm_solve_stairstep_multi_dev(
+            3, (VP * 3)(*[t.data_ptr() for t in phis]), (VP * 3)(*[t.data_ptr() for t in rhss]), VP(dsolid.data_ptr()),
+            bg.ctypes.data_as(VP), (VP * 18)(*[t.data_ptr() for t in faces_dev]), *[VP(t.data_ptr()) for t in dax],
+            nx, ny, nz, ctypes.c_double(1e-10), 2000000, 50, method, sweeps, res, VP(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+        return list(sweeps), list(res)
+
+    def timer(which):
+        nl, tot = ctypes.c_longlong(), ctypes.c_double()
+        lib.fpm_timing_read(which, ctypes.byref(nl), ctypes.byref(tot), 1)
+        return nl.value, tot.value
+
+    out = {}
+    for label, method, warm, steps in (("mg", 4, 1, 2), ("fp64", 0, 0, 1)):
+        for _ in range(warm):
+            solve(method)
+        torch.cuda.synchronize()
+        lib.fpm_timing_enable(1)
+        timer(3), timer(2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            sw, res = solve(method)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lib.fpm_timing_enable(0)
+        it_mixed, it_fp64 = timer(3), timer(2)
+        out[label] = {"seconds": e0.elapsed_time(e1) / steps / 1e3, "iterations": sw, "residual": res,
+                      "solves_timed": steps, "phi": [t.cpu().numpy().copy() for t in phis],
+                      "iter_timer": {"mg": it_mixed, "fp64": it_fp64}}
+    line = {"workload": "3 ellipsoids 384x384x192, ratio 1.02, phi_x/phi_y/phi_z to 1e-10 max-norm residual",
+            "grid": [nx, ny, nz], "tolerance": 1e-10, "check_interval": 50,
+            "value": out["mg"]["seconds"], "unit": "s", "higher_is_better": False,
+            "arm": "FP32 PCG with an aggregation-multigrid preconditioner in FP64 refinement (all three per launch)",
+            "speedup_vs_fp64": out["fp64"]["seconds"] / out["mg"]["seconds"]}
+    fx = None
+    if os.path.exists(C3_FIXTURE):
+        fx = np.load(C3_FIXTURE)
+        if tuple(int(x) for x in fx["grid"]) != (nx, ny, nz):
+            fx = None
+    for label in ("mg", "fp64"):
+        o = out[label]
+        d = {k: o[k] for k in ("seconds", "iterations", "residual", "solves_timed")}
+        if fx is not None:
+            d["phi_x_vs_oracle"] = fixture_error(o["phi"][0], nx, ny, fx)
+        line[label] = d
+    line["fp64"]["iterations_oracle_phi_x"] = int(fx["iterations"]) if fx is not None else None
+    line["mg"]["vs_gpu_fp64_rel_linf"] = [rel_linf(a, b) for a, b in zip(out["mg"]["phi"], out["fp64"]["phi"])]
+    # roofline of the iteration: algorithmic bytes of level 0 (coarse levels
+    # not counted) and of the reference's FP64 iteration over their timers
+    nl, ms = out["mg"]["iter_timer"]["mg"]
+    mg_bytes = MG_LEVEL0_BYTES * float(n3) * sum(out["mg"]["iterations"]) * out["mg"]["solves_timed"]
+    nl64, ms64 = out["fp64"]["iter_timer"]["fp64"]
+    fp64_bytes = FP64_PCG_BYTES * float(n3) * sum(out["fp64"]["iterations"])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    line["roofline"] = {
+        "bound": "hbm", "unit": "GB/s", "peak": peak,
+        "mg_iteration": {"achieved": mg_bytes / (ms / 1e3) / 1e9, "frac": mg_bytes / (ms / 1e3) / 1e9 / peak,
+                         "bytes_per_cell_rhs": MG_LEVEL0_BYTES, "iteration_ms_all_rhs": ms / max(nl, 1),
+                         "note": "level-0 bytes over the whole iteration time (coarse levels included in the time)"},
+        "fp64_iteration": {"achieved": fp64_bytes / (ms64 / 1e3) / 1e9,
+                           "frac": fp64_bytes / (ms64 / 1e3) / 1e9 / peak, "bytes_per_cell": FP64_PCG_BYTES,
+                           "iteration_ms": ms64 / max(nl64, 1)}}
+    if not args.no_cpu_baseline:
+        import oracle as orc
+        cores = orc.max_threads()
+        per_it = oracle_pcg_iteration_s(f, bgs[0], faces_host[0], cores)
+        total_its = sum(out["fp64"]["iterations"])
+        line["cpu_baseline"] = {"value": per_it * total_its, "unit": "s", "cores": cores, "kind": "port",
+                                "sample": f"oracle FP64 PCG, 20 iterations of phi_x timed ({per_it * 1e3:.1f} ms per "
+                                          f"iteration, OpenMP over z-planes) x {total_its} iterations (the FP64 arm's "
+                                          f"count for the three potentials)"}
+    return line
+
+
 # ---------------------------------------------------------------- GPU arm
+# Sweep kernels of the Jacobi methods: (C ABI method id, timer id, kernel,
+# arithmetic, FP64 instructions per cell or None).
+JACOBI_METHODS = {
+    "jacobi_fma": (6, 1, "k_jacobi_f64_fma", "f64 (fused multiply-add)", 8),
+    "jacobi": (1, 1, "k_jacobi_f64", "f64 (separately rounded, bit-identical to the oracle per sweep)", 15),
+    "jacobi_df": (2, 0, "k_jacobi_df_tma", "f32x2 double-float (48-bit significand)", None),
+}
+
+
+def oracle_solve(f, faces, threads):
+    """The oracle's 2000-sweep weighted-Jacobi solve of the same problem on
+    `threads` host cores (operator build, sweeps, residual check, gauge):
+    returns (phi, seconds)."""
+    import oracle as orc
+    orc.build()
+    orc.set_threads(threads)
+    phi = f["phi"].copy(order="F")
+    t0 = time.perf_counter()
+    sw, _ = orc.solve_stairstep_poisson_3d(phi, f["rhs"], f["solid"], f["body"], *faces, f["xc"], f["yc"], f["zc"],
+                                           f["dx"], f["dy"], f["dz"], -1.0, SWEEPS, SWEEPS, "jacobi")
+    el = time.perf_counter() - t0
+    orc.set_threads(1)
+    assert sw == SWEEPS
+    return phi, el
+
+
+def rel_linf(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -504,6 +693,7 @@ def main():
     lib.fpm_kernel_launches.restype = ctypes.c_longlong
 
     n = args.n
+    head = args.method
     f = workload(n)
     faces = [a.copy(order="F") for a in f["faces"]]
     ss.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], f["body"], *faces, f["dx"], f["dy"], f["dz"])
@@ -517,39 +707,62 @@ def main():
     sw, res = ctypes.c_int(), ctypes.c_double()
     stream = torch.cuda.current_stream()
 
-    def step():
+    def step(method):
         d_phi.zero_()
         rc = lib.fpm_solve_stairstep_poisson_3d_dev(
             P(d_phi), P(d_rhs), P(d_solid), bg.ctypes.data_as(ctypes.c_void_p), *[P(t) for t in d_faces],
-            *[P(t) for t in d_axes], n, n, n, ctypes.c_double(-1.0), SWEEPS, SWEEPS, 2, ctypes.byref(sw),
-            ctypes.byref(res), ctypes.c_void_p(stream.cuda_stream))
+            *[P(t) for t in d_axes], n, n, n, ctypes.c_double(-1.0), SWEEPS, SWEEPS, JACOBI_METHODS[method][0],
+            ctypes.byref(sw), ctypes.byref(res), ctypes.c_void_p(stream.cuda_stream))
         if rc != 0:
             raise RuntimeError(lib.fpm_last_error().decode())
 
-    for _ in range(args.warmup):
-        step()
-    assert sw.value == SWEEPS
-    barrier()
-    torch.cuda.synchronize()
-    lib.fpm_timing_enable(1)
-    lib.fpm_timing_read(0, ctypes.byref(ctypes.c_longlong()), ctypes.byref(ctypes.c_double()), 1)
-    launches0 = lib.fpm_kernel_launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    def sweep_ms(method):
+        nl, tot = ctypes.c_longlong(), ctypes.c_double()
+        lib.fpm_timing_read(JACOBI_METHODS[method][1], ctypes.byref(nl), ctypes.byref(tot), 1)
+        return tot.value / max(nl.value, 1)
+
+    def timed(method, steps, warmup, clocks=False):
+        """(ms per solve, ms per sweep kernel, kernel launches, clock summary)"""
+        for _ in range(warmup):
+            step(method)
+        assert sw.value == SWEEPS
+        barrier()
+        torch.cuda.synchronize()
+        lib.fpm_timing_enable(1)
+        sweep_ms(method)  # clears the counter
+        launches0 = lib.fpm_kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clk = ClockSampler(local) if clocks else None
+        if clk:
+            clk.__enter__()
         e0.record(stream)
-        for _ in range(args.steps):
-            step()
+        for _ in range(steps):
+            step(method)
         e1.record(stream)
         torch.cuda.synchronize()
-    launches = lib.fpm_kernel_launches() - launches0
-    lib.fpm_timing_enable(0)
-    barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    nl, tot = ctypes.c_longlong(), ctypes.c_double()
-    lib.fpm_timing_read(0, ctypes.byref(nl), ctypes.byref(tot), 1)
-    sweep_ms = tot.value / max(nl.value, 1)
+        if clk:
+            clk.__exit__(None, None, None)
+        launches = lib.fpm_kernel_launches() - launches0
+        lib.fpm_timing_enable(0)
+        barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps)
+        return ms, sweep_ms(method), launches, (clk.summary() if clk else None)
+
+    ms, head_sweep_ms, launches, clocks = timed(head, args.steps, args.warmup, clocks=True)
     value = world * algorithmic_gb(n) / (ms / 1e3)
     residual = res.value
+    phis = {head: d_phi.cpu().numpy().reshape(f["phi"].shape, order="F").copy()}
+    others = {}
+    if not args.head_only:
+        for m in JACOBI_METHODS:
+            if m == head:
+                continue
+            oms, osw, _, _ = timed(m, 2, 1)
+            phis[m] = d_phi.cpu().numpy().reshape(f["phi"].shape, order="F").copy()
+            others[m] = {"dtype": JACOBI_METHODS[m][3], "kernel": JACOBI_METHODS[m][2],
+                         "value": world * algorithmic_gb(n) / (oms / 1e3), "unit": "GB/s", "ms_per_solve": oms,
+                         "sweep_us": osw * 1e3,
+                         "sweep_gbs": BYTES_PER_CELL_SWEEP * float(n) ** 3 / (osw / 1e3) / 1e9}
 
     # e2e through the host-array C ABI with pinned buffers
     def pinned(a):
@@ -570,20 +783,30 @@ def main():
         args_ = [h_phi.ctypes.data_as(ctypes.c_void_p), h_in[0][0].ctypes.data_as(ctypes.c_void_p),
                  h_in[1][0].ctypes.data_as(ctypes.c_void_p), bg.ctypes.data_as(ctypes.c_void_p)]
         args_ += [x[0].ctypes.data_as(ctypes.c_void_p) for x in h_in[2:]]
-        rc = lib.fpm_solve_stairstep_poisson_3d(*args_, n, n, n, ctypes.c_double(-1.0), SWEEPS, SWEEPS, 2,
-                                                ctypes.byref(sw), ctypes.byref(res))
+        rc = lib.fpm_solve_stairstep_poisson_3d(*args_, n, n, n, ctypes.c_double(-1.0), SWEEPS, SWEEPS,
+                                                JACOBI_METHODS[head][0], ctypes.byref(sw), ctypes.byref(res))
         if rc != 0:
             raise RuntimeError(lib.fpm_last_error().decode())
 
     e2e_step()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
+    e2e_steps = max(1, args.steps // 2)
+    for _ in range(e2e_steps):
         e2e_step()
-    e2e_ms = max_over_ranks((time.perf_counter() - t0) / max(1, args.steps // 2) * 1e3)
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / e2e_steps * 1e3)
     e2e_value = world * algorithmic_gb(n) / (e2e_ms / 1e3)
+    e2e_parity = rel_linf(h_phi, phis[head])
     for x in [p0] + [x[1] for x in h_in]:
         lib.fpm_host_free(ctypes.c_void_p(x))
+
+    fp64_rate = ctypes.c_double()
+    if lib.fpm_measure_fp64_rate(ctypes.byref(fp64_rate), ctypes.c_void_p(stream.cuda_stream)) != 0:
+        raise RuntimeError(lib.fpm_last_error().decode())
+
+    pcg = None
+    if not args.no_pcg and world == 1:
+        pcg = pcg_c3(args, lib)
 
     reps.close()
     if rank != 0:
@@ -595,42 +818,63 @@ def main():
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    achieved = BYTES_PER_CELL_SWEEP * float(n) ** 3 / (sweep_ms / 1e3) / 1e9
+    achieved = BYTES_PER_CELL_SWEEP * float(n) ** 3 / (head_sweep_ms / 1e3) / 1e9
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "jacobi_df_256cubed.json")
+    prof = os.path.join(ROOT, "profiles", f"{JACOBI_METHODS[head][2]}_256cubed.json")
     if n == 256 and os.path.exists(prof):
         try:
             traffic = json.load(open(prof)).get("dram_bytes_per_launch")
         except (OSError, ValueError):
             traffic = None
-    tx, ty, kc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    tuned = None
-    if lib.fpm_jacobi_df_config(n, n, n, ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(kc)) == 0:
-        tuned = {"tile": [tx.value, ty.value], "planes_per_cta": kc.value}
-    cpu = None
+    roofline = {"bound": "hbm", "kernel": JACOBI_METHODS[head][2], "achieved": achieved, "peak": peak,
+                "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "avg_launch_us": head_sweep_ms * 1e3, "algorithmic_bytes_per_launch": BYTES_PER_CELL_SWEEP * n ** 3}
+    fp64_per_cell = JACOBI_METHODS[head][4]
+    if fp64_per_cell:
+        got = fp64_per_cell * float(n) ** 3 / (head_sweep_ms / 1e3)
+        roofline["fp64_pipe"] = {"instructions_per_cell": fp64_per_cell, "achieved_per_s": got,
+                                 "peak_per_s": fp64_rate.value, "frac": got / fp64_rate.value,
+                                 "peak_source": "measured in this run (fpm_measure_fp64_rate)"}
+    for m, o in others.items():
+        o["hbm_frac"] = o["sweep_gbs"] / peak
+        if JACOBI_METHODS[m][4]:
+            o["fp64_pipe_frac"] = JACOBI_METHODS[m][4] * float(n) ** 3 / (o["sweep_us"] * 1e-6) / fp64_rate.value
+    if "jacobi_df" in others:
+        traffic_df = None
+        prof = os.path.join(ROOT, "profiles", "jacobi_df_256cubed.json")
+        if n == 256 and os.path.exists(prof):
+            traffic_df = json.load(open(prof)).get("dram_bytes_per_launch")
+        others["jacobi_df"]["traffic"] = traffic_df
+    cpu, parity = None, None
     if world == 1 and not args.no_cpu_baseline:
-        gbs, cores, nsw, el = cpu_sample(n)
+        import oracle as orc
+        orc.build()
+        cores = orc.max_threads()
+        ref_phi, el = oracle_solve(f, faces, cores)
+        gbs = algorithmic_gb(n) / el
         cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
-               "sample": f"{nsw} weighted-Jacobi sweeps of the {n}^3 operator in {el:.1f} s (oracle, OpenMP)"}
+               "sample": f"the whole {SWEEPS}-sweep {n}^3 solve in {el:.1f} s (oracle, OpenMP over z-planes)"}
         # the reference's serial order on one core, beside the all-cores figure
         g1, _, n1, e1 = cpu_sample(n, budget_s=4.0, threads=1)
         cpu["single_core"] = {"value": g1, "unit": "GB/s", "cores": 1,
                               "sample": f"{n1} sweeps of the same operator in {e1:.1f} s (oracle, one thread)"}
-    cfg = config(n)
+        parity = {"vs": f"oracle weighted Jacobi, {SWEEPS} sweeps of the same operator, gauge removed",
+                  "tolerance": 1e-12, "rel_linf": rel_linf(phis[head], ref_phi), "e2e_vs_device": e2e_parity}
+        for m in others:
+            others[m]["rel_linf_vs_oracle"] = rel_linf(phis[m], ref_phi)
+        parity["pass"] = parity["rel_linf"] <= 1e-12
+    cfg = config(n, head)
     cfg["parallelism"] = f"replicas x{world}"
-    cfg["autotuned"] = tuned
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32x2 (double-float, 48-bit significand) sweeps, f64 residuals",
-            "data": "synthetic (seeded boxes)", "config": cfg,
-            "roofline": {"bound": "hbm", "kernel": "k_jacobi_df_tma", "achieved": achieved, "peak": peak,
-                         "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "avg_launch_us": sweep_ms * 1e3,
-                         "algorithmic_bytes_per_launch": BYTES_PER_CELL_SWEEP * n ** 3},
-            "cpu_baseline": cpu,
+            "vs_baseline": None, "dtype": "f64" if fp64_per_cell else JACOBI_METHODS[head][3],
+            "arithmetic": JACOBI_METHODS[head][3], "data": "synthetic (seeded boxes)", "config": cfg,
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity,
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": e2e_ms},
-            "gpu_launches": int(launches), "clocks": clk.summary(), "final_residual": residual}
+            "gpu_launches": int(launches), "clocks": clocks, "final_residual": residual, "other_methods": others}
+    if pcg is not None:
+        line["pcg_c3"] = pcg
     print(json.dumps(line), flush=True)
 
 

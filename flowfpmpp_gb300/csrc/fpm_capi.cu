@@ -341,7 +341,9 @@ static double pcg_loop(const SolveArgs& a, const Dims& d, double* p, const doubl
 // jacobi_iterate (src/fpm_stairstep_mpi_3d.f90:200-225): sweeps in chunks of
 // check_interval, max-norm residual after each chunk.  The two buffers swap
 // roles instead of copying back; every sweep reads the latest iterate, so the
-// values are those of the reference's ping-pong with copy.
+// values are those of the reference's ping-pong with copy.  FPM_METHOD_JACOBI
+// sweeps with separately rounded operations, FPM_METHOD_JACOBI_FMA with fused
+// multiply-adds.
 static void jacobi_loop_f64(const SolveArgs& a, const Dims& d, double* next, const double* src, const double* diag,
                             const double* rdiag, const Coefs& c, Common& cm, int* sweeps, cudaStream_t st) {
   double *cur = a.phi, *oth = next;
@@ -353,7 +355,8 @@ static void jacobi_loop_f64(const SolveArgs& a, const Dims& d, double* next, con
     {
       TimedRun t(FPM_TIMER_JACOBI_F64, nsteps, st);
       for (int s = 0; s < nsteps; s++) {
-        CUDA_TRY(launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
+        CUDA_TRY(a.method == FPM_METHOD_JACOBI_FMA ? launch_jacobi_f64_fma(d, cur, oth, src, rdiag, c, st)
+                                                   : launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
         std::swap(cur, oth);
       }
     }
@@ -1034,7 +1037,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
 // solve them one after the other; FPM_METHOD_PCG_MIXED solves them together.
 static bool valid_method(int m) {
   return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED ||
-         m == FPM_METHOD_PCG_MG || m == FPM_METHOD_FCG_LEARNED;
+         m == FPM_METHOD_PCG_MG || m == FPM_METHOD_FCG_LEARNED || m == FPM_METHOD_JACOBI_FMA;
 }
 
 // FPM_METHOD_FCG_LEARNED: FP64 flexible CG (Notay's FCG(1): the Polak-Ribiere
@@ -1244,7 +1247,8 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
         if (m > 0) CUDA_TRY(launch_init_fields(d, a.solid, a.phi, next, st));
         CUDA_TRY(cudaMemsetAsync(cm.S, 0, sizeof(SolveScalars), st));
         if (a.method == FPM_METHOD_PCG) pcg_loop(a, d, next, src[m], diag, rdiag, c, A, cm, &sweeps[m], st);
-        else if (a.method == FPM_METHOD_JACOBI) jacobi_loop_f64(a, d, next, src[m], diag, rdiag, c, cm, &sweeps[m], st);
+        else if (a.method == FPM_METHOD_JACOBI || a.method == FPM_METHOD_JACOBI_FMA)
+          jacobi_loop_f64(a, d, next, src[m], diag, rdiag, c, cm, &sweeps[m], st);
         else jacobi_loop_df(a, d, src[m], diag, rdiag, coef, c, A, cm, &sweeps[m], st);
       }
     }
@@ -1330,6 +1334,22 @@ int fpm_jacobi_df_config(int nx, int ny, int nz, int* tile_x, int* tile_y, int* 
   });
 }
 int fpm_version(void) { return 100; }
+
+int fpm_measure_fp64_rate(double* instr_per_s, void* stream) {
+  return guarded([&] {
+    if (!instr_per_s) throw Error{FPM_E_ARG, "null argument"};
+    require_device();
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int blocks = 0, threads = 0;
+    fp64_rate_shape(sms, &blocks, &threads);
+    Scratch A(st);
+    double* out = A.get<double>((size_t)blocks * threads);
+    CUDA_TRY(fp64_rate_probe(out, blocks, threads, st, instr_per_s));
+  });
+}
 
 void* fpm_host_alloc(size_t bytes) {
   void* p = nullptr;
@@ -1711,8 +1731,8 @@ int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, con
     if (!a || !b || !src || !rdiag || !xc || !yc || !zc || !dx || !dy || !dz) throw Error{FPM_E_ARG, "null argument"};
     if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
     if (nsweeps < 0) throw Error{FPM_E_ARG, "nsweeps must be >= 0"};
-    if (method != FPM_METHOD_JACOBI && method != FPM_METHOD_JACOBI_DF)
-      throw Error{FPM_E_METHOD, "sweeps need method jacobi or jacobi_df"};
+    if (method != FPM_METHOD_JACOBI && method != FPM_METHOD_JACOBI_DF && method != FPM_METHOD_JACOBI_FMA)
+      throw Error{FPM_E_METHOD, "sweeps need method jacobi, jacobi_df or jacobi_fma"};
     require_device();
     cudaStream_t st = (cudaStream_t)stream;
     const Dims d{nx, ny, nz};
@@ -1720,12 +1740,13 @@ int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, con
     const long long ncoef = 2LL * (nx + ny + nz);
     double* coef = A.get<double>(ncoef);
     CUDA_TRY(launch_axis_coefs(Axes{xc, yc, zc, dx, dy, dz}, nx, ny, nz, coef, st));
-    if (method == FPM_METHOD_JACOBI) {
+    if (method == FPM_METHOD_JACOBI || method == FPM_METHOD_JACOBI_FMA) {
       Coefs c = coef_views(coef, nx, ny, nz);
       double *cur = a, *oth = b;
       TimedRun t(FPM_TIMER_JACOBI_F64, nsweeps, st);
       for (int s = 0; s < nsweeps; s++) {
-        CUDA_TRY(launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
+        CUDA_TRY(method == FPM_METHOD_JACOBI_FMA ? launch_jacobi_f64_fma(d, cur, oth, src, rdiag, c, st)
+                                                 : launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
         std::swap(cur, oth);
       }
     } else {

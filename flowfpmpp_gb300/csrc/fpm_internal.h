@@ -57,6 +57,10 @@ cudaError_t launch_build_operator(const Dims& d, const double* rhs, const int32_
 cudaError_t launch_init_fields(const Dims& d, const int32_t* solid, double* phi, double* next, cudaStream_t st);
 cudaError_t launch_jacobi_f64(const Dims& d, const double* a, double* b, const double* src, const double* rdiag,
                               const Coefs& c, cudaStream_t st);
+cudaError_t launch_jacobi_f64_fma(const Dims& d, const double* a, double* b, const double* src, const double* rdiag,
+                                  const Coefs& c, cudaStream_t st);
+void fp64_rate_shape(int sms, int* blocks, int* threads);
+cudaError_t fp64_rate_probe(double* out, int blocks, int threads, cudaStream_t st, double* instr_per_s);
 cudaError_t launch_copy_interior(const Dims& d, const double* from, double* to, cudaStream_t st);
 cudaError_t launch_operator_residual(const Dims& d, const double* phi, const double* src, const double* diag,
                                      const Coefs& c, SolveScalars* S, const RedBuf& rb, cudaStream_t st);

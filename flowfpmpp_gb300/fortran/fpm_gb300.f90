@@ -158,6 +158,7 @@ contains
       case ('jacobi_df'); m = 2
       case ('pcg_mixed'); m = 3
       case ('pcg_mg'); m = 4
+      case ('jacobi_fma'); m = 6
       case default; error stop 'stair-step method must be pcg or jacobi'
       end select
     end if

@@ -17,9 +17,15 @@ MAGIC = b"FFPM2D02"
 
 
 def read_ffpm2d02(path):
-    """Returns a frame dict (nx, ny, xf, yf, u, v, solid, dt, ring, kin, time)."""
-    with open(path, "rb") as fh:
-        raw = fh.read()
+    """Returns a frame dict (nx, ny, xf, yf, u, v, solid, dt, ring, kin, time).
+    A path ending in .xz is decompressed first."""
+    if str(path).endswith(".xz"):
+        import lzma
+        with lzma.open(path, "rb") as fh:
+            raw = fh.read()
+    else:
+        with open(path, "rb") as fh:
+            raw = fh.read()
     if raw[:8] != MAGIC:
         raise ValueError("unexpected input format")
     nx, ny = (int(x) for x in np.frombuffer(raw, dtype="<i4", count=2, offset=8))

@@ -65,6 +65,9 @@ extern "C" {
 #define FPM_METHOD_FCG_LEARNED 5 /* FP64 flexible CG with the learned network as preconditioner (one diagonal
                                     step on what the network leaves); FP64 PCG finishes if it stalls.  Only
                                     through fpm_solve_stairstep_learned_dev (it needs the network) */
+#define FPM_METHOD_JACOBI_FMA 6 /* weighted Jacobi 0.2/0.8 in FP64 storage and arithmetic with fused multiply-adds
+                                   (the reference's summation order, one rounding per multiply-add); differs
+                                   from FPM_METHOD_JACOBI in the last bits, twice as fast on GB300's FP64 pipe */
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char* fpm_last_error(void);
@@ -75,7 +78,7 @@ int fpm_version(void);
  * kernel `which` (FPM_TIMER_*), the number of launches and their total
  * device time; reset != 0 clears that counter afterwards. */
 #define FPM_TIMER_JACOBI_DF 0   /* double-float Jacobi sweep (TMA-streamed) */
-#define FPM_TIMER_JACOBI_F64 1  /* FP64 Jacobi sweep */
+#define FPM_TIMER_JACOBI_F64 1  /* FP64 Jacobi sweep (FPM_METHOD_JACOBI or FPM_METHOD_JACOBI_FMA) */
 #define FPM_TIMER_PCG_ITER 2    /* one FP64 PCG iteration (three kernels) */
 #define FPM_TIMER_PCG_MIXED_ITER 3 /* one FP32 inner PCG iteration over all right-hand sides */
 #define FPM_TIMER_FRAMES_ITER 4 /* one batched FP32 PCG iteration over every frame of a 2-D batch */
@@ -87,6 +90,11 @@ int fpm_timing_read(int which, long long* launches, double* total_ms, int reset)
 /* Tile shape (x, y) and planes per CTA the double-float Jacobi autotuner chose
  * for an nx*ny*nz grid (after a double-float run at that size). */
 int fpm_jacobi_df_config(int nx, int ny, int nz, int* tile_x, int* tile_y, int* kchunk);
+/* Measures the device's FP64 fused multiply-add rate (instructions per
+ * second, best of two timed launches of independent FMA chains): the peak of
+ * the FP64-pipe roofline that FP64 kernels are reported against.  No
+ * reference counterpart (a measurement utility). */
+int fpm_measure_fp64_rate(double* instr_per_s, void* stream);
 /* Pinned (page-locked) host memory for fast transfers; NULL on failure. */
 void* fpm_host_alloc(size_t bytes);
 void fpm_host_free(void* p);

@@ -62,4 +62,6 @@ def main(path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/examples/data/flapping_foil_216000.bin")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_foil_golden.py <flapping_foil_216000.bin>")
+    main(sys.argv[1])

@@ -117,13 +117,24 @@ def test_df_sweeps_within_1e12_after_2000(gpu_lib):
     assert abs(out_g["res"] - out_o["res"]) <= 1e-9 * out_o["res"]
 
 
-@pytest.mark.parametrize("method", ["jacobi", "jacobi_df", "pcg"])
+def test_fma_sweeps_within_1e12_after_2000(gpu_lib):
+    """FP64 sweeps with fused multiply-adds stay within 1e-12 relative of the
+    separately rounded FP64 oracle after 2000 sweeps."""
+    c = stairstep_case_exact(False)
+    out_g = gpu_run(c, "jacobi_fma", -1.0, 2000, ci=2000)
+    out_o = cpu_run(c, "jacobi", -1.0, 2000, ci=2000)
+    assert out_g["sweeps"] == 2000
+    assert rel_linf(out_g["phi"], out_o["phi"]) <= 1e-12
+    assert abs(out_g["res"] - out_o["res"]) <= 1e-9 * out_o["res"]
+
+
+@pytest.mark.parametrize("method", ["jacobi", "jacobi_fma", "jacobi_df", "pcg"])
 def test_exact_linear_solution_gpu(gpu_lib, method):
     """The reference's exactness test (test_stairstep_exact_3d.f90:40-50) on the GPU."""
     c = stairstep_case_exact(True)
     # The double-float iterate carries a 48-bit significand, so its max-norm
     # residual floors near 1e-11 on this grid; it is held to the PCG tolerance.
-    tol = 1e-12 if method == "jacobi" else 1e-10
+    tol = 1e-12 if method in ("jacobi", "jacobi_fma") else 1e-10
     g = gpu_run(c, method, tol, 400000)
     gx, gy, gz, vortex, adv, totals = g["terms"]
     errors, ierr = exact_expectations(c, g["phi"], gx, gy, gz, vortex, totals)
@@ -131,7 +142,7 @@ def test_exact_linear_solution_gpu(gpu_lib, method):
     assert g["res"] <= 2 * tol and g["chk"] < 1e-9
     assert errors[0] < 1e-9 and errors[1] < 1e-9 and errors[2] < 1e-9 and errors[3] == 0
     assert ierr < 1e-10 and np.all(np.isfinite([g["res"], g["chk"], *errors, *totals]))
-    o = cpu_run(c, method if method != "jacobi_df" else "jacobi", tol, 400000)
+    o = cpu_run(c, "jacobi" if method.startswith("jacobi") else method, tol, 400000)
     assert abs(g["sweeps"] - o["sweeps"]) <= 50
 
 
