@@ -512,6 +512,87 @@ def oracle_pcg_iteration_s(f, body, faces, threads):
     return (times[1] - times[0]) / 20.0
 
 
+TERMS_MULTI_BYTES = 220   # nine flow fields + solid once, phi and five outputs per potential (three potentials)
+TERMS_SINGLE_BYTES = 124  # one potential per call: phi, nine flow fields, solid, five outputs
+
+
+def c3_densities(lib, f, phis_host, faces_host, faces_dev, bgs, dsolid, dax, stream, check_oracle):
+    """Force densities of the three potentials in the C1-style flow on the C3
+    grid: the one-pass kernel for all three (double-float per cell) timed
+    against three calls of the bit-identical FP64 kernel; phi_x's fields and
+    integrals against the oracle's FP64 densities on the same potential."""
+    import torch
+    from flowfpmpp_gb300 import workloads
+    nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    n3 = nx * ny * nz
+    fl = workloads.flow_c1(f)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    dflow = [dev(fl[k]) for k in ("u", "v", "w", "ox", "oy", "oz", "ax", "ay", "az")]
+    dphi = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in phis_host]
+    outs = [torch.empty(n3, dtype=torch.float64, device="cuda") for _ in range(15)]
+    bounds = np.array([-1e300, 1e300] * 3)
+    VP = ctypes.c_void_p
+    bg = np.ascontiguousarray(np.concatenate(bgs))
+    tot = (ctypes.c_double * 6)()
+
+    def fused():
+        rc = lib.fpm_compute_stairstep_fpm_terms_3d_multi_dev(
+            3, (VP * 3)(*[t.data_ptr() for t in dphi]), *[VP(t.data_ptr()) for t in dflow], VP(dsolid.data_ptr()),
+            bg.ctypes.data_as(VP), *[VP(t.data_ptr()) for t in dax], (VP * 18)(*[t.data_ptr() for t in faces_dev]),
+            bounds.ctypes.data_as(VP), (VP * 15)(*[t.data_ptr() for t in outs]), tot, nx, ny, nz,
+            VP(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+
+    def single():
+        t2 = (ctypes.c_double * 2)()
+        for m in range(3):
+            b = np.ascontiguousarray(bgs[m])
+            rc = lib.fpm_compute_stairstep_fpm_terms_3d_dev(
+                VP(dphi[m].data_ptr()), *[VP(t.data_ptr()) for t in dflow], VP(dsolid.data_ptr()),
+                b.ctypes.data_as(VP), *[VP(t.data_ptr()) for t in dax],
+                *[VP(t.data_ptr()) for t in faces_dev[6 * m:6 * m + 6]], bounds.ctypes.data_as(VP),
+                *[VP(o.data_ptr()) for o in outs[5 * m:5 * m + 5]], t2, nx, ny, nz, VP(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(lib.fpm_last_error().decode())
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
+    t_single = timed(single, 2)
+    t_fused = timed(fused, 5)
+    res = {"kernel": "k_terms_multi<3>", "seconds_three_potentials": t_fused,
+           "bytes_per_cell": TERMS_MULTI_BYTES, "gbs": TERMS_MULTI_BYTES * float(n3) / t_fused / 1e9,
+           "arithmetic": "double-float per cell (48-bit significand), FP64 storage and integrals",
+           "integrals": [tot[m] for m in range(6)],
+           "single_potential_fp64_kernel": {"kernel": "k_terms", "seconds_three_calls": t_single,
+                                            "gbs": 3 * TERMS_SINGLE_BYTES * float(n3) / t_single / 1e9,
+                                            "arithmetic": "f64, bit-identical to the oracle"},
+           "speedup_vs_three_calls": t_single / t_fused}
+    if check_oracle:
+        import oracle as orc
+        ro = orc.compute_stairstep_fpm_terms_3d(phis_host[0].reshape(f["phi"].shape, order="F"), fl["u"], fl["v"],
+                                                fl["w"], fl["ox"], fl["oy"], fl["oz"], fl["ax"], fl["ay"], fl["az"],
+                                                f["solid"], bgs[0], f["xc"], f["yc"], f["zc"], f["dx"], f["dy"],
+                                                f["dz"], *faces_host[0], bounds)
+        fused()
+        torch.cuda.synchronize()
+        errs = [rel_linf(outs[c].cpu().numpy(), np.asarray(ro[c]).ravel(order="F")) for c in range(5)]
+        scale = max(abs(ro[5][0]), abs(ro[5][1]), 1e-300)
+        res["phi_x_vs_oracle"] = {"fields_rel_linf": max(errs), "per_field": errs,
+                                  "integrals_rel": max(abs(tot[0] - ro[5][0]), abs(tot[1] - ro[5][1])) / scale,
+                                  "tolerance": 1e-8}
+    return res
+
+
 def pcg_c3(args, lib):
     """The PCG half of the metric on the three-ellipsoid 384x384x192 grid:
     phi_x, phi_y, phi_z to a 1e-10 max-norm residual with the multigrid-
@@ -617,6 +698,9 @@ def pcg_c3(args, lib):
         "fp64_iteration": {"achieved": fp64_bytes / (ms64 / 1e3) / 1e9,
                            "frac": fp64_bytes / (ms64 / 1e3) / 1e9 / peak, "bytes_per_cell": FP64_PCG_BYTES,
                            "iteration_ms": ms64 / max(nl64, 1)}}
+    if not args.no_densities:
+        line["densities"] = c3_densities(lib, f, out["mg"]["phi"], faces_host, faces_dev, bgs, dsolid, dax, stream,
+                                         check_oracle=not args.no_cpu_baseline)
     if not args.no_cpu_baseline:
         import oracle as orc
         cores = orc.max_threads()

@@ -1652,6 +1652,54 @@ int fpm_compute_stairstep_fpm_terms_3d_dev(const double* phi, const double* u, c
   });
 }
 
+int fpm_compute_stairstep_fpm_terms_3d_multi_dev(int npot, const double* const* phi, const double* u,
+                                                 const double* v, const double* w, const double* ox,
+                                                 const double* oy, const double* oz, const double* ax,
+                                                 const double* ay, const double* az, const int32_t* solid,
+                                                 const double* body_grad, const double* xc, const double* yc,
+                                                 const double* zc, const double* dx, const double* dy,
+                                                 const double* dz, const double* const* faces, const double* bounds,
+                                                 double* const* outs, double* totals, int nx, int ny, int nz,
+                                                 void* stream) {
+  return guarded([&] {
+    if (npot < 1 || npot > kMaxRhs) throw Error{FPM_E_ARG, "npot must be 1..4"};
+    if (!phi || !u || !v || !w || !ox || !oy || !oz || !ax || !ay || !az || !solid || !body_grad || !xc || !yc ||
+        !zc || !dx || !dy || !dz || !faces || !bounds || !outs || !totals)
+      throw Error{FPM_E_ARG, "null argument"};
+    for (int m = 0; m < npot; m++) {
+      if (!phi[m]) throw Error{FPM_E_ARG, "null argument"};
+      for (int c = 0; c < 6; c++)
+        if (!faces[6 * m + c]) throw Error{FPM_E_ARG, "null argument"};
+      for (int c = 0; c < 5; c++)
+        if (!outs[5 * m + c]) throw Error{FPM_E_ARG, "null argument"};
+    }
+    if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
+    require_device();
+    cudaStream_t st = (cudaStream_t)stream;
+    const Dims d{nx, ny, nz};
+    Scratch A(st);
+    Trace t("stair-step FPM terms");
+    Flow fl{u, v, w, ox, oy, oz, ax, ay, az};
+    Axes axes{xc, yc, zc, dx, dy, dz};
+    Faces f[kMaxRhs];
+    for (int m = 0; m < npot; m++)
+      f[m] = Faces{const_cast<double*>(faces[6 * m]),     const_cast<double*>(faces[6 * m + 1]),
+                   const_cast<double*>(faces[6 * m + 2]), const_cast<double*>(faces[6 * m + 3]),
+                   const_cast<double*>(faces[6 * m + 4]), const_cast<double*>(faces[6 * m + 5])};
+    const dim3 tg = terms_multi_grid(d);
+    const size_t nb = (size_t)tg.x * tg.y * tg.z;
+    double* partials = A.get<double>(2 * (size_t)npot * nb);
+    unsigned int* ticket = A.get<unsigned int>(1);
+    double* dtot = A.get<double>(2 * (size_t)npot);
+    void* tables = A.get<unsigned char>(terms_multi_table_bytes(d));
+    CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
+    CUDA_TRY(launch_terms_multi(d, npot, phi, fl, solid, body_grad, axes, f, bounds, outs, tables, partials, ticket,
+                                dtot, st));
+    CUDA_TRY(cudaMemcpyAsync(totals, dtot, 2 * npot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  });
+}
+
 int fpm_compute_stairstep_fpm_terms_3d(const double* phi, const double* u, const double* v, const double* w,
                                        const double* ox, const double* oy, const double* oz, const double* ax,
                                        const double* ay, const double* az, const int32_t* solid,

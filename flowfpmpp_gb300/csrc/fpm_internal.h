@@ -83,6 +83,16 @@ struct Flow {
 struct TermsOut {
   double *gx, *gy, *gz, *vortex, *advection;
 };
+// Force densities of np <= kMaxRhs potentials in one pass (fpm_terms_multi.cu):
+// phi[m], faces[m], bg[3m..3m+2] per potential; outs[5m..5m+4] = gx, gy, gz,
+// vortex, advection; totals[2m], totals[2m+1] = the two integrals.  tables
+// holds terms_multi_table_bytes(d); partials 2 np x (blocks of cells_launch).
+cudaError_t launch_terms_multi(const Dims& d, int np, const double* const* phi, const Flow& fl,
+                               const int32_t* solid, const double* bg, const Axes& ax, const Faces* faces,
+                               const double bounds[6], double* const* outs, void* tables, double* partials,
+                               unsigned int* ticket, double* totals, cudaStream_t st);
+size_t terms_multi_table_bytes(const Dims& d);
+dim3 terms_multi_grid(const Dims& d);  // partials: 2 np x its block count
 // rcp: scratch for (nx+2) + (ny+2) + nz spacing reciprocals.
 cudaError_t launch_terms(const Dims& d, const double* phi, const Flow& fl, const int32_t* solid, const double bg[3],
                          const Axes& ax, const Faces& f, const double bounds[6], const TermsOut& o, double* rcp,

@@ -176,6 +176,24 @@ int fpm_compute_stairstep_fpm_terms_3d_dev(const double* phi, const double* u, c
                                            const double* yhi, const double* zlo, const double* zhi,
                                            const double* bounds, double* gx, double* gy, double* gz, double* vortex,
                                            double* advection, double* totals, int nx, int ny, int nz, void* stream);
+/* compute_stairstep_fpm_terms_3d (src/fpm_stairstep_mpi_3d.f90:426-497) for
+ * npot (1..4) potentials of one grid and flow in one pass, device arrays:
+ * the nine flow fields and solid are read once for all potentials.
+ * phi[m] (padded), body_grad[3m..3m+2] (host), faces[6m..6m+5] = xlo, xhi,
+ * ylo, yhi, zlo, zhi of potential m; outs[5m..5m+4] = gx, gy, gz, vortex,
+ * advection; totals[2m], totals[2m+1] (host) = its two integrals.  The
+ * per-cell arithmetic is double-float (48-bit significand; densities within
+ * about 1e-14 relative of the FP64 evaluation), not bit-identical to the
+ * single-potential call. */
+int fpm_compute_stairstep_fpm_terms_3d_multi_dev(int npot, const double* const* phi, const double* u,
+                                                 const double* v, const double* w, const double* ox,
+                                                 const double* oy, const double* oz, const double* ax,
+                                                 const double* ay, const double* az, const int32_t* solid,
+                                                 const double* body_grad, const double* xc, const double* yc,
+                                                 const double* zc, const double* dx, const double* dy,
+                                                 const double* dz, const double* const* faces, const double* bounds,
+                                                 double* const* outs, double* totals, int nx, int ny, int nz,
+                                                 void* stream);
 
 
 /* ---- fpm_laplace_3d (no body; src/fpm_laplace_3d.f90) -------------------

@@ -225,3 +225,22 @@ def test_partition_3d_known_answers():
     cm = -terms[0] / (4 * math.pi * 0.5 ** 3 / 3)
     assert abs(cm - cm_ref) < 1e-12 and round(cm, 3) == pytest.approx(0.639, abs=1e-12)
     assert np.all(terms[1:] == 0)
+
+
+def test_c3_fixture_matches_the_generator():
+    """The committed C3 oracle fixture (tests/golden/make_c3_oracle.py) was
+    made from the inputs the seeded generator still produces: axes and solid
+    flags hash to the recorded digest, and the oracle's PCG met 1e-10."""
+    import importlib.util
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location("make_c3_oracle", os.path.join(here, "golden", "make_c3_oracle.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    fx = np.load(mk.OUT)
+    from flowfpmpp_gb300 import workloads
+    f = workloads.ellipsoids_grid()
+    assert str(fx["inputs_sha256"]) == mk.inputs_digest(f)
+    assert tuple(int(x) for x in fx["grid"]) == (f["nx"], f["ny"], f["nz"])
+    assert float(fx["residual"]) <= 1e-10 and int(fx["iterations"]) > 0
+    assert fx["sample"].size == -(-f["nx"] * f["ny"] * f["nz"] // int(fx["stride"]))
