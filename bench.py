@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="grid size per axis (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--method", choices=["jacobi_fma", "jacobi", "jacobi_df"], default="jacobi_fma",
+    ap.add_argument("--method", choices=["jacobi_fma", "jacobi_tf", "jacobi", "jacobi_df"], default="jacobi_fma",
                     help="jacobi256: the sweep timed as the headline (the others are timed as secondary keys)")
     ap.add_argument("--head-only", action="store_true", help="jacobi256: time only the headline method")
     ap.add_argument("--no-pcg", action="store_true",
@@ -71,11 +71,12 @@ def parse():
     ap.add_argument("--no-densities", action="store_true",
                     help="pcg_sphere / pcg_ellipsoids: skip the force densities on the solved potentials")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
-                    help="pcg_ellipsoids only: a smaller grid of the same generator (profiling runs)")
+                    help="pcg_ellipsoids / densities: a smaller grid of the same generator (profiling runs)")
     ap.add_argument("--arms", default="fp64,mixed,mg,learned_mixed,learned_mg",
                     help="pcg_sphere / pcg_ellipsoids: comma-separated solver arms to time (profiling runs take "
                          "one); learned_guess: add fcg_learned for the flexible CG with the network")
-    ap.add_argument("--workload", choices=["jacobi256", "pcg_sphere", "pcg_ellipsoids", "foil_frames", "learned_guess"],
+    ap.add_argument("--workload", choices=["jacobi256", "pcg_sphere", "pcg_ellipsoids", "foil_frames", "learned_guess",
+                                           "densities"],
                     default="jacobi256",
                     help="jacobi256: the headline bandwidth benchmark; pcg_sphere / pcg_ellipsoids: three-potential PCG "
                          "time to 1e-10 (plain FP64 vs mixed precision)")
@@ -713,11 +714,222 @@ def pcg_c3(args, lib):
     return line
 
 
+# ---------------------------------------------------------------- C1 and C4 inside the default line
+def multi_solve(lib, f, method, steps, warmup):
+    """phi_x, phi_y, phi_z of grid f to 1e-10 through fpm_solve_stairstep_multi_dev
+    (device arrays): (seconds per solve, iterations, residuals, potentials)."""
+    import torch
+    from flowfpmpp_gb300 import stairstep as ss
+    nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    faces_dev, bgs = [], []
+    for axis in range(3):
+        body = np.zeros(3)
+        body[axis] = 1.0
+        faces = [x.copy(order="F") for x in f["faces"]]
+        ss.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], body, *faces, f["dx"], f["dy"], f["dz"])
+        faces_dev += [dev(x) for x in faces]
+        bgs.append(body)
+    rhss = [dev(f["rhs"]) for _ in range(3)]
+    phis = [dev(f["phi"]) for _ in range(3)]
+    dsolid = dev(f["solid"])
+    dax = [dev(f[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    VP = ctypes.c_void_p
+    bg = np.ascontiguousarray(np.concatenate(bgs))
+    stream = torch.cuda.current_stream()
+    sweeps = (ctypes.c_int * 3)()
+    res = (ctypes.c_double * 3)()
+
+    def solve():
+        for t in phis:
+            t.zero_()
+        rc = lib.fpm_solve_stairstep_multi_dev(
+            3, (VP * 3)(*[t.data_ptr() for t in phis]), (VP * 3)(*[t.data_ptr() for t in rhss]), VP(dsolid.data_ptr()),
+            bg.ctypes.data_as(VP), (VP * 18)(*[t.data_ptr() for t in faces_dev]), *[VP(t.data_ptr()) for t in dax],
+            nx, ny, nz, ctypes.c_double(1e-10), 2000000, 50, method, sweeps, res, VP(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+
+    for _ in range(warmup):
+        solve()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    shape = f["phi"].shape
+    return (e0.elapsed_time(e1) / steps / 1e3, list(sweeps), list(res),
+            [t.cpu().numpy().reshape(shape, order="F") for t in phis])
+
+
+def pcg_c1(args, lib):
+    """The C1 case: sphere r = 0.5 on the 64x64x32 grid of ratio 1.03,
+    phi_x, phi_y, phi_z to 1e-10 with plain FP64 PCG and with the multigrid
+    refinement, each potential against the oracle's FP64 PCG (1e-9), and the
+    oracle's whole three-potential solve on the host cores."""
+    from flowfpmpp_gb300 import workloads
+    import oracle as orc
+    f = workloads.sphere_grid()
+    out = {}
+    for label, method in (("fp64", 0), ("mg", 4)):
+        sec, sw, res, phis = multi_solve(lib, f, method, steps=5, warmup=2)
+        out[label] = {"seconds": sec, "iterations": sw, "residual": res, "phi": phis}
+    orc.build()
+    cores = orc.max_threads()
+    orc.set_threads(cores)
+    ref, t0 = [], time.perf_counter()
+    for axis in range(3):
+        body = np.zeros(3)
+        body[axis] = 1.0
+        faces = [x.copy(order="F") for x in f["faces"]]
+        orc.enforce_stairstep_compatibility_3d(f["rhs"], f["solid"], body, *faces, f["dx"], f["dy"], f["dz"])
+        phi = f["phi"].copy(order="F")
+        orc.solve_stairstep_poisson_3d(phi, f["rhs"], f["solid"], body, *faces, f["xc"], f["yc"], f["zc"], f["dx"],
+                                       f["dy"], f["dz"], 1e-10, 2000000, 50, "pcg")
+        ref.append(phi)
+    el = time.perf_counter() - t0
+    orc.set_threads(1)
+    line = {"workload": "sphere r=0.5, 64x64x32 on [-4,4]^2 x [-2,2], ratio 1.03, phi_x/phi_y/phi_z to 1e-10",
+            "value": out["mg"]["seconds"], "unit": "s", "higher_is_better": False,
+            "speedup_vs_fp64": out["fp64"]["seconds"] / out["mg"]["seconds"],
+            "cpu_baseline": {"value": el, "unit": "s", "cores": cores, "kind": "port",
+                             "sample": "the oracle's FP64 PCG of the three potentials (OpenMP over z-planes)"}}
+    for label in ("fp64", "mg"):
+        o = out[label]
+        line[label] = {"seconds": o["seconds"], "iterations": o["iterations"], "residual": o["residual"],
+                       "rel_linf_vs_oracle": [rel_linf(a, b) for a, b in zip(o["phi"], ref)]}
+    line["parity_pass"] = all(x <= 1e-9 for lb in ("fp64", "mg") for x in line[lb]["rel_linf_vs_oracle"])
+    return line
+
+
+def oracle_frame(fr):
+    """The reference foil example's per-frame work (examples/flapping_foil_fpm.f90:61-81)
+    on the oracle: phi_x, phi_y by FP64 PCG to 1e-10, then fpm_partition_terms_2d."""
+    import oracle as orc
+    from flowfpmpp_gb300.workloads import frame_as_stairstep
+    s = frame_as_stairstep(fr)
+    terms, phis = np.zeros((2, 4)), []
+    for d in range(2):
+        body = np.zeros(3)
+        body[d] = 1.0
+        faces = [x.copy(order="F") for x in s["faces"]]
+        orc.enforce_stairstep_compatibility_3d(s["rhs"], s["solid"], body, *faces, s["dx"], s["dy"], s["dz"])
+        phi = s["phi"].copy(order="F")
+        orc.solve_stairstep_poisson_3d(phi, s["rhs"], s["solid"], body, *faces, s["xc"], s["yc"], s["zc"], s["dx"],
+                                       s["dy"], s["dz"], 1e-10, 2000000, 50, "pcg")
+        p2 = np.asfortranarray(phi[1:fr["nx"] + 1, 1:fr["ny"] + 1, 0])
+        terms[d], _, _ = orc.fpm_partition_terms_2d(p2, body[:2], fr["u"], fr["v"], fr["solid"], fr["xf"], fr["yf"],
+                                                    fr["kin"], fr["ring"], fr["dt"], fr["nu"])
+        phis.append(p2)
+    return terms, phis
+
+
+def frames_c4(args, lib):
+    """The C4 batch: 256 uneven 2-D foil frames (96^2..512^2, ratio 1.02),
+    phi_x and phi_y to 1e-10 and the four partition terms each, host arrays in
+    and out through fpm_partition_frames_2d; the three smallest frames against
+    the oracle, and the oracle's time on them scaled to the batch's cells."""
+    import torch
+    from flowfpmpp_gb300 import partition as pt
+    from flowfpmpp_gb300 import workloads
+    import oracle as orc
+    frames = workloads.foil_frames()
+    cells = sum(f["nx"] * f["ny"] for f in frames)
+    pt.partition_frames_2d(frames, tolerance=1e-10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    terms, sweeps, res, phis = pt.partition_frames_2d(frames, tolerance=1e-10, return_phi=True)
+    el = time.perf_counter() - t0
+    orc.build()
+    cores = orc.max_threads()
+    orc.set_threads(cores)
+    pick = sorted(range(len(frames)), key=lambda m: frames[m]["nx"] * frames[m]["ny"])[:3]
+    errs_phi, errs_terms, t_orc, cells_orc = [], [], 0.0, 0
+    for m in pick:
+        t1 = time.perf_counter()
+        ot, op = oracle_frame(frames[m])
+        t_orc += time.perf_counter() - t1
+        cells_orc += frames[m]["nx"] * frames[m]["ny"]
+        for d in range(2):
+            errs_phi.append(rel_linf(phis[m][d], op[d]))
+        errs_terms.append(float(np.abs(terms[m] - ot).max() / max(np.abs(ot).max(), 1e-300)))
+    orc.set_threads(1)
+    cpu_s = t_orc * cells / cells_orc
+    return {"workload": "256 foil frames 96^2..512^2, ratio 1.02, phi_x/phi_y to 1e-10 + 4 terms each",
+            "value": len(frames) / el, "unit": "frames/s", "higher_is_better": True, "seconds_per_batch": el,
+            "cells_2d": int(cells), "max_residual": float(np.max(res)), "all_converged": bool(np.all(res <= 1e-10)),
+            "iterations": {"max": int(sweeps.max()), "mean": float(sweeps.mean())},
+            "path": "each frame's pair by one multigrid-preconditioned refinement call, frames on worker streams",
+            "vs_oracle": {"frames": pick, "phi_rel_linf": max(errs_phi), "terms_rel": max(errs_terms),
+                          "tolerance": {"phi": 1e-9, "terms": 1e-8}},
+            "cpu_baseline": {"value": len(frames) / cpu_s, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": f"oracle FP64 PCG + terms of the 3 smallest frames in {t_orc:.1f} s, scaled "
+                                       f"by cells to the batch"}}
+
+
+# ---------------------------------------------------------------- force densities alone
+def run_densities(args):
+    """fpm_compute_stairstep_fpm_terms_3d_multi_dev for three seeded random
+    potentials and flow fields on the three-ellipsoid grid (default
+    384x384x192; --grid for a smaller one), timed over `steps` calls."""
+    import torch
+    from flowfpmpp_gb300 import build as fbuild
+    fbuild.build()
+    import flowfpmpp_gb300
+    from flowfpmpp_gb300 import workloads
+    lib = flowfpmpp_gb300.lib()
+    f = workloads.ellipsoids_grid(*args.grid) if args.grid else workloads.ellipsoids_grid()
+    nx, ny, nz = f["nx"], f["ny"], f["nz"]
+    n3 = nx * ny * nz
+    g = torch.Generator(device="cuda").manual_seed(5)
+    phis = [torch.randn((nx + 2) * (ny + 2) * nz, dtype=torch.float64, device="cuda", generator=g) for _ in range(3)]
+    flow = [torch.randn(n3, dtype=torch.float64, device="cuda", generator=g) for _ in range(9)]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+    dsolid = dev(f["solid"])
+    dax = [dev(f[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    faces = [dev(x) for _ in range(3) for x in f["faces"]]
+    outs = [torch.empty(n3, dtype=torch.float64, device="cuda") for _ in range(15)]
+    bounds = np.array([-1e300, 1e300] * 3)
+    bg = np.array([1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0])
+    VP = ctypes.c_void_p
+    tot = (ctypes.c_double * 6)()
+    stream = torch.cuda.current_stream()
+
+    def call():
+        rc = lib.fpm_compute_stairstep_fpm_terms_3d_multi_dev(
+            3, (VP * 3)(*[t.data_ptr() for t in phis]), *[VP(t.data_ptr()) for t in flow], VP(dsolid.data_ptr()),
+            bg.ctypes.data_as(VP), *[VP(t.data_ptr()) for t in dax], (VP * 18)(*[t.data_ptr() for t in faces]),
+            bounds.ctypes.data_as(VP), (VP * 15)(*[t.data_ptr() for t in outs]), tot, nx, ny, nz,
+            VP(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fpm_last_error().decode())
+
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / max(args.steps, 1) / 1e3
+    print(json.dumps({"metric": "force densities of three potentials in one pass", "value": sec, "unit": "s",
+                      "higher_is_better": False, "steps": args.steps, "warmup": args.warmup,
+                      "config": {"workload": f"random fields on the three-ellipsoid grid {nx}x{ny}x{nz}",
+                                 "grid": [nx, ny, nz]},
+                      "gbs": 220.0 * n3 / sec / 1e9, "bytes_per_cell": 220}), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
 # Sweep kernels of the Jacobi methods: (C ABI method id, timer id, kernel,
 # arithmetic, FP64 instructions per cell or None).
 JACOBI_METHODS = {
     "jacobi_fma": (6, 1, "k_jacobi_f64_fma", "f64 (fused multiply-add)", 8),
+    "jacobi_tf": (7, 5, "k_jacobi_tf_tma", "f64 storage, triple-float arithmetic (about 2^-60 before the FP64 "
+                                           "rounding)", None),
     "jacobi": (1, 1, "k_jacobi_f64", "f64 (separately rounded, bit-identical to the oracle per sweep)", 15),
     "jacobi_df": (2, 0, "k_jacobi_df_tma", "f32x2 double-float (48-bit significand)", None),
 }
@@ -760,6 +972,10 @@ def main():
     if args.workload == "learned_guess":
         if rank == 0:
             run_learned(args)
+        return
+    if args.workload == "densities":
+        if rank == 0:
+            run_densities(args)
         return
     if args.workload != "jacobi256":
         if rank == 0:
@@ -888,9 +1104,11 @@ def main():
     if lib.fpm_measure_fp64_rate(ctypes.byref(fp64_rate), ctypes.c_void_p(stream.cuda_stream)) != 0:
         raise RuntimeError(lib.fpm_last_error().decode())
 
-    pcg = None
+    pcg = c1 = c4 = None
     if not args.no_pcg and world == 1:
         pcg = pcg_c3(args, lib)
+        c1 = pcg_c1(args, lib)
+        c4 = frames_c4(args, lib)
 
     reps.close()
     if rank != 0:
@@ -951,7 +1169,7 @@ def main():
     cfg["parallelism"] = f"replicas x{world}"
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if fp64_per_cell else JACOBI_METHODS[head][3],
+            "vs_baseline": None, "dtype": "f64" if head in ("jacobi_fma", "jacobi", "jacobi_tf") else "f32x2",
             "arithmetic": JACOBI_METHODS[head][3], "data": "synthetic (seeded boxes)", "config": cfg,
             "roofline": roofline, "cpu_baseline": cpu, "parity": parity,
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -959,6 +1177,8 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "final_residual": residual, "other_methods": others}
     if pcg is not None:
         line["pcg_c3"] = pcg
+        line["pcg_c1"] = c1
+        line["frames_c4"] = c4
     print(json.dumps(line), flush=True)
 
 

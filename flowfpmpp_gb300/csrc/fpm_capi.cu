@@ -524,6 +524,130 @@ static void jacobi_loop_df(const SolveArgs& a, const Dims& d, const double* src,
   *sweeps = sw;
 }
 
+// ---------------------------------------------------------------- triple-float Jacobi plan
+static std::map<std::tuple<int, int, int>, DfChoice> g_tf_cache;
+
+static JacobiTfPlan make_tf_plan(Scratch& A, const Dims& d) {
+  JacobiTfPlan pl;
+  std::memset(&pl, 0, sizeof(pl));
+  pl.nx = d.nx;
+  pl.ny = d.ny;
+  pl.nz = d.nz;
+  pl.px = ((long long)d.nx + 2 + 1) & ~1LL;
+  const size_t nphi = (size_t)pl.px * (d.ny + 2) * d.nz;
+  pl.a = A.get<double>(nphi);
+  pl.b = A.get<double>(nphi);
+  pl.sr = A.get<double>(2 * (size_t)d.ncell());
+  pl.coef = A.get<float4>(2 * (size_t)(d.nx + d.ny + d.nz));
+  pl.err = A.get<int>(1);
+  pl.shape = 0;
+  pl.kchunk = 8;
+  return pl;
+}
+
+// Tile shape and planes per CTA of the triple-float sweep: cached per grid
+// size; otherwise (unless FPM_TF_AUTOTUNE=0) five timed sweeps a -> b of each
+// candidate.  FPM_TF_SHAPE / FPM_TF_KCHUNK pin the choice.
+static void tf_choose(JacobiTfPlan& pl, cudaStream_t st) {
+  const Dims d{pl.nx, pl.ny, pl.nz};
+  const auto key = std::make_tuple(pl.nx, pl.ny, pl.nz);
+  if (const char* fs = std::getenv("FPM_TF_SHAPE")) {
+    pl.shape = std::atoi(fs) % jacobi_tf_num_shapes();
+    const char* fk = std::getenv("FPM_TF_KCHUNK");
+    pl.kchunk = fk ? std::atoi(fk) : 8;
+    if (pl.kchunk < 1) pl.kchunk = 1;
+    CUDA_TRY(jacobi_tf_encode(pl));
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tf_cache.find(key);
+    if (it != g_tf_cache.end()) {
+      pl.shape = it->second.shape;
+      pl.kchunk = it->second.kchunk;
+      CUDA_TRY(jacobi_tf_encode(pl));
+      return;
+    }
+  }
+  const char* env = std::getenv("FPM_TF_AUTOTUNE");
+  DfChoice best{0, std::min(8, d.nz)};
+  if (!(env && env[0] == '0')) {
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    for (int s = 0; s < jacobi_tf_num_shapes(); s++) {
+      for (const int kc : {4, 8, 16, 32}) {
+        if (kc > d.nz && kc != 4) continue;
+        pl.shape = s;
+        pl.kchunk = std::min(kc, d.nz);
+        CUDA_TRY(jacobi_tf_encode(pl));
+        CUDA_TRY(jacobi_tf_sweep(pl, pl.a, pl.b, st));
+        CUDA_TRY(cudaEventRecord(e0, st));
+        for (int r = 0; r < 5; r++) CUDA_TRY(jacobi_tf_sweep(pl, pl.a, pl.b, st));
+        CUDA_TRY(cudaEventRecord(e1, st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (verbose_level() >= 2) {
+          int tx, ty;
+          jacobi_tf_shape(s, &tx, &ty);
+          std::fprintf(stderr, "fpm tf autotune: shape %d tile %dx%d planes %d: %.1f us per sweep\n", s, tx, ty,
+                       pl.kchunk, 200.f * ms);
+        }
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = DfChoice{s, pl.kchunk};
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tf_cache[key] = best;
+  }
+  pl.shape = best.shape;
+  pl.kchunk = best.kchunk;
+  CUDA_TRY(jacobi_tf_encode(pl));
+}
+
+// The weighted-Jacobi iteration with FP64 storage and triple-float arithmetic:
+// phi lives in the TMA kernel's FP64 layout between checks and is unpacked
+// for each residual check.
+static void jacobi_loop_tf(const SolveArgs& a, const Dims& d, const double* src, const double* diag,
+                           const double* rdiag, const double* coef, const Coefs& c, Scratch& A, Common& cm,
+                           int* sweeps, cudaStream_t st) {
+  JacobiTfPlan pl = make_tf_plan(A, d);
+  CUDA_TRY(jacobi_tf_pack(pl, a.phi, src, rdiag, coef, st));
+  tf_choose(pl, st);
+  CUDA_TRY(cudaMemsetAsync(pl.err, 0, sizeof(int), st));
+  double *cur = pl.a, *oth = pl.b;
+  double residual = HUGE_VAL;
+  int sw = 0;
+  const int ci = a.ci < 1 ? 1 : a.ci;
+  while (sw < a.max_sweeps && residual > a.tol) {
+    int nsteps = ci < a.max_sweeps - sw ? ci : a.max_sweeps - sw;
+    {
+      TimedRun t(FPM_TIMER_JACOBI_TF, nsteps, st);
+      for (int s = 0; s < nsteps; s++) {
+        CUDA_TRY(jacobi_tf_sweep(pl, cur, oth, st));
+        std::swap(cur, oth);
+      }
+    }
+    sw += nsteps;
+    CUDA_TRY(jacobi_tf_unpack(pl, cur, a.phi, st));
+    CUDA_TRY(launch_operator_residual(d, a.phi, src, diag, c, cm.S, cm.rb, st));
+    residual = read_scalars(cm.S, st).res;
+    int h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&h, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (h) throw Error{FPM_E_TIMEOUT, "triple-float Jacobi pipeline wait timed out"};
+  }
+  *sweeps = sw;
+}
+
 // Mixed-precision PCG for 1..4 right-hand sides sharing the operator.
 // One FP32 diagonal PCG per right-hand side (batched in the same kernels)
 // whose residual is periodically replaced by the FP64 true residual -- the
@@ -1037,7 +1161,8 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
 // solve them one after the other; FPM_METHOD_PCG_MIXED solves them together.
 static bool valid_method(int m) {
   return m == FPM_METHOD_PCG || m == FPM_METHOD_JACOBI || m == FPM_METHOD_JACOBI_DF || m == FPM_METHOD_PCG_MIXED ||
-         m == FPM_METHOD_PCG_MG || m == FPM_METHOD_FCG_LEARNED || m == FPM_METHOD_JACOBI_FMA;
+         m == FPM_METHOD_PCG_MG || m == FPM_METHOD_FCG_LEARNED || m == FPM_METHOD_JACOBI_FMA ||
+         m == FPM_METHOD_JACOBI_TF;
 }
 
 // FPM_METHOD_FCG_LEARNED: FP64 flexible CG (Notay's FCG(1): the Polak-Ribiere
@@ -1249,6 +1374,8 @@ static void solve_multi_dev(int nrhs, const SolveArgs* args, int* sweeps, double
         if (a.method == FPM_METHOD_PCG) pcg_loop(a, d, next, src[m], diag, rdiag, c, A, cm, &sweeps[m], st);
         else if (a.method == FPM_METHOD_JACOBI || a.method == FPM_METHOD_JACOBI_FMA)
           jacobi_loop_f64(a, d, next, src[m], diag, rdiag, c, cm, &sweeps[m], st);
+        else if (a.method == FPM_METHOD_JACOBI_TF)
+          jacobi_loop_tf(a, d, src[m], diag, rdiag, coef, c, A, cm, &sweeps[m], st);
         else jacobi_loop_df(a, d, src[m], diag, rdiag, coef, c, A, cm, &sweeps[m], st);
       }
     }
@@ -1779,8 +1906,9 @@ int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, con
     if (!a || !b || !src || !rdiag || !xc || !yc || !zc || !dx || !dy || !dz) throw Error{FPM_E_ARG, "null argument"};
     if (nx < 1 || ny < 1 || nz < 1) throw Error{FPM_E_SIZE, "empty grid"};
     if (nsweeps < 0) throw Error{FPM_E_ARG, "nsweeps must be >= 0"};
-    if (method != FPM_METHOD_JACOBI && method != FPM_METHOD_JACOBI_DF && method != FPM_METHOD_JACOBI_FMA)
-      throw Error{FPM_E_METHOD, "sweeps need method jacobi, jacobi_df or jacobi_fma"};
+    if (method != FPM_METHOD_JACOBI && method != FPM_METHOD_JACOBI_DF && method != FPM_METHOD_JACOBI_FMA &&
+        method != FPM_METHOD_JACOBI_TF)
+      throw Error{FPM_E_METHOD, "sweeps need method jacobi, jacobi_fma, jacobi_tf or jacobi_df"};
     require_device();
     cudaStream_t st = (cudaStream_t)stream;
     const Dims d{nx, ny, nz};
@@ -1797,6 +1925,26 @@ int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, con
                                                  : launch_jacobi_f64(d, cur, oth, src, rdiag, c, st));
         std::swap(cur, oth);
       }
+    } else if (method == FPM_METHOD_JACOBI_TF) {
+      JacobiTfPlan pl = make_tf_plan(A, d);
+      CUDA_TRY(jacobi_tf_pack(pl, a, src, rdiag, coef, st));
+      tf_choose(pl, st);
+      CUDA_TRY(cudaMemsetAsync(pl.err, 0, sizeof(int), st));
+      CUDA_TRY(jacobi_tf_pack(pl, a, src, rdiag, coef, st));  // the autotuner overwrote b
+      double *cur = pl.a, *oth = pl.b;
+      {
+        TimedRun t(FPM_TIMER_JACOBI_TF, nsweeps, st);
+        for (int s = 0; s < nsweeps; s++) {
+          CUDA_TRY(jacobi_tf_sweep(pl, cur, oth, st));
+          std::swap(cur, oth);
+        }
+      }
+      CUDA_TRY(jacobi_tf_unpack(pl, pl.a, a, st));
+      CUDA_TRY(jacobi_tf_unpack(pl, pl.b, b, st));
+      int h = 0;
+      CUDA_TRY(cudaMemcpyAsync(&h, pl.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      if (h) throw Error{FPM_E_TIMEOUT, "triple-float Jacobi pipeline wait timed out"};
     } else {
       JacobiDfPlan pl = make_df_plan(A, d);
       CUDA_TRY(jacobi_df_pack(pl, a, src, rdiag, coef, st));

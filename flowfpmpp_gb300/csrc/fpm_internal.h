@@ -122,6 +122,30 @@ void jacobi_df_shape(int shape, int* tx, int* ty);
 cudaError_t jacobi_df_sweep(const JacobiDfPlan& pl, const float2* src_phi, float2* dst_phi, cudaStream_t st);
 cudaError_t jacobi_df_unpack(const JacobiDfPlan& pl, const float2* cur, double* phi, cudaStream_t st);
 
+// TMA-streamed Jacobi with FP64 storage and triple-float arithmetic
+// (fpm_jacobi_tf.cu); the same pipeline as the double-float plan.
+struct JacobiTfPlan {
+  int nx, ny, nz;
+  long long px;      // x pitch (elements) of the internal phi layout, even
+  int kchunk;        // planes per CTA along z
+  int shape;         // index into the tile-shape table
+  double *a, *b;     // internal phi buffers, px * (ny+2) * nz
+  double* sr;        // (src, rdiag) pairs, 2 * nx * ny * nz
+  float4* coef;      // cw, ce, cs, cn, cb, ct as three FP32 limbs
+  float4 point2;     // 0.2 as three FP32 limbs
+  int* err;          // set to 1 if a pipeline wait timed out
+  CUtensorMap tm_a, tm_b, tm_sr;
+};
+int jacobi_tf_num_shapes();
+void jacobi_tf_shape(int shape, int* tx, int* ty);
+cudaError_t jacobi_tf_pack(JacobiTfPlan& pl, const double* phi, const double* src, const double* rdiag,
+                           const double* coef64, cudaStream_t st);
+cudaError_t jacobi_tf_encode(JacobiTfPlan& pl);
+cudaError_t jacobi_tf_sweep(const JacobiTfPlan& pl, const double* src_phi, double* dst_phi, cudaStream_t st);
+cudaError_t jacobi_tf_unpack(const JacobiTfPlan& pl, const double* cur, double* phi, cudaStream_t st);
+bool tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint64_t d0, uint64_t d1, uint64_t d2,
+                   uint64_t stride1_bytes, uint64_t stride2_bytes, uint32_t b0, uint32_t b1);
+
 // Mixed-precision multi-right-hand-side PCG (fpm_pcg_mixed.cu).
 constexpr int kMaxRhs = 4;
 // FP32 vector layout: cell (i, j, k), i in [0, nx+1], j in [0, ny+1], k in

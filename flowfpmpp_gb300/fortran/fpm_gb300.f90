@@ -159,6 +159,7 @@ contains
       case ('pcg_mixed'); m = 3
       case ('pcg_mg'); m = 4
       case ('jacobi_fma'); m = 6
+      case ('jacobi_tf'); m = 7
       case default; error stop 'stair-step method must be pcg or jacobi'
       end select
     end if

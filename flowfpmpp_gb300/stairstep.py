@@ -19,7 +19,7 @@ import numpy as np
 
 from ._lib import check, lib
 
-METHODS = {"pcg": 0, "jacobi": 1, "jacobi_df": 2, "pcg_mixed": 3, "pcg_mg": 4, "fcg_learned": 5, "jacobi_fma": 6}
+METHODS = {"pcg": 0, "jacobi": 1, "jacobi_df": 2, "pcg_mixed": 3, "pcg_mg": 4, "fcg_learned": 5, "jacobi_fma": 6, "jacobi_tf": 7}
 
 _D = ctypes.c_double
 _I = ctypes.c_int
@@ -93,7 +93,8 @@ def solve_stairstep_poisson_3d(phi, rhs, solid, body_grad, xlo, xhi, ylo, yhi, z
     """src/fpm_stairstep_mpi_3d.f90:106-330.  Solves in place (``phi`` is the
     initial guess) and returns ``(sweeps, residual)``.  ``method`` is 'pcg'
     (default), 'jacobi', 'jacobi_fma' (the same weighted Jacobi in FP64 with
-    fused multiply-adds), 'jacobi_df' (in double-float arithmetic),
+    fused multiply-adds), 'jacobi_tf' (FP64 storage, triple-float arithmetic),
+    'jacobi_df' (in double-float arithmetic),
     'pcg_mixed' (FP32 PCG inside FP64 iterative refinement) or 'pcg_mg' (the
     refinement with a multigrid-preconditioned FP32 PCG)."""
     nx, ny, nz = rhs.shape

@@ -68,6 +68,9 @@ extern "C" {
 #define FPM_METHOD_JACOBI_FMA 6 /* weighted Jacobi 0.2/0.8 in FP64 storage and arithmetic with fused multiply-adds
                                    (the reference's summation order, one rounding per multiply-add); differs
                                    from FPM_METHOD_JACOBI in the last bits, twice as fast on GB300's FP64 pipe */
+#define FPM_METHOD_JACOBI_TF 7  /* weighted Jacobi 0.2/0.8 with FP64 storage and triple-float arithmetic on the
+                                   FP32 pipe: inputs split exactly into three FP32 limbs, products and sums
+                                   error-free down to about 2^-60 relative, each result rounded to FP64 */
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char* fpm_last_error(void);
@@ -82,7 +85,8 @@ int fpm_version(void);
 #define FPM_TIMER_PCG_ITER 2    /* one FP64 PCG iteration (three kernels) */
 #define FPM_TIMER_PCG_MIXED_ITER 3 /* one FP32 inner PCG iteration over all right-hand sides */
 #define FPM_TIMER_FRAMES_ITER 4 /* one batched FP32 PCG iteration over every frame of a 2-D batch */
-#define FPM_TIMER_COUNT 5
+#define FPM_TIMER_JACOBI_TF 5    /* Jacobi sweep with FP64 storage and triple-float arithmetic (TMA-streamed) */
+#define FPM_TIMER_COUNT 6
 int fpm_timing_enable(int on);
 /* Number of kernels this library has launched in this process. */
 long long fpm_kernel_launches(void);
@@ -303,8 +307,10 @@ int fpm_stairstep_build_operator_dev(const double* rhs, const int32_t* solid, co
  * alternating a -> b -> a ...  (padded arrays with zero physical halo and
  * zero solid cells, as after the solver's init loop).  The latest iterate is
  * in a when nsweeps is even, else in b.  method FPM_METHOD_JACOBI (FP64,
- * bit-identical per sweep) or FPM_METHOD_JACOBI_DF (double-float arithmetic;
- * a and b are converted in and out once per call). */
+ * bit-identical per sweep), FPM_METHOD_JACOBI_FMA (FP64 with fused
+ * multiply-adds), FPM_METHOD_JACOBI_TF (FP64 storage, triple-float
+ * arithmetic) or FPM_METHOD_JACOBI_DF (double-float arithmetic; for the last
+ * two, a and b are copied into and out of the kernel's layout once per call). */
 int fpm_stairstep_jacobi_sweeps_dev(double* a, double* b, const double* src, const double* rdiag, const double* xc,
                                     const double* yc, const double* zc, const double* dx, const double* dy,
                                     const double* dz, int nx, int ny, int nz, int nsweeps, int method, void* stream);
@@ -325,7 +331,9 @@ int fpm_stairstep_operator_residual_dev(const double* phi, const double* src, co
  * (cudaGetSymbolAddress) with that device current; make that first call
  * before any stream capture.  All calls share the array, so calls whose GPU
  * work overlaps (different streams or host threads) race: serialise them.
- * Same arguments and result as fpm_stairstep_operator_residual_dev. */
+ * Same arguments and result as fpm_stairstep_operator_residual_dev; like it,
+ * the call copies the result to *value and waits for the stream before it
+ * returns. */
 int fpm_stairstep_operator_residual_noalloc_dev(const double* phi, const double* src, const double* diag,
                                                 const double* xc, const double* yc, const double* zc,
                                                 const double* dx, const double* dy, const double* dz, int nx, int ny,

@@ -128,13 +128,94 @@ def test_fma_sweeps_within_1e12_after_2000(gpu_lib):
     assert abs(out_g["res"] - out_o["res"]) <= 1e-9 * out_o["res"]
 
 
-@pytest.mark.parametrize("method", ["jacobi", "jacobi_fma", "jacobi_df", "pcg"])
+def test_tf_sweeps_within_1e12_after_2000(gpu_lib):
+    """FP64-storage triple-float sweeps stay within 1e-12 relative of the
+    separately rounded FP64 oracle after 2000 sweeps (a bound the FP64 oracle
+    itself only meets to its own rounding)."""
+    c = stairstep_case_exact(False)
+    out_g = gpu_run(c, "jacobi_tf", -1.0, 2000, ci=2000)
+    out_o = cpu_run(c, "jacobi", -1.0, 2000, ci=2000)
+    assert out_g["sweeps"] == 2000
+    assert rel_linf(out_g["phi"], out_o["phi"]) <= 1e-12
+    assert abs(out_g["res"] - out_o["res"]) <= 1e-9 * out_o["res"]
+
+
+def _sweep_longdouble(a, src, rdiag, coefs, nx, ny, nz):
+    """One weighted-Jacobi sweep (src/fpm_stairstep_mpi_3d.f90:384-399)
+    evaluated in numpy's long double (64- or 113-bit significand), rounded to
+    FP64 at the end: the reference the triple-float sweep is held to."""
+    L = np.longdouble
+    A = a.astype(L)
+    cw, ce, cs, cn, cb, ct = (np.asarray(x, dtype=L) for x in coefs)
+    s = src.astype(L)
+    s = s + cw[:, None, None] * A[0:nx, 1:ny + 1, :]
+    s = s + ce[:, None, None] * A[2:nx + 2, 1:ny + 1, :]
+    s = s + cs[None, :, None] * A[1:nx + 1, 0:ny, :]
+    s = s + cn[None, :, None] * A[1:nx + 1, 2:ny + 2, :]
+    kb = [max(k - 1, 0) for k in range(nz)]
+    kt = [min(k + 1, nz - 1) for k in range(nz)]
+    s = s + cb[None, None, :] * A[1:nx + 1, 1:ny + 1, kb]
+    s = s + ct[None, None, :] * A[1:nx + 1, 1:ny + 1, kt]
+    b = L(0.2) * A[1:nx + 1, 1:ny + 1, :] + rdiag.astype(L) * s
+    # magnitude of the terms, for cells where the sum cancels
+    m = np.abs(src) + np.abs(cw[:, None, None] * A[0:nx, 1:ny + 1, :]).astype(np.float64)
+    for part in (ce[:, None, None] * A[2:nx + 2, 1:ny + 1, :], cs[None, :, None] * A[1:nx + 1, 0:ny, :],
+                 cn[None, :, None] * A[1:nx + 1, 2:ny + 2, :], cb[None, None, :] * A[1:nx + 1, 1:ny + 1, kb],
+                 ct[None, None, :] * A[1:nx + 1, 1:ny + 1, kt]):
+        m = m + np.abs(part).astype(np.float64)
+    mag = 0.2 * np.abs(a[1:nx + 1, 1:ny + 1, :]) + np.abs(rdiag) * m
+    return b.astype(np.float64), mag
+
+
+def test_tf_sweep_rounds_like_wider_arithmetic(gpu_lib):
+    """One sweep from a random field: the triple-float result is within one
+    FP64 ulp of the long-double evaluation rounded to FP64 in every cell, and
+    on average closer to it than the separately rounded FP64 sweep."""
+    if np.finfo(np.longdouble).nmant <= 52:
+        pytest.skip("numpy long double is FP64 on this host")
+    c = stairstep_case_exact(False)
+    nx, ny, nz = c["nx"], c["ny"], c["nz"]
+    faces = [f.copy(order="F") for f in c["faces"]]
+    orc.enforce_stairstep_compatibility_3d(c["rhs"], c["solid"], c["body"], *faces, c["dx"], c["dy"], c["dz"])
+    coefs = orc.stairstep_coefficients(c["xc"], c["yc"], c["zc"], c["dx"], c["dy"], c["dz"])
+    src, diag, rdiag, _ = orc.build_operator(c["rhs"], c["solid"], c["body"], *faces, coefs, c["dx"], c["dy"],
+                                             c["dz"], False)
+    rng = np.random.default_rng(11)
+    a = np.zeros((nx + 2, ny + 2, nz), order="F")
+    a[1:nx + 1, 1:ny + 1, :] = rng.standard_normal((nx, ny, nz)) * (c["solid"][1:nx + 1, 1:ny + 1, :] == 0)
+    b = a.copy(order="F")
+    ga, gb = to_dev(a), to_dev(b)
+    dsrc, drd = to_dev(src), to_dev(rdiag)
+    dax = [to_dev(c[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    rc = gpu_lib.fpm_stairstep_jacobi_sweeps_dev(ptr(ga), ptr(gb), ptr(dsrc), ptr(drd), *[ptr(x) for x in dax],
+                                                 I(nx), I(ny), I(nz), I(1), I(7), stream_ptr())
+    assert rc == 0, gpu_lib.fpm_last_error()
+    tf = from_dev(gb, a.shape)[1:nx + 1, 1:ny + 1, :]
+    ref, mag = _sweep_longdouble(a, src, rdiag, coefs, nx, ny, nz)
+    b64 = a.copy(order="F")
+    orc.jacobi_sweep(a, b64, src, rdiag, coefs)
+    f64 = b64[1:nx + 1, 1:ny + 1, :]
+    ulp = np.spacing(np.abs(ref))
+    err_tf = np.abs(tf - ref) / ulp
+    err_64 = np.abs(f64 - ref) / ulp
+    # within one ulp where the sum does not cancel by more than 2^6; elsewhere
+    # within one ulp plus 2^-55 of the terms' magnitude (the separately
+    # rounded FP64 sweep is off by up to 11 x 2^-55 of it on this field)
+    plain = np.abs(ref) >= mag / 64
+    assert err_tf[plain].max() <= 1.0, err_tf[plain].max()
+    assert (np.abs(tf - ref) <= ulp + 2.0 ** -55 * mag).all()
+    assert err_tf.mean() < err_64.mean(), (err_tf.mean(), err_64.mean())
+    print(f"ulps from the long-double sweep: triple-float max {err_tf.max():.1f} mean {err_tf.mean():.3f}, "
+          f"separately rounded FP64 max {err_64.max():.1f} mean {err_64.mean():.3f}")
+
+
+@pytest.mark.parametrize("method", ["jacobi", "jacobi_fma", "jacobi_tf", "jacobi_df", "pcg"])
 def test_exact_linear_solution_gpu(gpu_lib, method):
     """The reference's exactness test (test_stairstep_exact_3d.f90:40-50) on the GPU."""
     c = stairstep_case_exact(True)
     # The double-float iterate carries a 48-bit significand, so its max-norm
     # residual floors near 1e-11 on this grid; it is held to the PCG tolerance.
-    tol = 1e-12 if method in ("jacobi", "jacobi_fma") else 1e-10
+    tol = 1e-12 if method in ("jacobi", "jacobi_fma", "jacobi_tf") else 1e-10
     g = gpu_run(c, method, tol, 400000)
     gx, gy, gz, vortex, adv, totals = g["terms"]
     errors, ierr = exact_expectations(c, g["phi"], gx, gy, gz, vortex, totals)

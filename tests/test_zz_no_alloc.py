@@ -79,6 +79,34 @@ def test_no_alloc_residual_matches_allocating_entry_point(gpu_lib):
     assert ref2 > 0 and new2 == ref2 and ref2 != ref1
 
 
+def test_no_alloc_residual_leaves_free_device_memory_unchanged(gpu_lib):
+    """The property the entry point exists for: after a first call (which
+    loads the kernels and looks the scratch address up), further calls do not
+    change the device's free memory."""
+    import torch
+    c2, phi2 = _case(53, 17, 9, seed=5)
+    src2, diag2 = _operator(c2)
+    nx, ny, nz = c2["nx"], c2["ny"], c2["nz"]
+    dphi, dsrc, ddiag = to_dev(phi2), to_dev(src2), to_dev(diag2)
+    dax = [to_dev(c2[k]) for k in ("xc", "yc", "zc", "dx", "dy", "dz")]
+    v = D()
+
+    def call():
+        rc = gpu_lib.fpm_stairstep_operator_residual_noalloc_dev(ptr(dphi), ptr(dsrc), ptr(ddiag),
+                                                                 *[ptr(x) for x in dax], I(nx), I(ny), I(nz),
+                                                                 ctypes.byref(v), stream_ptr())
+        assert rc == 0, gpu_lib.fpm_last_error()
+        return v.value
+
+    first = call()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    values = [call() for _ in range(3)]
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert all(x == first for x in values)
+
+
 def test_no_alloc_rejects_sizes_beyond_its_limit(gpu_lib):
     c = stairstep_case_exact(False)
     src, diag = _operator(c)
