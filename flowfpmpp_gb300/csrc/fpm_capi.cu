@@ -2395,6 +2395,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     CUDA_TRY(cudaMemsetAsync(b.iters, 0, nq * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(b.active, 0, nq * sizeof(int), st));
     b.tol2 = kUpdateDrop * kUpdateDrop;  // each (frame, direction) stops its FP32 iteration at the update drop
+                                         // (the multigrid method sets its own below)
     b.pmul = A.get<double>(nq);
     b.keep = A.get<int>(nq);
     b.dir = A.get<int>(nq);
@@ -2427,11 +2428,15 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     const int chunk_len = check_interval < 1 ? 1 : check_interval;
     long long total = 0;
     ChunkGraphs graphs;
+    // 10 % margin: the final residual pass after the gauge re-evaluates the
+    // potentials with a different summation order, which near the FP64 floor
+    // can move the max-norm by ~1e-3 relative
+    const double target = 0.9 * tolerance;
     std::vector<double> best(res), prev(res), pmul(nq, 0.0), rz(nq), rz0(nq);
     std::vector<int> live(nq), since(nq, 0), keepv(nq, 0), slow(nq, 0), to64(nq, 0), extra_its(nq, 0);
     bool any = false;
     for (size_t q = 0; q < nq; q++) {
-      live[q] = res[q] > tolerance && res[q] == res[q];
+      live[q] = res[q] > target && res[q] == res[q];
       set[q] = live[q];
       scale[q] = res[q] > 0 ? 1.0 / res[q] : 1.0;
       any = any || live[q];
@@ -2439,11 +2444,90 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     // Frame method: the batched FP32 diagonal PCG above, or (multigrid)
     // every (frame, direction) solved on its own by the multigrid-
     // preconditioned refinement, several at once on worker streams.
-    const int frames_mg = [] {
+    // Frame method: every frame's pair in the same launches with the batched
+    // 2-D multigrid preconditioner (default), the same with the diagonal
+    // preconditioner (FPM_FRAMES_METHOD=batched), or every pair solved on its
+    // own by the multigrid-preconditioned refinement on worker streams
+    // (FPM_FRAMES_METHOD=individual).
+    const int fmethod = [] {
       const char* e = std::getenv("FPM_FRAMES_METHOD");
-      return (e && std::strcmp(e, "batched") == 0) ? 0 : 1;
+      if (e && std::strcmp(e, "batched") == 0) return 0;
+      if (e && std::strcmp(e, "individual") == 0) return 1;
+      return 2;
     }();
-    int individual_method = FPM_METHOD_PCG;
+    const int frames_mg = fmethod == 1;
+    const bool batched_mg = fmethod == 2;
+    int individual_method = batched_mg ? FPM_METHOD_PCG_MG : FPM_METHOD_PCG;
+    const double drop2 = batched_mg ? kMgDrop * kMgDrop : kUpdateDrop * kUpdateDrop;
+    b.tol2 = drop2;
+    // the multigrid hierarchy of every frame
+    FramesMg M;
+    std::memset(&M, 0, sizeof(M));
+    std::vector<int> nrestrict_lv(kFmMaxLevels, 0), nall_lv(kFmMaxLevels, 0);
+    if (batched_mg) {
+      Trace tm("frames: multigrid set-up");
+      std::vector<int> nlev(nframes);
+      std::vector<FmLevel> lv((size_t)nframes * kFmMaxLevels, FmLevel{0, 0, 0});
+      std::vector<long long> pool(kFmMaxLevels, 0);
+      int maxlev = 0;
+      for (int f = 0; f < nframes; f++) {
+        int nxl = fr[f].nx, nyl = fr[f].ny, l = 0;
+        lv[(size_t)f * kFmMaxLevels] = FmLevel{nxl, nyl, fr[f].o2};
+        while (l + 1 < kFmMaxLevels && (l < 1 || nxl > kFmCoarseSide || nyl > kFmCoarseSide)) {
+          nxl = (nxl + 1) / 2;
+          nyl = (nyl + 1) / 2;
+          l++;
+          lv[(size_t)f * kFmMaxLevels + l] = FmLevel{nxl, nyl, pool[l]};
+          pool[l] += (long long)nxl * nyl;
+        }
+        if (nxl > kFmCoarseSide || nyl > kFmCoarseSide)
+          throw Error{FPM_E_LIMIT, "frame too large for the multigrid hierarchy"};
+        nlev[f] = l + 1;
+        maxlev = std::max(maxlev, l + 1);
+      }
+      M.nlev = maxlev;
+      M.omega = (float)env_double("FPM_FRAMES_OMEGA", 0.9);
+      M.coarse_sweeps = (int)env_double("FPM_FRAMES_COARSE_SWEEPS", 60);
+      M.cscale = (float)env_double("FPM_FRAMES_CSCALE", 1.0);
+      M.lv = A.upload(lv.data(), lv.size());
+      M.nlevels = A.upload(nlev.data(), nlev.size());
+      for (int l = 1; l < maxlev; l++) {
+        // tiles of the frames that have level l: those for which it is not the
+        // coarsest first (restriction and prolongation walk that prefix)
+        std::vector<FmTile> tl;
+        for (int pass = 0; pass < 2; pass++)
+          for (int f = 0; f < nframes; f++) {
+            if (nlev[f] <= l) continue;
+            const bool coarsest = nlev[f] - 1 == l;
+            if (coarsest != (pass == 1)) continue;
+            const FmLevel& L = lv[(size_t)f * kFmMaxLevels + l];
+            for (int j0 = 0; j0 < L.ny; j0 += 8)
+              for (int i0 = 0; i0 < L.nx; i0 += 32) tl.push_back(FmTile{f, i0, j0});
+            if (pass == 0) nrestrict_lv[l] = (int)tl.size();
+          }
+        nall_lv[l] = (int)tl.size();
+        M.tiles[l] = A.upload(tl.data(), tl.size());
+        M.te[l] = A.get<float>(pool[l]);
+        M.tn[l] = A.get<float>(pool[l]);
+        M.dinv[l] = A.get<float>(pool[l]);
+        for (int r = 0; r < 2; r++) {
+          M.b[l][r] = A.get<float>(pool[l]);
+          M.xa[l][r] = A.get<float>(pool[l]);
+          M.xb[l][r] = A.get<float>(pool[l]);
+        }
+      }
+      M.te[0] = A.get<float>(n2);
+      M.tn[0] = A.get<float>(n2);
+      M.dinv[0] = A.get<float>(n2);
+      for (int r = 0; r < 2; r++) {
+        M.r[r] = A.get<float>(n2);
+        M.z[r] = A.get<float>(n2);
+        M.p[r] = A.get<float>(n2);
+        M.q[r] = A.get<float>(n2);
+        M.e[r] = A.get<float>(n2);
+      }
+      CUDA_TRY(fm_setup(dfr, dtf, ntiles, b, M, nall_lv.data(), st));
+    }
     if (frames_mg) {
       for (size_t q = 0; q < nq; q++) {
         to64[q] = live[q];
@@ -2456,7 +2540,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       push_set();
       CUDA_TRY(cudaMemcpyAsync(b.scale, scale.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
       CUDA_TRY(cudaMemcpyAsync(b.pmul, pmul.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
-      CUDA_TRY(launch_k_b2_start(dfr, dtf, ntiles, b, st));
+      if (batched_mg) CUDA_TRY(fm_start(dfr, dtf, ntiles, b, M, nrestrict_lv.data(), nframes, st));
+      else CUDA_TRY(launch_k_b2_start(dfr, dtf, ntiles, b, st));
     };
     if (any) push_start();
     // The iteration kernels run over the tiles of the frames that still have
@@ -2484,12 +2569,28 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       graphs.clear();
     };
     rebuild_tiles();
+    // With the batched multigrid, the last pairs (the frames whose aggregates
+    // straddle the body converge slowly) leave the batch when at most this
+    // fraction of the pairs is still iterating: each is then solved on its
+    // own, several at once, instead of the whole batch's launches running
+    // for a few frames.
+    const double tail = batched_mg ? env_double("FPM_FRAMES_TAIL", 0.2) : 0.0;
+    int nlive0 = 0;
+    for (size_t q = 0; q < nq; q++) nlive0 += live[q];
     while (any && total < max_sweeps) {
+      if (tail > 0) {
+        int nlive = 0;
+        for (size_t q = 0; q < nq; q++) nlive += live[q];
+        if (nlive <= tail * nlive0) break;
+      }
       int chunk = chunk_len;
       if (chunk > max_sweeps - total) chunk = (int)(max_sweeps - total);
       {
         TimedRun t(FPM_TIMER_FRAMES_ITER, chunk, st);
-        graphs.run(chunk, st, [&](cudaStream_t s2) { CUDA_TRY(launch_b2_iteration(dfr, dtf, nact, bi, s2)); });
+        graphs.run(chunk, st, [&](cudaStream_t s2) {
+          if (batched_mg) CUDA_TRY(fm_iteration(dfr, dtf, nact, bi, M, nrestrict_lv.data(), nframes, s2));
+          else CUDA_TRY(launch_b2_iteration(dfr, dtf, nact, bi, s2));
+        });
       }
       total += chunk;
       pull(act.data(), b.active, nq * sizeof(int));
@@ -2500,7 +2601,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         set[q] = 0;
         if (!live[q]) continue;
         since[q] += chunk;
-        const bool dropped = rz[q] <= kUpdateDrop * kUpdateDrop * rz0[q];
+        const bool dropped = rz[q] <= drop2 * rz0[q];
         const bool broke = !act[q] && !dropped;
         if (broke || dropped || since[q] >= kUpdateMax || total >= max_sweeps) {
           set[q] = 1;
@@ -2510,7 +2611,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       }
       if (!upd) continue;
       push_set();  // apply with the scales the corrections were computed in
-      CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
+      if (batched_mg) CUDA_TRY(fm_apply(dfr, dtf, ntiles, b, M, st));
+      else CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
       CUDA_TRY(launch_k_b2_tres(dfr, dtf, ntiles, b, st));
       pull(res.data(), b.res, nq * sizeof(double));
       {
@@ -2549,8 +2651,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
                          res[q], prev[q], act[q] ? "" : "breakdown ", restart ? "restart" : "keep");
           slow[q] = res[q] * kSlowGain > prev[q] ? slow[q] + 1 : 0;
           prev[q] = res[q];
-          const bool hand_over = slow[q] >= kSlowUpdates && res[q] > tolerance;
-          if (!(res[q] > tolerance) || !(res[q] == res[q]) || stall[q] >= kStallUpdates || hand_over) {
+          const bool hand_over = slow[q] >= kSlowUpdates && res[q] > target;
+          if (!(res[q] > target) || !(res[q] == res[q]) || stall[q] >= kStallUpdates || hand_over) {
             live[q] = 0;
             set[q] = 0;
             act[q] = 0;
@@ -2592,7 +2694,12 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     }
     if (pend) {
       push_set();
-      CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
+      if (batched_mg) CUDA_TRY(fm_apply(dfr, dtf, ntiles, b, M, st));
+      else CUDA_TRY(launch_k_b2_apply(dfr, dtf, ntiles, b, st));
+      // the batch's tail: solved on its own from the current phi
+      if (batched_mg)
+        for (size_t q = 0; q < nq; q++)
+          if (live[q]) to64[q] = 1;
     }
     // (frame, direction) pairs solved on their own: with the multigrid frame
     // method all of them; otherwise those whose FP32 iteration stagnated

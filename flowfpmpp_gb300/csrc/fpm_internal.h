@@ -242,6 +242,38 @@ B2_DECL(k_b2_part1)
 B2_DECL(k_b2_part2)
 cudaError_t launch_b2_iteration(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, cudaStream_t st);
 
+// Batched 2-D multigrid preconditioner of the frames (fpm_frames_mg.cu).
+constexpr int kFmMaxLevels = 12;
+constexpr int kFmMaxCoarse = 1024;  // threads of the coarsest-level kernel (cells of a 32 x 32 level)
+constexpr int kFmCoarseSide = 8;    // a frame's coarsest level has at most this many cells per side
+struct FmLevel {
+  int nx, ny;
+  long long off;  // offset of the frame's level in the level's pools (level 0: Frame2::o2)
+};
+struct FmTile {
+  int f, i0, j0;  // frame and 0-based origin of a 32 x 8 tile
+};
+struct FramesMg {
+  int nlev;                              // levels of the deepest frame
+  const FmLevel* lv;                     // [frame * kFmMaxLevels + level]
+  const int* nlevels;                    // levels per frame (>= 2; the last one is the coarsest)
+  const FmTile* tiles[kFmMaxLevels];     // level >= 1: frames whose level is not their coarsest first
+  float *te[kFmMaxLevels], *tn[kFmMaxLevels], *dinv[kFmMaxLevels];  // faces east / north, omega / diag
+  float *b[kFmMaxLevels][2], *xa[kFmMaxLevels][2], *xb[kFmMaxLevels][2];  // levels >= 1, per direction
+  float *r[2], *z[2], *p[2], *q[2], *e[2];  // level 0 (2-D frame layout), per direction
+  float omega;
+  float cscale;  // scale of the prolonged coarse correction (the cycle stays symmetric)
+  int coarse_sweeps;
+};
+cudaError_t fm_setup(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
+                     const int* ntiles_lv, cudaStream_t st);
+cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
+                     const int* nrestrict_lv, int nframes, cudaStream_t st);
+cudaError_t fm_iteration(const Frame2* fr, const int* tf, int nact, const Batch2& b, const FramesMg& M,
+                         const int* nrestrict_lv, int nframes, cudaStream_t st);
+cudaError_t fm_apply(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
+                     cudaStream_t st);
+
 // ---- no-body Neumann solvers and densities (fpm_laplace.cu) --------------
 cudaError_t launch_neumann_compat(int nx, int ny, int nz, const double* rhs, Faces f, const double* dx,
                                   const double* dy, const double* dz, int uniform, double area_uniform,
