@@ -28,8 +28,8 @@
 //
 // Values with magnitude below 2^-74 keep only their leading limb(s) (their
 // relative precision drops; the absolute error stays below 2^-98); magnitudes
-// of 2^127 and above take the FP64-rate conversion (they never occur in a
-// stair-step solve).
+// of 2^127 and above become infinities (they never occur in a stair-step
+// solve); NaN stays NaN.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -53,12 +53,13 @@ __device__ __forceinline__ Limbs split3(double x) {
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
   const int e = (int)((hi32 >> 20) & 0x7FFu);
   Limbs r{0.f, 0.f, 0.f};
+  const unsigned sign = hi32 & 0x80000000u;
   if (e < 897) return r;  // zero, or below 2^-126
-  if (e > 1150) {         // 2^127 and above, infinities, NaN
-    r.h = __double2float_rn(x);
+  if (e > 1150) {         // 2^127 and above: infinity; NaN stays NaN (bit operations, no conversion)
+    const bool nan = e == 2047 && ((hi32 & 0xFFFFFu) | lo32) != 0u;
+    r.h = __uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u));
     return r;
   }
-  const unsigned sign = hi32 & 0x80000000u;
   r.h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29));
   const unsigned rem = lo32 & 0x1FFFFFFFu;  // 29 bits below h
   // n as an exact FP32 integer: (2^23 + n) - 2^23 for n < 2^23
@@ -73,13 +74,17 @@ __device__ __forceinline__ Limbs split3(double x) {
   return r;
 }
 
-// FP32 -> FP64 by bit assembly (exact; zero and subnormals give a signed zero).
+// FP32 -> FP64 by bit assembly (exact; zero and subnormals give a signed zero;
+// infinities and NaN map to themselves).  Only integer operations: the
+// conversion instruction runs on the FP64 pipe, and even a rarely taken
+// branch to it is predicated into every call.
 __device__ __forceinline__ double f32_bits_to_f64(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xFFu;
-  if (e == 0xFFu) return (double)f;
   const unsigned sign = u & 0x80000000u;
-  const unsigned hi = e == 0u ? sign : sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+  // exponent: zero/subnormal -> 0, infinity/NaN -> 2047, else rebiased
+  const unsigned eo = e == 0u ? 0u : (e == 0xFFu ? 2047u : e + 896u);
+  const unsigned hi = e == 0u ? sign : sign | (eo << 20) | ((u & 0x7FFFFFu) >> 3);
   const unsigned lo = e == 0u ? 0u : (u << 29);
   return __hiloint2double((int)hi, (int)lo);
 }

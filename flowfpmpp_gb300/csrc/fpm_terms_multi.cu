@@ -25,18 +25,19 @@ namespace {
 // FP64 -> (hi, lo) with hi the FP64 value truncated to 24 bits and lo the
 // next 23 bits of the remainder: hi + lo is within 2^-46 relative of x.
 // Integer and FP32 operations only.  Magnitudes below 2^-126 become zero (far below
-// any tolerance of the densities); magnitudes of 2^127 and above, infinities
-// and NaN take the FP64-rate conversion so that they propagate.
+// any tolerance of the densities); magnitudes of 2^127 and above become
+// infinities and NaN stays NaN.  (The conversion instructions run on the FP64
+// pipe, and even a rarely taken branch to one is predicated into every call.)
 __device__ __forceinline__ float2 split_f64(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
   const int e = (int)((hi32 >> 20) & 0x7FFu);
-  if (e < 897) return make_float2(0.f, 0.f);
-  if (e > 1150) {
-    const float h = __double2float_rz(x);
-    return make_float2(h, 0.f);
-  }
   const unsigned sign = hi32 & 0x80000000u;
+  if (e < 897) return make_float2(0.f, 0.f);
+  if (e > 1150) {  // 2^127 and above: infinity; NaN stays NaN (bit operations, no conversion)
+    const bool nan = e == 2047 && ((hi32 & 0xFFFFFu) | lo32) != 0u;
+    return make_float2(__uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u)), 0.f);
+  }
   const float h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29));
   float l = 0.f;
   if (e >= 943) {  // the scale 2^(e-1069) of the remainder's top 23 bits is a normal float
@@ -51,14 +52,14 @@ __device__ __forceinline__ float2 split_f64(double x) {
 
 // FP32 -> FP64 by bit assembly (exact; the conversion instruction runs on the
 // FP64 pipe).  Zero and subnormal inputs give a signed zero (a subnormal FP32
-// value is far below the densities' tolerance); infinities and NaN take the
-// conversion instruction.
+// value is far below the densities' tolerance); infinities and NaN map to
+// themselves.
 __device__ __forceinline__ double f32_to_f64(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xFFu;
-  if (e == 0xFFu) return (double)f;
   const unsigned sign = u & 0x80000000u;
-  const unsigned hi = e == 0u ? sign : sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+  const unsigned eo = e == 0u ? 0u : (e == 0xFFu ? 2047u : e + 896u);
+  const unsigned hi = e == 0u ? sign : sign | (eo << 20) | ((u & 0x7FFFFFu) >> 3);
   const unsigned lo = e == 0u ? 0u : (u << 29);
   return __hiloint2double((int)hi, (int)lo);
 }
