@@ -143,8 +143,6 @@ cudaError_t jacobi_tf_pack(JacobiTfPlan& pl, const double* phi, const double* sr
 cudaError_t jacobi_tf_encode(JacobiTfPlan& pl);
 cudaError_t jacobi_tf_sweep(const JacobiTfPlan& pl, const double* src_phi, double* dst_phi, cudaStream_t st);
 cudaError_t jacobi_tf_unpack(const JacobiTfPlan& pl, const double* cur, double* phi, cudaStream_t st);
-bool tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint64_t d0, uint64_t d1, uint64_t d2,
-                   uint64_t stride1_bytes, uint64_t stride2_bytes, uint32_t b0, uint32_t b1);
 
 // Mixed-precision multi-right-hand-side PCG (fpm_pcg_mixed.cu).
 constexpr int kMaxRhs = 4;
@@ -388,6 +386,11 @@ cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, c
 // (fpm_jacobi_tma.cu).
 bool tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint64_t d0, uint64_t d1, uint64_t d2,
                    uint64_t stride1_bytes, uint64_t stride2_bytes, uint32_t b0, uint32_t b1);
+// Tensor map of `rank` dimensions (dims[0] contiguous; strides[r - 1] is the
+// byte stride of dimension r), the given box, no swizzle, zero out-of-bounds
+// fill (fpm_jacobi_tma.cu).
+bool tma_encode(CUtensorMap* map, CUtensorMapDataType type, int rank, void* base, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box);
 
 // ---- learned initial guess (fpm_learned.cu, fpm_net.cu) -------------------
 cudaError_t launch_learn_inputs(const Dims& d, const double* src, const double* diag, const Axes& ax, uint8_t* fluid,

@@ -359,6 +359,22 @@ bool tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint6
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
+bool tma_encode(CUtensorMap* map, CUtensorMapDataType type, int rank, void* base, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box) {
+  auto fn = encode_fn();
+  if (!fn || rank < 1 || rank > 5) return false;
+  cuuint64_t d[5], st[4];
+  cuuint32_t b[5], estr[5];
+  for (int r = 0; r < rank; r++) {
+    d[r] = dims[r];
+    b[r] = box[r];
+    estr[r] = 1;
+    if (r > 0) st[r - 1] = strides[r - 1];
+  }
+  CUresult res = fn(map, type, (cuuint32_t)rank, base, d, st, b, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return res == CUDA_SUCCESS;
+}
 static bool encode_3d(CUtensorMap* map, void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t stride1_bytes,
                       uint64_t stride2_bytes, uint32_t b0, uint32_t b1) {
   return tma_encode_3d(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, base, d0, d1, d2, stride1_bytes, stride2_bytes, b0, b1);

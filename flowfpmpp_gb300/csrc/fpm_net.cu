@@ -49,6 +49,14 @@ struct NetError {
       throw NetError{FPM_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)};          \
   } while (0)
 
+// The tcgen05 convolution's bounded waits: a timeout is reported as an error
+// (its outputs are invalid) instead of a hang.
+void check_tc(cudaStream_t st) {
+  int flag = 0;
+  NET_TRY(conv_tc_error(st, &flag));
+  if (flag) throw NetError{FPM_E_TIMEOUT, "tensor-core convolution: a bounded wait gave up"};
+}
+
 template <class F>
 int net_guard(F&& f) {
   try {
@@ -606,6 +614,7 @@ void* net_create(unsigned long long seed) {
 using fpm::net::Net;
 using fpm::net::NetError;
 using fpm::net::net_guard;
+using fpm::net::check_tc;
 
 extern "C" {
 
@@ -662,6 +671,7 @@ int fpm_net_forward_dev(void* net, int nx, int ny, int nz, const uint8_t* fluid,
     NET_TRY(cudaMemcpy2DAsync(out, sizeof(float), p->A.y, 16 * sizeof(float), sizeof(float), (size_t)n,
                               cudaMemcpyDeviceToDevice, st));
     NET_TRY(cudaStreamSynchronize(st));
+    check_tc(st);
   });
 }
 
@@ -677,6 +687,7 @@ int fpm_net_backward_dev(void* net, int nx, int ny, int nz, const uint8_t* fluid
     const double l = p->loss(fluid, target, true, st);
     p->backward(st);
     NET_TRY(cudaStreamSynchronize(st));
+    check_tc(st);
     if (loss) *loss = l;
   });
 }
@@ -696,6 +707,7 @@ int fpm_net_train_step_dev(void* net, int nx, int ny, int nz, const uint8_t* flu
     p->backward(st);
     p->adam(lr, st);
     NET_TRY(cudaStreamSynchronize(st));
+    check_tc(st);
     if (loss) *loss = l;
   });
 }

@@ -46,6 +46,9 @@ struct WgradArgs {
 
 cudaError_t launch_conv(const ConvArgs& a, int cout, cudaStream_t st);
 cudaError_t launch_conv_wgrad(const WgradArgs& w, int cout, cudaStream_t st);
+// Reads and clears the timeout flag of the tcgen05 convolution (nonzero: a
+// bounded wait for its tensor-core work gave up and the output is invalid).
+cudaError_t conv_tc_error(cudaStream_t st, int* flag);
 
 }  // namespace net
 }  // namespace fpm

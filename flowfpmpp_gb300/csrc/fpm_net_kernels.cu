@@ -3,8 +3,10 @@
 // Activations are channels-last BF16: voxel v = i + nx (j + ny k) (x fastest,
 // the solver's own cell order), channel c at v * C + c.  A 3x3x3 convolution
 // with zero padding is an implicit GEMM, M = voxels, N = output channels,
-// K = 27 taps x input channels, run on the tensor cores with
-// mma.sync.m16n8k16 (BF16 operands, FP32 accumulation).
+// K = 27 taps x input channels, run on the tensor cores: layers whose rows
+// are multiples of 128 voxels on tcgen05.mma with tensor-memory accumulators
+// and TMA-staged operands (k_conv_tc, below), the others and the weight
+// gradients with mma.sync.m16n8k16 (BF16 operands, FP32 accumulation).
 //
 // Forward / backward-data tile: a CTA of 4 warps owns 4 rows (j) x 32 voxels
 // (i) of one plane k; each warp owns one row (two m16 tiles) and all output
@@ -23,6 +25,8 @@
 // N = ci, K = voxel GEMM; both operands are read transposed out of shared
 // memory (ldmatrix.trans).
 #include <cuda_bf16.h>
+
+#include <cstdlib>
 
 #include "fpm_internal.h"
 #include "fpm_net.h"
@@ -300,12 +304,338 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs w) {
   }
 }
 
+// ---------------------------------------------------------------- tcgen05 convolution
+// The same convolution on the fifth-generation tensor cores for rows of 128
+// voxels (nx a multiple of 128).  A CTA owns the 128 voxels i0 .. i0+127 of
+// TJ x TK rows (j0 .. j0+TJ-1, k0 .. k0+TK-1), M = 128 voxels, N = COUT, and
+// accumulates each output row in its own tensor-memory (TMEM) columns (FP32,
+// lane = voxel).  Per 16-channel input slice the CTA stages the (TJ+2) x
+// (TK+2) neighbouring rows of 130 voxels and the slice's weights for the 27
+// taps in the K-major no-swizzle operand layout (core matrices of 8 rows x
+// 16 bytes, the two 8-channel halves of the slice in separate arrays):
+// channels of the same-resolution input A arrive by two 4-D TMA boxes
+// {8 channels, 130 voxels, TJ+2, TK+2} (zero fill outside the grid), the
+// upsampled half-resolution input B and the weights by cp.async.  One thread
+// then issues 27 tcgen05.mma (M128 x N COUT x K16, BF16) per output row: tap
+// (di, dj, dk) of row (tj, tk) reads staged row (tj+1+dj, tk+1+dk) from voxel
+// 1 + di, so the shifted operands cost nothing and every staged row serves
+// up to nine output rows.  A commit to an mbarrier tells the CTA when the
+// operands may be overwritten; the epilogue reads the accumulators with
+// tcgen05.ld (warp w owns TMEM lanes 32w .. 32w+31).  Tiles are sized so that
+// two CTAs fit an SM (shared memory and 512 TMEM columns).  Waits are bounded:
+// a timeout sets g_conv_tc_err, waits (bounded) for the copies and MMAs in
+// flight and returns after freeing the tensor memory.
+namespace {
+constexpr int kTcM = 128;                     // voxels per row
+constexpr int kTcVox = kTcM + 2;              // staged voxels per neighbour row
+constexpr int kTcRowBytes = kTcVox * 16;      // one 8-channel half of a staged row
+constexpr unsigned kTcSpin = 1u << 20;
+
+// Output rows (TJ x TK) per CTA and TMEM columns per output row (CS) for the
+// layer widths that run on this kernel (the full- and half-resolution layers
+// of the network); other widths stay on the mma.sync kernel.
+template <int COUT>
+struct TcTile {
+  static constexpr bool on = false;
+  static constexpr int TJ = 1, TK = 1, CS = 16;
+};
+template <>
+struct TcTile<16> { static constexpr bool on = true; static constexpr int TJ = 4, TK = 2, CS = 16; };
+template <>
+struct TcTile<32> { static constexpr bool on = true; static constexpr int TJ = 2, TK = 2, CS = 32; };
+template <>
+struct TcTile<48> { static constexpr bool on = true; static constexpr int TJ = 2, TK = 2, CS = 64; };
+template <>
+struct TcTile<80> { static constexpr bool on = true; static constexpr int TJ = 1, TK = 1, CS = 128; };
+
+template <int COUT>
+struct TcCfg {
+  static constexpr int TJ = TcTile<COUT>::TJ, TK = TcTile<COUT>::TK, CS = TcTile<COUT>::CS;
+  static constexpr int kRowsIn = (TJ + 2) * (TK + 2);
+  static constexpr int kLoaded = kRowsIn * kTcRowBytes;        // bytes of one staged half
+  static constexpr int kHalf = (kLoaded + 127) / 128 * 128;    // 128-byte aligned TMA destination
+  static constexpr int kAct = 2 * kHalf;
+  static constexpr int kWts = 27 * 2 * COUT * 16;
+  static constexpr int kSmem = kAct + kWts;
+  static constexpr int kAcc = TJ * TK * CS;
+  static constexpr int kCols = kAcc <= 32 ? 32 : kAcc <= 64 ? 64 : kAcc <= 128 ? 128 : kAcc <= 256 ? 256 : 512;
+  static_assert(COUT % 16 == 0 && COUT >= 16 && COUT <= 256 && CS >= COUT, "N of an M=128 MMA");
+  static_assert(kAcc <= 512, "TMEM columns");
+};
+
+__device__ int g_conv_tc_err;
+
+__device__ __forceinline__ uint64_t tc_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+  // K-major, no swizzle: start, leading (K) and stride (M/N) byte offsets in
+  // 16-byte units, descriptor version 1 (bits 46-47)
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ bool tc_wait(unsigned bar, unsigned parity) {
+  for (unsigned it = 0; it < kTcSpin; ++it) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(1000u)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tc_load_4d(unsigned dst, const CUtensorMap* map, int c, int i, int j, int k,
+                                           unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(i), "r"(j), "r"(k), "r"(bar)
+      : "memory");
+}
+}  // namespace
+
+template <int COUT>
+__global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, const __grid_constant__ CUtensorMap tm_a) {
+  using C = TcCfg<COUT>;
+  extern __shared__ __align__(128) char smem[];
+  char* act = smem;                // [2 halves][TK+2][TJ+2][130 voxels][16 B]
+  char* wts = smem + C::kAct;      // [27 taps][2 halves][COUT][16 B]
+  __shared__ __align__(8) uint64_t bars[2];  // 0: the slice's TMA boxes, 1: the slice's MMAs
+  __shared__ unsigned tmem_base_s;
+  __shared__ float bias_s[COUT];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int c = tid; c < COUT; c += 128) bias_s[c] = a.bias ? a.bias[c] : 0.f;
+  const int i0 = blockIdx.x * kTcM, j0 = blockIdx.y * C::TJ, k0 = blockIdx.z * C::TK;
+  const unsigned bar_ld = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_ld) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_mma) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_a)) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(C::kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = tmem_base_s;
+  // instruction descriptor: F32 accumulator, BF16 A and B, both K-major, N, M
+  constexpr unsigned kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(COUT >> 3) << 17) |
+                              ((unsigned)(kTcM >> 4) << 24);
+  const int hx = a.nx >> 1, hy = a.ny >> 1;
+  const int nslices = a.cin / 16;
+  bool ok = true, mma_pending = false, ld_pending = false;
+  unsigned ph_ld = 0, ph_mma = 0;
+  for (int s = 0; s < nslices; s++) {
+    // the previous slice's MMAs must be done before its operands are overwritten
+    if (mma_pending && tc_wait(bar_mma, ph_mma)) {
+      ph_mma ^= 1u;
+      mma_pending = false;
+    }
+    if (__syncthreads_or(mma_pending)) {
+      ok = false;
+      break;
+    }
+    const int c0 = s * 16;
+    const bool from_a = c0 < a.ca;
+    if (from_a) {
+      if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_ld), "r"(2 * C::kLoaded)
+                     : "memory");
+        tc_load_4d(smem_u32(act), &tm_a, c0, i0 - 1, j0 - 1, k0 - 1, bar_ld);
+        tc_load_4d(smem_u32(act + C::kHalf), &tm_a, c0 + 8, i0 - 1, j0 - 1, k0 - 1, bar_ld);
+      }
+      ld_pending = true;
+    } else {
+      // upsampled half-resolution input: row by row, voxel i reads B at i >> 1
+      for (int row = 0; row < C::kRowsIn; row++) {
+        const int jj = j0 - 1 + row % (C::TJ + 2), kk = k0 - 1 + row / (C::TJ + 2);
+        const bool rin = jj >= 0 && jj < a.ny && kk >= 0 && kk < a.nz;
+        const __nv_bfloat16* brow =
+            rin ? a.b + (long long)hx * ((jj >> 1) + (long long)hy * (kk >> 1)) * a.cb + (c0 - a.ca) : a.b;
+        char* drow = act + row * kTcRowBytes;
+        for (int c = tid; c < kTcVox * 2; c += 128) {
+          const int vox = c >> 1, h = c & 1, i = i0 - 1 + vox;
+          const bool in = rin && i >= 0 && i < a.nx;
+          cp_async16(drow + h * C::kHalf + vox * 16, in ? brow + (long long)(i >> 1) * a.cb + 8 * h : a.b, in);
+        }
+      }
+    }
+    const __nv_bfloat16* wsrc = a.w + (long long)s * 27 * COUT * 16;
+    for (int idx = tid; idx < 27 * COUT * 2; idx += 128) {
+      const int r = idx >> 1, h = idx & 1;  // r = t * COUT + co
+      const int t = r / COUT, co = r - t * COUT;
+      cp_async16(wts + (t * 2 + h) * COUT * 16 + co * 16, wsrc + r * 16 + 8 * h, true);
+    }
+    cp_async_wait_all();
+    // the cp.async operands were written through the generic proxy; the MMA
+    // reads them through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (ld_pending && tc_wait(bar_ld, ph_ld)) {
+      ph_ld ^= 1u;
+      ld_pending = false;
+    }
+    if (__syncthreads_or(ld_pending)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const unsigned act_a = smem_u32(act), wts_a = smem_u32(wts);
+      for (int o = 0; o < C::TJ * C::TK; o++) {
+        const int tj = o % C::TJ, tk = o / C::TJ;
+        const unsigned d = tmem + (unsigned)(o * C::CS);
+        for (int t = 0; t < 27; t++) {
+          const int di = t % 3, dj = (t / 3) % 3, dk = t / 9;  // offsets + 1
+          const int row = (tj + dj) + (C::TJ + 2) * (tk + dk);
+          const uint64_t ad = tc_desc(act_a + row * kTcRowBytes + di * 16, C::kHalf, 128);
+          const uint64_t bd = tc_desc(wts_a + (t * 2) * COUT * 16, COUT * 16, 128);
+          const unsigned acc = (s > 0 || t > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+              "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc)
+              : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_mma)
+                   : "memory");
+    }
+    mma_pending = true;
+  }
+  if (ok && mma_pending && tc_wait(bar_mma, ph_mma)) {
+    ph_mma ^= 1u;
+    mma_pending = false;
+  }
+  if (__syncthreads_or(!ok || mma_pending)) {
+    if (tid == 0) {
+      atomicExch(&g_conv_tc_err, 1);
+      // bounded waits for the work still in flight before the memory is released
+      if (mma_pending) tc_wait(bar_mma, ph_mma);
+      if (ld_pending) tc_wait(bar_ld, ph_ld);
+    }
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue: voxel i of this warp's 32 TMEM lanes, every output row of the tile
+    const int i = i0 + 32 * warp + lane;
+    for (int o = 0; o < C::TJ * C::TK; o++) {
+      const int j = j0 + o % C::TJ, k = k0 + o / C::TJ;
+      if (j >= a.ny || k >= a.nz) continue;  // uniform over the CTA
+      const long long v = i + (long long)a.nx * (j + (long long)a.ny * k);
+#pragma unroll
+      for (int c16 = 0; c16 < COUT / 16; c16++) {
+        float x[16];
+        unsigned r[16];
+        const unsigned taddr = tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(o * C::CS + 16 * c16);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int e = 0; e < 16; e++) x[e] = __uint_as_float(r[e]);
+        const int cb = 16 * c16;
+        if (a.mode == kConvBf16) {
+          unsigned q[8];
+#pragma unroll
+          for (int e = 0; e < 16; e += 2) {
+            float x0 = x[e] + bias_s[cb + e], x1 = x[e + 1] + bias_s[cb + e + 1];
+            if (a.relu) {
+              x0 = fmaxf(x0, 0.f);
+              x1 = fmaxf(x1, 0.f);
+            }
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
+            q[e / 2] = *reinterpret_cast<const unsigned*>(&h2);
+          }
+          uint4* dst = reinterpret_cast<uint4*>(a.y + v * COUT + cb);
+          dst[0] = make_uint4(q[0], q[1], q[2], q[3]);
+          dst[1] = make_uint4(q[4], q[5], q[6], q[7]);
+        } else if (a.mode == kConvF32) {
+          float4* dst = reinterpret_cast<float4*>(a.yf + v * COUT + cb);
+#pragma unroll
+          for (int e = 0; e < 4; e++)
+            dst[e] = make_float4(x[4 * e] + bias_s[cb + 4 * e], x[4 * e + 1] + bias_s[cb + 4 * e + 1],
+                                 x[4 * e + 2] + bias_s[cb + 4 * e + 2], x[4 * e + 3] + bias_s[cb + 4 * e + 3]);
+        } else if (cb < a.csplit) {  // csplit is a multiple of 16: the chunk is all A
+          float4* g = reinterpret_cast<float4*>(a.ga + v * a.csplit + cb);
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            float4 t = g[e];
+            t.x += x[4 * e];
+            t.y += x[4 * e + 1];
+            t.z += x[4 * e + 2];
+            t.w += x[4 * e + 3];
+            g[e] = t;
+          }
+        } else {
+          // the 2x2x2 sum into the half-resolution B: lanes 2m and 2m + 1 hold
+          // voxels i and i + 1 of the same half-resolution voxel
+#pragma unroll
+          for (int e = 0; e < 16; e++) x[e] += __shfl_xor_sync(0xffffffffu, x[e], 1);
+          if (!(lane & 1)) {
+            const long long vb = (i >> 1) + (long long)hx * ((j >> 1) + (long long)hy * (k >> 1));
+            float4* g = reinterpret_cast<float4*>(a.gb + vb * (COUT - a.csplit) + (cb - a.csplit));
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+              atomicAdd(g + e, make_float4(x[4 * e], x[4 * e + 1], x[4 * e + 2], x[4 * e + 3]));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::kCols) : "memory");
+}
+
 // ---------------------------------------------------------------- launchers
 static size_t conv_smem(int cout) { return (size_t)kActBytes + (size_t)27 * cout * 32; }
 static size_t wgrad_smem(int cout) { return (size_t)kRows * kTx * (cout * 2 + 16) + 6 * kHaloVox * 48; }
 
+static bool tc_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("FPM_CONV_TC");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+template <int COUT>
+static cudaError_t launch_conv_tc(const ConvArgs& a, cudaStream_t st) {
+  using C = TcCfg<COUT>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv_tc<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  // the same-resolution input as {ca channels, nx, ny, nz}, box {8, 130, TJ+2, TK+2}
+  CUtensorMap tm;
+  const uint64_t cs = 2ull * a.ca;
+  const uint64_t dims[4] = {(uint64_t)a.ca, (uint64_t)a.nx, (uint64_t)a.ny, (uint64_t)a.nz};
+  const uint64_t strides[3] = {cs, cs * a.nx, cs * a.nx * a.ny};
+  const uint32_t box[4] = {8, (uint32_t)kTcVox, (uint32_t)(C::TJ + 2), (uint32_t)(C::TK + 2)};
+  if (!tma_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(a.a), dims, strides, box))
+    return cudaErrorInvalidValue;
+  const dim3 grid(a.nx / kTcM, (a.ny + C::TJ - 1) / C::TJ, (a.nz + C::TK - 1) / C::TK);
+  k_conv_tc<COUT><<<grid, 128, C::kSmem, st>>>(a, tm);
+  note_launch();
+  return cudaGetLastError();
+}
+
 template <int COUT>
 static cudaError_t launch_conv_t(const ConvArgs& a, cudaStream_t st) {
+  if constexpr (TcTile<COUT>::on) {
+    if (tc_enabled() && a.nx % kTcM == 0 && (a.mode != kConvGrad || a.csplit % 16 == 0))
+      return launch_conv_tc<COUT>(a, st);
+  }
   static bool attr = false;
   const size_t sm = conv_smem(COUT);
   if (!attr) {
@@ -358,6 +688,16 @@ cudaError_t launch_conv_wgrad(const WgradArgs& w, int cout, cudaStream_t st) {
     case 64: return launch_wgrad_t<64>(w, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// Reads and clears the tcgen05 convolution's timeout flag.
+cudaError_t conv_tc_error(cudaStream_t st, int* flag) {
+  cudaError_t e = cudaMemcpyFromSymbolAsync(flag, g_conv_tc_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess || *flag == 0) return e;
+  const int zero = 0;
+  return cudaMemcpyToSymbolAsync(g_conv_tc_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
 }
 
 }  // namespace net

@@ -37,7 +37,12 @@ def _layers():
         o += nw + co
 
 
-def test_forward_and_gradients_match_oracle(gpu_lib):
+@pytest.mark.parametrize("shape", [(16, 16, 8), (128, 8, 8), (256, 8, 8)])
+def test_forward_and_gradients_match_oracle(gpu_lib, shape):
+    """Layers whose rows are multiples of 128 voxels run on the tcgen05
+    tensor-core kernel (TMEM accumulators), the others on the mma.sync kernel:
+    (128, 8, 8) the full-resolution layers (16 and 48 output channels),
+    (256, 8, 8) also the half-resolution ones (32 and 80); (16, 16, 8) none."""
     from flowfpmpp_gb300.learned import LearnedGuess
     rng = np.random.default_rng(5)
     net = LearnedGuess(seed=11)
@@ -48,7 +53,7 @@ def test_forward_and_gradients_match_oracle(gpu_lib):
     last_w, last_b = list(_layers())[-1]
     p[last_b.start + 1:last_b.stop] = 0.0  # the head keeps output channel 0 only
     net.set_params(p)
-    fluid, mx, my, mz, rhs, target = _tiny(rng)
+    fluid, mx, my, mz, rhs, target = _tiny(rng, *shape)
     nx, ny, nz = fluid.shape
     args = (nx, ny, nz, _dev(fluid), _dev(mx), _dev(my), _dev(mz), _dev(rhs))
     y = net.forward(*args).cpu().numpy().reshape((nx, ny, nz), order="F")
