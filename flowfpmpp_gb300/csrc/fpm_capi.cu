@@ -1023,6 +1023,8 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     v.p[m] = zeros(n0);
     v.q[m] = zeros(n0);
     v.e[m] = zeros(n0);
+    v.r2[m] = zeros(n0);
+    v.p2[m] = zeros(n0);
     r64.p[m] = A.get<double>(d.ncell());
     phis.p[m] = phi[m];
     S64[m] = A.get<SolveScalars>(1);
@@ -1120,7 +1122,7 @@ static void mg_solve(const Dims& d, int nrhs, double* const phi[], const double*
     const int zero = 0;
     for (int m = 0; m < nrhs; m++)  // park them until their restart
       if ((upd >> m) & 1u) CUDA_TRY(cudaMemcpyAsync(&S[m].active, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(mg_pcg_apply(H, d, v, scale, upd, phis, st));
+    CUDA_TRY(mg_pcg_apply(H, d, v, S, scale, upd, phis, st));
     unsigned restart = 0;
     for (int m = 0; m < nrhs; m++) {
       if (!((upd >> m) & 1u)) continue;

@@ -329,7 +329,7 @@ constexpr int kMgMaxLevels = 16;
 // the level-1 solution x1 of each right-hand side, level 0's omega D^-1 and
 // the open-face bits.
 struct MgMaps {
-  CUtensorMap z[kMaxRhs], p[kMaxRhs], r[kMaxRhs], x1[kMaxRhs], dinv, fb;
+  CUtensorMap z[kMaxRhs], p[kMaxRhs], r[kMaxRhs], x1[kMaxRhs], q[kMaxRhs], p2[kMaxRhs], r2[kMaxRhs], dinv, fb;
 };
 struct MgHierarchy {
   int nlev, nrhs;
@@ -355,6 +355,10 @@ struct MgHierarchy {
 };
 struct MgVecs {  // level-0 PCG vectors per right-hand side
   float *r[kMaxRhs], *z[kMaxRhs], *p[kMaxRhs], *q[kMaxRhs], *e[kMaxRhs];
+  // second r and p buffers of the multigrid PCG: the passes that update r and
+  // p read one buffer (with halos) and write the other, alternating with the
+  // parity of the inner iteration count
+  float *r2[kMaxRhs], *p2[kMaxRhs];
 };
 struct MgScalars {  // one per right-hand side
   double rz, rz0, pq, alpha, beta, tol2;
@@ -379,8 +383,8 @@ cudaError_t mg_setup(MgHierarchy& H, const Dims& d, const int32_t* solid, const 
 cudaError_t mg_pcg_start(const MgHierarchy& H, const DPtr4& rv, const double* scale, unsigned mask, MgVecs& v,
                          MgScalars* S, const MgRed& rb, cudaStream_t st);
 cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, const MgRed& rb, cudaStream_t st);
-cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const double* scale, unsigned mask,
-                         const DPtr4& phi, cudaStream_t st);
+cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const MgScalars* S,
+                         const double* scale, unsigned mask, const DPtr4& phi, cudaStream_t st);
 
 // 3-D tensor map with box (b0, b1, 1), no swizzle, zero out-of-bounds fill
 // (fpm_jacobi_tma.cu).

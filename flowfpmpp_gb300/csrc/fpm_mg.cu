@@ -238,18 +238,6 @@ struct P0 {
   bool live;
   long long base;
 };
-__device__ __forceinline__ P0 p0_pos(const MixedGrid& G) {
-  P0 t;
-  t.zc = (G.nz + G.kc - 1) / G.kc;
-  t.m = (int)blockIdx.z / t.zc;
-  t.g = blockIdx.x * 32 + threadIdx.x;
-  t.j = blockIdx.y * 4 + threadIdx.y + 1;
-  t.live = t.g < G.ng && t.j <= G.ny;
-  t.k0 = ((int)blockIdx.z - t.m * t.zc) * G.kc + 1;
-  t.k1 = min(G.nz, t.k0 + G.kc - 1);
-  t.base = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (t.k0 - 1));
-  return t;
-}
 
 // Sum of s over the blocks of right-hand side m (the zc chunks of its
 // blockIdx.z range); true in the last of them, with *out set in thread 0.
@@ -602,16 +590,24 @@ namespace {
 // their x-y halo and turns them into the stencil operand in shared memory
 // when a plane lands:
 //   kSpmv      p = z + beta p_old (the direction update); q = A p, p.q and
-//              alpha = rz / pq.  The new p is written by the update kernel.
-//   kResidual  t = wd r (the first pre-smoothing sweep from zero);
-//              b1 = cscale x P^T (r - A t), the residual restricted to level 1
-//              on the fly (an aggregate's two planes summed in registers, its
-//              two rows through shared memory; chunks hold whole aggregates)
+//              alpha = rz / pq; writes p and q, and adds the previous
+//              iteration's alpha p_old to e (so e lags one step: the apply
+//              pass adds the last alpha p)
+//   kResidual  r = r_old - alpha q (the PCG residual update; not at a start),
+//              written out; t = wd r (the first pre-smoothing sweep from
+//              zero); b1 = cscale x P^T (r - A t), the residual restricted to
+//              level 1 on the fly (an aggregate's two planes summed in
+//              registers, its two rows through shared memory; chunks hold
+//              whole aggregates)
 //   kSmooth    y = wd r + P x1 (the pre-smoothed iterate plus the prolonged
 //              level-1 correction, the level-1 tile of each plane's parents
 //              streamed alongside); z = y + wd (r - A y), r.z and the PCG
 //              scalar updates (start: rz = rz0, beta = 0 and p = 0; otherwise
 //              beta and the stop test)
+// r and p have two buffers each: kSpmv reads p from buffer (iters & 1) and
+// writes buffer (iters & 1) ^ 1, kResidual does the same for r, and kSmooth
+// (which counts the iteration) reads the new r, so no pass writes a field
+// that another CTA of the same pass reads as a halo.
 // A CTA owns kTX x kTY cells of a plane (a warp per row, four cells per
 // thread) and marches through kc0 planes.  Thread 0 keeps a 4-deep ring of
 // planes (both operand tiles, the open-face bits, the level-1 tile) in flight
@@ -630,6 +626,7 @@ namespace {
 //            x neighbours; the x start is a multiple of 4 (16 bytes)
 //   bits     (kTX + 16) x (kTY + 2) bytes from the same corner (x a multiple
 //            of 16 bytes; the bits' row pitch pxb is a multiple of 16)
+//   q        (kResidual) the operand box of q
 //   x1       kCW x kCH floats of level 1 (rows padded to 16 bytes) from
 //            (kTX bx / 2 - 4, kTY by / 2 - 1, parent plane): the parents of
 //            the operand tile's cells
@@ -651,9 +648,10 @@ static_assert((kCW * 4) % 16 == 0, "level-1 box rows are whole 16-byte units");
 static_assert(kPW % 4 == 0 && 2 * (kQ - 1) + 3 < kCW, "prolongation: float4 rows, parents inside the tile");
 static_assert(kHalo4 <= kTThreads, "one halo float4 per thread at most");
 
-// One ring stage: operand A, operand B, bits, and for kSmooth the level-1 tile.
+// One ring stage: operand A, operand B, bits, and the level-1 tile (kSmooth)
+// or q (kResidual).
 __host__ __device__ constexpr uint32_t tma_stage(int mode) {
-  return 2 * kXStage + kBStage + (mode == kSmooth ? kX1Stage : 0u);
+  return 2 * kXStage + kBStage + (mode == kSmooth ? kX1Stage : mode == kResidual ? kXStage : 0u);
 }
 __host__ __device__ constexpr uint32_t tma_smem(int mode) { return kXSt * tma_stage(mode) + 8 * kXSt; }
 
@@ -677,13 +675,18 @@ __global__ void __launch_bounds__(kTThreads, 3)
   t.g = x0 / 4 + q;
   t.j = y0 + ty + 1;
   t.live = t.g < G.ng && t.j <= G.ny;
-  // operand A: z (kSpmv) or r; operand B: p (kSpmv) or wd
-  const CUtensorMap* ma = MODE == kSpmv ? (m == 0 ? &M.z[0] : m == 1 ? &M.z[1] : m == 2 ? &M.z[2] : &M.z[3])
-                                        : (m == 0 ? &M.r[0] : m == 1 ? &M.r[1] : m == 2 ? &M.r[2] : &M.r[3]);
-  const CUtensorMap* mb = MODE == kSpmv ? (m == 0 ? &M.p[0] : m == 1 ? &M.p[1] : m == 2 ? &M.p[2] : &M.p[3])
-                                        : &M.dinv;
-  const CUtensorMap* m1 = m == 0 ? &M.x1[0] : m == 1 ? &M.x1[1] : m == 2 ? &M.x1[2] : &M.x1[3];
+  auto sel = [m](const CUtensorMap* a) { return m == 0 ? a : m == 1 ? a + 1 : m == 2 ? a + 2 : a + 3; };
+  // buffers: par = current r / p (kSmooth reads the r that kResidual wrote)
+  const int par = S[m].iters & 1;
+  const int rpar = MODE == kSmooth && !start ? par ^ 1 : par;
+  // operand A: z (kSpmv) or r; operand B: p (kSpmv) or wd; kResidual: q
+  const CUtensorMap* ma = MODE == kSpmv ? sel(M.z) : (rpar ? sel(M.r2) : sel(M.r));
+  const CUtensorMap* mb = MODE == kSpmv ? (par ? sel(M.p2) : sel(M.p)) : &M.dinv;
+  const CUtensorMap* m1 = MODE == kSmooth ? sel(M.x1) : sel(M.q);
+  const bool with_q = MODE == kResidual && !start;
   const float beta = MODE == kSpmv ? (float)S[m].beta : 0.f;
+  // kSpmv: the previous alpha (for e += alpha p_old); kResidual: this one
+  const float alpha = MODE == kSmooth ? 0.f : (float)S[m].alpha;
   if (tid == 0) {
     for (int s = 0; s < kXSt; s++) tma::mbar_init(bar_base + 8 * s, 1);
     tma::mbar_init_fence();
@@ -694,11 +697,12 @@ __global__ void __launch_bounds__(kTThreads, 3)
   auto issue = [&](int p) {
     const int s = (p - (k0 - 1)) % kXSt;
     const uint32_t bar = bar_base + 8 * s, dst = s_base + s * kStage;
-    tma::mbar_expect_tx(bar, 2 * kXBytes + kBBytes + (MODE == kSmooth ? kX1Bytes : 0u));
+    tma::mbar_expect_tx(bar, 2 * kXBytes + kBBytes + (MODE == kSmooth ? kX1Bytes : with_q ? kXBytes : 0u));
     tma::load_3d(dst, ma, x0, y0, p - 1, bar);
     tma::load_3d(dst + kXStage, mb, x0, y0, p - 1, bar);
     tma::load_3d(dst + 2 * kXStage, &M.fb, x0, y0, p - 1, bar);
     if (MODE == kSmooth) tma::load_3d(dst + 2 * kXStage + kBStage, m1, x0 / 2 - 4, y0 / 2 - 1, (p - 1) >> 1, bar);
+    if (with_q) tma::load_3d(dst + 2 * kXStage + kBStage, m1, x0, y0, p - 1, bar);
   };
   auto ready = [&](int p) {
     const int u = p - (k0 - 1);
@@ -716,10 +720,15 @@ __global__ void __launch_bounds__(kTThreads, 3)
     unsigned char* st = smem + ((p - (k0 - 1)) % kXSt) * kStage;
     float* A = reinterpret_cast<float*>(st);
     float* B = reinterpret_cast<float*>(st + kXStage);
-    const float* X1 = reinterpret_cast<const float*>(st + 2 * kXStage + kBStage);
+    const float* X1 = reinterpret_cast<const float*>(st + 2 * kXStage + kBStage);  // kSmooth: level 1; kResidual: q
     auto one = [&](int e, int r, int a4, float4& ra, float4& rb4) {  // float4 e = (row r, column 4 a4)
       ra = *reinterpret_cast<const float4*>(A + e);
       rb4 = *reinterpret_cast<const float4*>(B + e);
+      if (MODE == kResidual && with_q) {  // r = r_old - alpha q, kept as this cell's raw value
+        const float4 qq = *reinterpret_cast<const float4*>(X1 + e);
+        ra = make_float4(fmaf(-alpha, qq.x, ra.x), fmaf(-alpha, qq.y, ra.y), fmaf(-alpha, qq.z, ra.z),
+                         fmaf(-alpha, qq.w, ra.w));
+      }
       const float2 a0 = lo2(ra), a1 = hi2(ra), b0 = lo2(rb4), b1 = hi2(rb4);
       float2 r0, r1;
       if (MODE == kSpmv) {  // p = z + beta p_old
@@ -757,6 +766,9 @@ __global__ void __launch_bounds__(kTThreads, 3)
     for (; next <= k0 + kXSt - 2 && next <= k1 + 1; next++) issue(next);
 
   float* __restrict__ out = MODE == kSpmv ? v.q[m] : (MODE == kResidual ? C.b[m] : v.z[m]);
+  // kSpmv: the new p; kResidual: the new r; kSmooth (start): p = 0
+  float* __restrict__ out2 = MODE == kSpmv ? (par ? v.p[m] : v.p2[m])
+                                           : MODE == kResidual ? (par ? v.r[m] : v.r2[m]) : (par ? v.p2[m] : v.p[m]);
   // kResidual: the odd rows' aggregate sums, double-buffered by aggregate
   // plane (with an odd nz the last two planes complete aggregates in
   // consecutive steps)
@@ -780,7 +792,13 @@ __global__ void __launch_bounds__(kTThreads, 3)
   }
   int kfail = k0;
   bool failed = false;
+  // kSpmv: e of this thread's cells, loaded one plane ahead
+  const long long base0 = 4LL * (t.g + 1) + (long long)G.px * (t.j + (long long)(G.ny + 2) * (k0 - 1));
+  float4 e_nxt = zero4();
+  if (MODE == kSpmv && t.live) e_nxt = ld4(v.e[m] + base0);
   for (int k = k0; k <= k1; k++) {
+    float4 e_cur = e_nxt;
+    if (MODE == kSpmv && t.live && k < k1) e_nxt = ld4(v.e[m] + base0 + (long long)G.plane * (k + 1 - k0));
     ok = ok && ready(k + 1);
     if (ok) transform(k + 1, nxt_a, nxt_b);
     __syncthreads();
@@ -807,10 +825,15 @@ __global__ void __launch_bounds__(kTThreads, 3)
       if (MODE == kSpmv) {
         st4(out + base, uu);
         acc.add4(pc, uu);
+        st4(out2 + base, pc);  // the new direction (pc is this thread's p = z + beta p_old)
+        const float4 &ee = e_cur, &po = cur_b;
+        st4(v.e[m] + base, make_float4(fmaf(alpha, po.x, ee.x), fmaf(alpha, po.y, ee.y), fmaf(alpha, po.z, ee.z),
+                                       fmaf(alpha, po.w, ee.w)));
       } else if (MODE == kResidual) {
         const float4& rr = cur_a;
         agg.x += (rr.x - uu.x) + (rr.y - uu.y);
         agg.y += (rr.z - uu.z) + (rr.w - uu.w);
+        if (with_q) st4(out2 + base, rr);
       } else {
         const float4 &rr = cur_a, &wd = cur_b;
         float zz[4];
@@ -819,7 +842,7 @@ __global__ void __launch_bounds__(kTThreads, 3)
           zz[n] = i0 + n < L.nx ? fmaf(el(wd, n), el(rr, n) - el(uu, n), el(pc, n)) : 0.f;
         const float4 z4 = make_float4(zz[0], zz[1], zz[2], zz[3]);
         st4(out + base, z4);
-        if (start) st4(v.p[m] + base, zero4());  // the first direction is z itself
+        if (start) st4(out2 + base, zero4());  // the first direction is z itself
         acc.add4(rr, z4);
       }
     }
@@ -881,32 +904,6 @@ __global__ void __launch_bounds__(kTThreads, 3)
   if (rz <= Q.tol2 * Q.rz0) Q.active = 0;
 }
 
-// p = z + beta p (the direction the spmv pass used), e += alpha p,
-// r -= alpha q: pointwise, so p is updated in place.
-__global__ void __launch_bounds__(128) k_mg0_update(MixedGrid G, MgVecs v, const MgScalars* S, unsigned mask) {
-  const P0 t = p0_pos(G);
-  MG_SKIP(t.m);
-  if (!t.live) return;
-  const float a = (float)S[t.m].alpha, bt = (float)S[t.m].beta;
-  const float* __restrict__ z = pick(v.z, t.m);
-  const float* __restrict__ q = pick(v.q, t.m);
-  float* __restrict__ p = pick(v.p, t.m);
-  float* __restrict__ e = pick(v.e, t.m);
-  float* __restrict__ r = pick(v.r, t.m);
-  long long base = t.base;
-  for (int k = t.k0; k <= t.k1; k++, base += G.plane) {
-    const float4 zz = ld4(z + base), qq = ld4(q + base);
-    float4 pp = *reinterpret_cast<const float4*>(p + base), ee = *reinterpret_cast<const float4*>(e + base),
-           rr = *reinterpret_cast<const float4*>(r + base);
-    pp = make_float4(fmaf(bt, pp.x, zz.x), fmaf(bt, pp.y, zz.y), fmaf(bt, pp.z, zz.z), fmaf(bt, pp.w, zz.w));
-    ee = make_float4(fmaf(a, pp.x, ee.x), fmaf(a, pp.y, ee.y), fmaf(a, pp.z, ee.z), fmaf(a, pp.w, ee.w));
-    rr = make_float4(fmaf(-a, qq.x, rr.x), fmaf(-a, qq.y, rr.y), fmaf(-a, qq.z, rr.z), fmaf(-a, qq.w, rr.w));
-    st4(p + base, pp);
-    st4(e + base, ee);
-    st4(r + base, rr);
-  }
-}
-
 struct Scale4 {
   double s[kMaxRhs];
 };
@@ -927,16 +924,24 @@ __global__ void k_mgp_load(MgLevel L, DPtr4 rv, Scale4 sc, unsigned mask, MgVecs
   }
 }
 
-// phi(padded) += e / scale on fluid cells
-__global__ void k_mgp_apply(MgLevel L, Dims d, MgVecs v, Scale4 sc, unsigned mask, DPtr4 phiv) {
+// phi(padded) += (e + alpha p) / scale on fluid cells: the correction with
+// the last iteration's alpha p, which the spmv pass adds to e only in the
+// iteration after (alpha is zero after a breakdown)
+__global__ void k_mgp_apply(MgLevel L, Dims d, MgVecs v, const MgScalars* S, Scale4 sc, unsigned mask,
+                            DPtr4 phiv) {
   MG_RHS(L);
   if (!((mask >> mrhs) & 1u)) return;
   const float* __restrict__ e = pick(v.e, mrhs);
+  const float a = (float)S[mrhs].alpha;
+  const float* __restrict__ p = (S[mrhs].iters & 1) ? pick(v.p2, mrhs) : pick(v.p, mrhs);
   const double scale = pick(sc.s, mrhs);
   double* __restrict__ phi = pick(phiv.p, mrhs);
   MG_CELLS(L) {
     const long long c = ix(L, i, j, k);
-    if (L.dinv[c] > 0.f) phi[d.ph(i + 1, j + 1, k + 1)] += (double)e[c] / scale;
+    if (L.dinv[c] > 0.f) {
+      const float ec = a != 0.f ? fmaf(a, p[c], e[c]) : e[c];
+      phi[d.ph(i + 1, j + 1, k + 1)] += (double)ec / scale;
+    }
   }
 }
 
@@ -954,11 +959,6 @@ Ops0 ops0(const MgHierarchy& H) {
 dim3 tma_grid(const MgHierarchy& H) {
   return dim3((unsigned)((H.g0.ng + kTX / 4 - 1) / (kTX / 4)), (unsigned)((H.g0.ny + kTY - 1) / kTY),
               (unsigned)(((H.g0.nz + H.kc0 - 1) / H.kc0) * H.nrhs));
-}
-
-dim3 g0_grid(const MixedGrid& G, int nrhs) {
-  return dim3((unsigned)((G.ng + 31) / 32), (unsigned)((G.ny + 3) / 4),
-              (unsigned)(((G.nz + G.kc - 1) / G.kc) * nrhs));
 }
 
 Scale4 scale4(const double* s, unsigned mask) {
@@ -1010,15 +1010,13 @@ cudaError_t mg_pcg_iteration(const MgHierarchy& H, MgVecs& v, MgScalars* S, cons
   k_mg0_tma<kSpmv><<<tma_grid(H), kTThreads, tma_smem(kSpmv), st>>>(H.maps, H.g0, H.kc0, L, H.lv[1], ops0(H), v,
                                                                      H.cscale, S, rb, all, 0);
   note_launch();
-  k_mg0_update<<<g0_grid(H.g0, H.nrhs), dim3(32, 4), 0, st>>>(H.g0, v, S, all);
-  note_launch();
   return level0_tail(H, v, S, rb, all, 0, st);
 }
 
-cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const double* scale, unsigned mask,
-                         const DPtr4& phi, cudaStream_t st) {
+cudaError_t mg_pcg_apply(const MgHierarchy& H, const Dims& d, const MgVecs& v, const MgScalars* S,
+                         const double* scale, unsigned mask, const DPtr4& phi, cudaStream_t st) {
   const MgLevel& L = H.lv[0];
-  k_mgp_apply<<<rhs_grid(L, H.nrhs), dim3(32, 8), 0, st>>>(L, d, v, scale4(scale, mask), mask, phi);
+  k_mgp_apply<<<rhs_grid(L, H.nrhs), dim3(32, 8), 0, st>>>(L, d, v, S, scale4(scale, mask), mask, phi);
   note_launch();
   return cudaGetLastError();
 }
@@ -1037,7 +1035,8 @@ cudaError_t mg_encode(MgHierarchy& H, const MgVecs& v) {
   bool ok = true;
   for (int m = 0; m < H.nrhs; m++) {
     ok = ok && f32(&H.maps.z[m], v.z[m], kPW, kPH) && f32(&H.maps.p[m], v.p[m], kPW, kPH) &&
-         f32(&H.maps.r[m], v.r[m], kPW, kPH);
+         f32(&H.maps.r[m], v.r[m], kPW, kPH) && f32(&H.maps.q[m], v.q[m], kPW, kPH) &&
+         f32(&H.maps.p2[m], v.p2[m], kPW, kPH) && f32(&H.maps.r2[m], v.r2[m], kPW, kPH);
   }
   const MgLevel& L1 = H.lv[1];
   for (int m = 0; m < H.nrhs; m++)
