@@ -2527,6 +2527,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         M.p[r] = A.get<float>(n2);
         M.q[r] = A.get<float>(n2);
         M.e[r] = A.get<float>(n2);
+        M.r2[r] = A.get<float>(n2);
+        M.p2[r] = A.get<float>(n2);
       }
       CUDA_TRY(fm_setup(dfr, dtf, ntiles, b, M, nall_lv.data(), st));
     }

@@ -21,9 +21,18 @@
 // folded into the residual), so it is a valid PCG preconditioner.
 //
 // Every kernel walks a tile list (32 x 8 cells of one frame at one level);
-// frames that have finished (per frame and direction flags) return at once,
-// and the per-frame reductions are segmented (last tile of a frame combines
-// the frame's partials in tile order), so results do not depend on timing.
+// frames that have finished (per frame and direction flags) return at once.
+// The level-0 stencil passes stage their operand with its one-cell halo in
+// shared memory (a 34 x 10 tile per direction) and carry the PCG vector
+// updates, so an iteration has no pointwise pass: the spmv pass forms
+// p = z + beta p_old, writes it and adds the previous alpha p_old to e (e lags
+// one step; the apply pass adds the last alpha p), the restriction pass forms
+// r = r_old - alpha q and writes it.  r and p have two buffers each, chosen by
+// the parity of the (frame, direction)'s iteration count, so no pass
+// overwrites a value another CTA reads as a halo.  The dot products go to one
+// partial per tile; a finalize kernel per frame and direction combines them in
+// tile order (one warp, fixed order) and updates the PCG scalars, so results
+// do not depend on timing.
 #include "fpm_internal.h"
 
 namespace fpm {
@@ -51,35 +60,36 @@ struct Sum2 {
   __device__ __forceinline__ double value() const { return (double)s + (double)e; }
 };
 
-// Segmented sum of kR values over the level-0 tiles of frame f (tile ids
-// tile0 .. tile0 + ntiles - 1); true in the last tile of the frame to finish,
-// with out[] = the frame's sums combined in tile order.
-__device__ bool fm_seg_sum(double (&s)[kR], int f, int tile, int tile0, int ntiles, double* partials,
-                           unsigned int* tickets, double (&out)[kR]) {
-  __shared__ bool am_last;
+// The level-0 operand tile with its halo: cell (i0 - 1 + x, j0 - 1 + y) of the
+// frame at [y][x]; threads 0 .. kHalo - 1 fill the halo.
+constexpr int kHX = 34, kHY = 10, kHalo = 2 * kHX + 2 * 8;
+__device__ __forceinline__ void halo_pos(int tid, int& x, int& y) {
+  if (tid < kHX) {
+    x = tid;
+    y = 0;
+  } else if (tid < 2 * kHX) {
+    x = tid - kHX;
+    y = kHY - 1;
+  } else {
+    const int k = tid - 2 * kHX;
+    y = 1 + (k >> 1);
+    x = (k & 1) ? kHX - 1 : 0;
+  }
+}
+
+// Per-tile partial of a level-0 dot product (block sum; thread 0 stores it).
+__device__ __forceinline__ void tile_partial(double (&s)[kR], int tile, double* partials) {
   double m[1] = {0.0};
   block_reduce<kR, 0>(s, m);
-  const int tid = lin_tid();
-  if (tid == 0) {
+  if (lin_tid() == 0)
     for (int n = 0; n < kR; n++) partials[(size_t)tile * kR + n] = s[n];
-    __threadfence();
-    const unsigned int t = atomicAdd(&tickets[f], 1u);
-    am_last = (t == (unsigned int)ntiles - 1);
-  }
-  __syncthreads();
-  if (!am_last) return false;
-  __threadfence();
-  double as[kR] = {0.0, 0.0}, am[1] = {0.0};
-  for (int bl = tid; bl < ntiles; bl += lin_nthreads())
-    for (int n = 0; n < kR; n++) as[n] += __ldcg(partials + (size_t)(tile0 + bl) * kR + n);
-  block_reduce<kR, 0>(as, am);
-  if (tid == 0) {
-    for (int n = 0; n < kR; n++) out[n] = as[n];
-    tickets[f] = 0u;
-    __threadfence();
-  }
-  __syncthreads();
-  return true;
+}
+
+// Sum of direction r's tile partials of frame f in tile order (one warp).
+__device__ __forceinline__ double frame_sum(const Frame2& F, int r, const double* partials) {
+  double s = 0.0;
+  for (int t = (int)threadIdx.x; t < F.ntiles; t += 32) s += __ldcg(partials + (size_t)(F.tile0 + t) * kR + r);
+  return warp_sum(s);
 }
 
 // Level-0 tile of this block: frame, 0-based cell, live flag.
@@ -201,32 +211,17 @@ __global__ void k_fm_dinv(const Frame2* __restrict__ fr, const int* __restrict__
 }
 
 // ---------------------------------------------------------------- the V-cycle
-// Residual of the first smoothing sweep from zero, restricted: on level l,
-// t = dinv b (stored as xa on levels >= 1), res = b - A t, and
-// b_{l+1} = sum of res over each 2 x 2 aggregate.  Level 0's b is r.
+// Residual of the first smoothing sweep from zero, restricted: on level
+// l >= 1, t = dinv b (stored as xa), res = b - A t, and b_{l+1} = sum of res
+// over each 2 x 2 aggregate (level 0: k_fm_restrict0).
 __global__ void __launch_bounds__(256) k_fm_restrict(const Frame2* __restrict__ fr,
                                                      const int* __restrict__ tile_frame, Batch2 b, FramesMg M, int l,
                                                      int mode) {
   __shared__ float res_s[kR][8][33];
-  int f, i, j;
-  FmLevel L;
-  bool live;
-  if (l == 0) {
-    const T0 t = t0_ref(fr, tile_frame, b.tiles);
-    const Frame2& F = fr[t.f];
-    f = t.f;
-    i = t.i;
-    j = t.j;
-    live = t.live;
-    L = FmLevel{F.nx, F.ny, F.o2};
-  } else {
-    const TL t = tl_ref(M, l);
-    f = t.f;
-    i = t.i;
-    j = t.j;
-    live = t.live;
-    L = t.L;
-  }
+  const TL t = tl_ref(M, l);
+  const int f = t.f, i = t.i, j = t.j;
+  const bool live = t.live;
+  const FmLevel L = t.L;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
   if (!act[0] && !act[1]) return;
@@ -237,7 +232,7 @@ __global__ void __launch_bounds__(256) k_fm_restrict(const Frame2* __restrict__ 
   for (int r = 0; r < kR; r++) {
     float res = 0.f;
     if (live && act[r]) {
-      const float* bb = (l == 0 ? M.r[r] : M.b[l][r]) + L.off;
+      const float* bb = M.b[l][r] + L.off;
       const float tc = dv[c] * bb[c];
       const float tw = i > 0 ? dv[c - 1] * bb[c - 1] : 0.f;
       const float tE = i + 1 < L.nx ? dv[c + 1] * bb[c + 1] : 0.f;
@@ -245,7 +240,7 @@ __global__ void __launch_bounds__(256) k_fm_restrict(const Frame2* __restrict__ 
       const float tN = j + 1 < L.ny ? dv[c + L.nx] * bb[c + L.nx] : 0.f;
       const float a = apply4(tc, tw, tE, ts, tN, i > 0 ? te[c - 1] : 0.f, te[c], j > 0 ? tn[c - L.nx] : 0.f, tn[c]);
       res = bb[c] - a;
-      if (l > 0) M.xa[l][r][L.off + c] = tc;
+      M.xa[l][r][L.off + c] = tc;
     }
     res_s[r][threadIdx.y][threadIdx.x] = res;
   }
@@ -332,175 +327,282 @@ __global__ void __launch_bounds__(256) k_fm_prolong(Batch2 b, FramesMg M, int l,
   }
 }
 
-// Level 0: y = dinv r + P xb_1, z = y + dinv (r - A y); r.z per frame and
-// direction.  Start mode (the pairs in the set): rz0 = rz, beta = 0, the
-// pair is active if rz > 0.  Iteration mode (the active pairs): the PCG
-// scalar update of the reference's pcg_iterate with this preconditioner --
-// beta = rz_new / rz, the direction update enabled, and the pair stops when
-// rz has dropped by the inner tolerance.
+// ---------------------------------------------------------------- level 0
+// The current r / p buffer of (frame f, direction r) and the other one.
+__device__ __forceinline__ int fm_par(const Batch2& b, int f, int r) { return b.iters[f * kR + r] & 1; }
+
+// Level-0 header of this block's tile.
+struct H0 {
+  T0 t;
+  int nx, ny, i0, j0, hx, hy;
+  long long o2, c;  // c: this thread's cell (valid when t.live)
+  bool halo;
+};
+__device__ __forceinline__ H0 h0_ref(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame,
+                                     const int* __restrict__ tiles) {
+  H0 h;
+  h.t = t0_ref(fr, tile_frame, tiles);
+  const Frame2& F = fr[h.t.f];
+  h.nx = F.nx;
+  h.ny = F.ny;
+  h.o2 = F.o2;
+  h.i0 = h.t.i - (int)threadIdx.x;
+  h.j0 = h.t.j - (int)threadIdx.y;
+  h.c = h.o2 + h.t.i + (long long)h.nx * h.t.j;
+  const int tid = lin_tid();
+  h.halo = tid < kHalo;
+  h.hx = h.hy = 0;
+  if (h.halo) halo_pos(tid, h.hx, h.hy);
+  return h;
+}
+// The frame cell of halo slot (hx, hy), or -1 outside the frame.
+__device__ __forceinline__ long long halo_cell(const H0& h) {
+  const int i = h.i0 - 1 + h.hx, j = h.j0 - 1 + h.hy;
+  return (i >= 0 && i < h.nx && j >= 0 && j < h.ny) ? h.o2 + i + (long long)h.nx * j : -1;
+}
+
+// q = A p with p = z + beta p_old formed on the fly (the direction update;
+// beta = 0 and p_old = 0 after a start); writes p and q, e += alpha_prev
+// p_old; p.q per tile.  The active pairs only.
+__global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame,
+                                                 Batch2 b, FramesMg M) {
+  __shared__ float ps[kR][kHY][kHX];
+  const H0 h = h0_ref(fr, tile_frame, b.tiles);
+  const int f = h.t.f;
+  bool act[kR];
+  for (int r = 0; r < kR; r++) act[r] = b.active[f * kR + r] != 0;
+  if (!act[0] && !act[1]) return;
+  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+  for (int r = 0; r < kR; r++) {
+    if (!act[r]) continue;
+    const int q = f * kR + r, par = fm_par(b, f, r);
+    const float beta = (float)b.beta[q], aprev = (float)b.alpha[q];
+    const float* __restrict__ pold = par ? M.p2[r] : M.p[r];
+    float* __restrict__ pnew = par ? M.p[r] : M.p2[r];
+    const float* __restrict__ z = M.z[r];
+    float pn = 0.f;
+    if (h.t.live) {
+      const float po = pold[h.c];
+      pn = fmaf(beta, po, z[h.c]);
+      pnew[h.c] = pn;
+      M.e[r][h.c] = fmaf(aprev, po, M.e[r][h.c]);
+    }
+    ps[r][y][x] = pn;
+    if (h.halo) {
+      const long long c = halo_cell(h);
+      ps[r][h.hy][h.hx] = c >= 0 ? fmaf(beta, pold[c], z[c]) : 0.f;
+    }
+  }
+  __syncthreads();
+  double s[kR] = {0.0, 0.0};
+  if (h.t.live) {
+    const long long c = h.c;
+    const float tw = h.t.i > 0 ? M.te[0][c - 1] : 0.f, te = M.te[0][c];
+    const float ts = h.t.j > 0 ? M.tn[0][c - h.nx] : 0.f, tn = M.tn[0][c];
+    for (int r = 0; r < kR; r++) {
+      if (!act[r]) continue;
+      const float pc = ps[r][y][x];
+      const float qv = apply4(pc, ps[r][y][x - 1], ps[r][y][x + 1], ps[r][y - 1][x], ps[r][y + 1][x], tw, te, ts, tn);
+      M.q[r][c] = qv;
+      Sum2 acc;
+      acc.add_prod(pc, qv);
+      s[r] = acc.value();
+    }
+  }
+  tile_partial(s, h.t.tile, b.partials);
+}
+
+// alpha = rz / p.q per active pair (a breakdown stops the pair).  One warp
+// per direction, one block per frame.
+__global__ void k_fm_fin_spmv(const Frame2* __restrict__ fr, Batch2 b) {
+  const int f = blockIdx.x, r = threadIdx.y, q = f * kR + r;
+  if (!b.active[q]) return;
+  const double pq = frame_sum(fr[f], r, b.partials);
+  if (threadIdx.x != 0) return;
+  if (!(pq > 0) || !(b.rz[q] > 0)) {
+    b.active[q] = 0;
+    b.alpha[q] = 0;
+  } else {
+    b.alpha[q] = b.rz[q] / pq;
+  }
+}
+
+// Level-0 restriction: r = r_old - alpha q (iteration mode; written to the
+// other r buffer), t = dinv r (the first smoothing sweep from zero),
+// b_1 = sum over each 2 x 2 aggregate of r - A t.
+__global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__ fr,
+                                                      const int* __restrict__ tile_frame, Batch2 b, FramesMg M,
+                                                      int mode) {
+  __shared__ float ts_s[kR][kHY][kHX];
+  __shared__ float res_s[kR][8][33];
+  const H0 h = h0_ref(fr, tile_frame, b.tiles);
+  const int f = h.t.f;
+  bool act[kR];
+  for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
+  if (!act[0] && !act[1]) return;
+  const float* __restrict__ dv = M.dinv[0];
+  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+  float rown[kR] = {0.f, 0.f};
+  for (int r = 0; r < kR; r++) {
+    if (!act[r]) continue;
+    const int par = fm_par(b, f, r);
+    const float alpha = mode ? 0.f : (float)b.alpha[f * kR + r];
+    const float* __restrict__ rold = par ? M.r2[r] : M.r[r];
+    const float* __restrict__ qv = M.q[r];
+    auto rn_at = [&](long long c) { return mode ? rold[c] : fmaf(-alpha, qv[c], rold[c]); };
+    float tc = 0.f;
+    if (h.t.live) {
+      const float rn = rn_at(h.c);
+      if (!mode) (par ? M.r[r] : M.r2[r])[h.c] = rn;
+      rown[r] = rn;
+      tc = dv[h.c] * rn;
+    }
+    ts_s[r][y][x] = tc;
+    if (h.halo) {
+      const long long c = halo_cell(h);
+      ts_s[r][h.hy][h.hx] = c >= 0 ? dv[c] * rn_at(c) : 0.f;
+    }
+  }
+  __syncthreads();
+  float tw = 0.f, te = 0.f, tS = 0.f, tN = 0.f;
+  if (h.t.live) {
+    const long long c = h.c;
+    tw = h.t.i > 0 ? M.te[0][c - 1] : 0.f;
+    te = M.te[0][c];
+    tS = h.t.j > 0 ? M.tn[0][c - h.nx] : 0.f;
+    tN = M.tn[0][c];
+  }
+  for (int r = 0; r < kR; r++) {
+    float res = 0.f;
+    if (h.t.live && act[r]) {
+      const float a =
+          apply4(ts_s[r][y][x], ts_s[r][y][x - 1], ts_s[r][y][x + 1], ts_s[r][y - 1][x], ts_s[r][y + 1][x], tw, te,
+                 tS, tN);
+      res = rown[r] - a;
+    }
+    res_s[r][threadIdx.y][threadIdx.x] = res;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 1) || (threadIdx.y & 1) || !h.t.live) return;
+  const FmLevel C = M.lv[(size_t)f * kFmMaxLevels + 1];
+  const int ci = h.t.i >> 1, cj = h.t.j >> 1;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = 0; r < kR; r++) {
+    if (!act[r]) continue;
+    const float sm = (res_s[r][ty][tx] + res_s[r][ty][tx + 1]) + (res_s[r][ty + 1][tx] + res_s[r][ty + 1][tx + 1]);
+    M.b[1][r][C.off + ci + (long long)C.nx * cj] = sm;
+  }
+}
+
+// Level 0: y = dinv r + P xb_1, z = y + dinv (r - A y); r.z per tile.  The
+// pairs selected by mode (start: those in the set, reading the r that the load
+// pass wrote; iteration: the active ones, reading the r of the restriction).
 __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr,
                                                    const int* __restrict__ tile_frame, Batch2 b, FramesMg M,
                                                    int mode) {
-  const T0 t = t0_ref(fr, tile_frame, b.tiles);
-  const Frame2& F = fr[t.f];
+  __shared__ float ys[kR][kHY][kHX];
+  const H0 h = h0_ref(fr, tile_frame, b.tiles);
+  const int f = h.t.f;
   bool act[kR];
-  for (int r = 0; r < kR; r++) act[r] = on(b, t.f, r, mode);
-  if (!act[0] && !act[1]) {
-    if (!mode && t.tile == F.tile0 && lin_tid() == 0) b.dir[t.f * kR] = b.dir[t.f * kR + 1] = 0;
-    return;
+  for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
+  if (!act[0] && !act[1]) return;
+  const FmLevel C = M.lv[(size_t)f * kFmMaxLevels + 1];
+  const float* __restrict__ dv = M.dinv[0];
+  const float cs = M.cscale;
+  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+  float rown[kR] = {0.f, 0.f};
+  const float dvc = h.t.live ? dv[h.c] : 0.f;
+  for (int r = 0; r < kR; r++) {
+    if (!act[r]) continue;
+    const int par = fm_par(b, f, r) ^ (mode ? 0 : 1);
+    const float* __restrict__ rr = par ? M.r2[r] : M.r[r];
+    const float* __restrict__ xc1 = M.xb[1][r] + C.off;
+    float yc = 0.f;
+    if (h.t.live) {
+      rown[r] = rr[h.c];
+      yc = fmaf(dvc, rown[r], cs * xc1[(h.t.i >> 1) + (long long)C.nx * (h.t.j >> 1)]);
+    }
+    ys[r][y][x] = yc;
+    if (h.halo) {
+      const long long c = halo_cell(h);
+      const int i = h.i0 - 1 + h.hx, j = h.j0 - 1 + h.hy;
+      ys[r][h.hy][h.hx] = c >= 0 ? fmaf(dv[c], rr[c], cs * xc1[(i >> 1) + (long long)C.nx * (j >> 1)]) : 0.f;
+    }
   }
-  const FmLevel C = M.lv[(size_t)t.f * kFmMaxLevels + 1];
+  __syncthreads();
   double s[kR] = {0.0, 0.0};
-  Sum2 acc[kR];
-  if (t.live) {
-    const int i = t.i, j = t.j, nx = F.nx, ny = F.ny;
-    const long long c = F.o2 + i + (long long)nx * j;
-    const float* te = M.te[0];
-    const float* tn = M.tn[0];
-    const float* dv = M.dinv[0];
+  if (h.t.live) {
+    const long long c = h.c;
+    const float tw = h.t.i > 0 ? M.te[0][c - 1] : 0.f, te = M.te[0][c];
+    const float tS = h.t.j > 0 ? M.tn[0][c - h.nx] : 0.f, tN = M.tn[0][c];
     for (int r = 0; r < kR; r++) {
       if (!act[r]) continue;
-      const float* rr = M.r[r];
-      const float* xc1 = M.xb[1][r] + C.off;
-      const float cs = M.cscale;
-      auto y = [&](int ii, int jj) {
-        const long long cc = F.o2 + ii + (long long)nx * jj;
-        return fmaf(dv[cc], rr[cc], cs * xc1[(ii >> 1) + (long long)C.nx * (jj >> 1)]);
-      };
-      const float yc = y(i, j);
-      const float a = apply4(yc, i > 0 ? y(i - 1, j) : 0.f, i + 1 < nx ? y(i + 1, j) : 0.f, j > 0 ? y(i, j - 1) : 0.f,
-                             j + 1 < ny ? y(i, j + 1) : 0.f, i > 0 ? te[c - 1] : 0.f, te[c],
-                             j > 0 ? tn[c - nx] : 0.f, tn[c]);
+      const float yc = ys[r][y][x];
+      const float a = apply4(yc, ys[r][y][x - 1], ys[r][y][x + 1], ys[r][y - 1][x], ys[r][y + 1][x], tw, te, tS, tN);
       // cells without a fluid face (solid) keep z = 0, so p, e and phi stay
       // zero there as the reference's operator requires
-      const float z = dv[c] > 0.f ? fmaf(dv[c], rr[c] - a, yc) : 0.f;
-      M.z[r][c] = z;
-      acc[r].add_prod(z, rr[c]);
+      const float zv = dvc > 0.f ? fmaf(dvc, rown[r] - a, yc) : 0.f;
+      M.z[r][c] = zv;
+      Sum2 acc;
+      acc.add_prod(zv, rown[r]);
+      s[r] = acc.value();
     }
   }
-  for (int r = 0; r < kR; r++) s[r] = acc[r].value();
-  double out[kR];
-  if (fm_seg_sum(s, t.f, t.tile, F.tile0, F.ntiles, b.partials, b.tickets, out) && lin_tid() == 0) {
-    for (int r = 0; r < kR; r++) {
-      const int q = t.f * kR + r;
-      if (!act[r]) {
-        if (!mode) b.dir[q] = 0;
-        continue;
-      }
-      const double rz = out[r];
-      if (mode) {
-        b.rz[q] = rz;
-        b.rz0[q] = rz;
-        b.beta[q] = 0.0;
-        b.active[q] = rz > 0 ? 1 : 0;
-        b.dir[q] = 1;
-        continue;
-      }
-      b.iters[q] += 1;
-      if (!(rz >= 0)) {
-        b.active[q] = 0;
-        b.dir[q] = 0;
-        continue;
-      }
-      b.beta[q] = rz / b.rz[q];
-      b.rz[q] = rz;
-      b.dir[q] = 1;
-      if (rz <= b.tol2 * b.rz0[q]) b.active[q] = 0;
-    }
-  }
+  tile_partial(s, h.t.tile, b.partials);
 }
 
-// p = z + beta p for the pairs whose last scalar update asked for it (in
-// start mode only the pairs in the set: the others are mid-iteration).
-__global__ void k_fm_direction(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b,
-                               FramesMg M, int mode) {
-  const T0 t = t0_ref(fr, tile_frame, b.tiles);
-  if (!t.live) return;
-  const Frame2& F = fr[t.f];
-  const long long c = F.o2 + t.i + (long long)F.nx * t.j;
-  for (int r = 0; r < kR; r++) {
-    const int q = t.f * kR + r;
-    if (!b.dir[q] || (mode && !b.in_set[q])) continue;
-    M.p[r][c] = fmaf((float)b.beta[q], M.p[r][c], M.z[r][c]);
+// The PCG scalars after the preconditioner: start mode (the pairs in the set):
+// rz0 = rz, beta = 0, the pair is active if rz > 0.  Iteration mode (the
+// active pairs): the scalar update of the reference's pcg_iterate with this
+// preconditioner -- beta = rz_new / rz, and the pair stops when rz has
+// dropped by the inner tolerance.
+__global__ void k_fm_fin_final(const Frame2* __restrict__ fr, Batch2 b, int mode) {
+  const int f = blockIdx.x, r = threadIdx.y, q = f * kR + r;
+  if (!on(b, f, r, mode)) return;
+  const double rz = frame_sum(fr[f], r, b.partials);
+  if (threadIdx.x != 0) return;
+  if (mode) {
+    b.rz[q] = rz;
+    b.rz0[q] = rz;
+    b.beta[q] = 0.0;
+    b.active[q] = rz > 0 ? 1 : 0;
+    return;
   }
-}
-
-// q = A p, p.q per frame and direction, alpha = rz / pq (a breakdown stops the pair).
-__global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame,
-                                                 Batch2 b, FramesMg M) {
-  const T0 t = t0_ref(fr, tile_frame, b.tiles);
-  const Frame2& F = fr[t.f];
-  bool act[kR];
-  for (int r = 0; r < kR; r++) act[r] = on(b, t.f, r, 0);
-  if (!act[0] && !act[1]) return;
-  double s[kR] = {0.0, 0.0};
-  Sum2 acc[kR];
-  if (t.live) {
-    const int i = t.i, j = t.j, nx = F.nx, ny = F.ny;
-    const long long c = F.o2 + i + (long long)nx * j;
-    const float* te = M.te[0];
-    const float* tn = M.tn[0];
-    for (int r = 0; r < kR; r++) {
-      if (!act[r]) continue;
-      const float* p = M.p[r];
-      const float pc = p[c];
-      const float q = apply4(pc, i > 0 ? p[c - 1] : 0.f, i + 1 < nx ? p[c + 1] : 0.f, j > 0 ? p[c - nx] : 0.f,
-                             j + 1 < ny ? p[c + nx] : 0.f, i > 0 ? te[c - 1] : 0.f, te[c], j > 0 ? tn[c - nx] : 0.f,
-                             tn[c]);
-      M.q[r][c] = q;
-      acc[r].add_prod(pc, q);
-    }
+  b.iters[q] += 1;
+  if (!(rz >= 0)) {
+    b.active[q] = 0;
+    return;
   }
-  for (int r = 0; r < kR; r++) s[r] = acc[r].value();
-  double out[kR];
-  if (fm_seg_sum(s, t.f, t.tile, F.tile0, F.ntiles, b.partials, b.tickets, out) && lin_tid() == 0) {
-    for (int r = 0; r < kR; r++) {
-      const int q = t.f * kR + r;
-      if (!act[r]) continue;
-      if (!(out[r] > 0) || !(b.rz[q] > 0)) {
-        b.active[q] = 0;
-        b.alpha[q] = 0;
-      } else {
-        b.alpha[q] = b.rz[q] / out[r];
-      }
-    }
-  }
-}
-
-// e += alpha p, r -= alpha q.
-__global__ void k_fm_update(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b, FramesMg M) {
-  const T0 t = t0_ref(fr, tile_frame, b.tiles);
-  if (!t.live) return;
-  const Frame2& F = fr[t.f];
-  const long long c = F.o2 + t.i + (long long)F.nx * t.j;
-  for (int r = 0; r < kR; r++) {
-    const int q = t.f * kR + r;
-    if (!b.active[q]) continue;
-    const float a = (float)b.alpha[q];
-    M.e[r][c] = fmaf(a, M.p[r][c], M.e[r][c]);
-    M.r[r][c] = fmaf(-a, M.q[r][c], M.r[r][c]);
-  }
+  b.beta[q] = rz / b.rz[q];
+  b.rz[q] = rz;
+  if (rz <= b.tol2 * b.rz0[q]) b.active[q] = 0;
 }
 
 // Start of an inner solve for the pairs in the set: r = scale (rV - mean) of
-// layer 1 on fluid cells (the layers are equal), e = 0, p = 0.
+// layer 1 on fluid cells (the layers are equal), e = 0, p = 0 (the current
+// buffers), alpha = 0 (nothing pending for e).
 __global__ void k_fm_load(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b, FramesMg M) {
   const T0 t = t0_ref(fr, tile_frame, nullptr);
-  if (!t.live) return;
   const Frame2& F = fr[t.f];
+  if (t.tile == F.tile0 && lin_tid() < kR && b.in_set[t.f * kR + lin_tid()]) b.alpha[t.f * kR + lin_tid()] = 0.0;
+  if (!t.live) return;
   const long long c = F.o2 + t.i + (long long)F.nx * t.j;
   const long long c3 = F.oint + t.i + (long long)F.nx * t.j;  // layer 1 of the 3-D interior fields
   const bool fl = b.diag[c3] > 0;
   for (int r = 0; r < kR; r++) {
     const int q = t.f * kR + r;
     if (!b.in_set[q]) continue;
-    M.r[r][c] = fl ? (float)((b.r64[r][c3] - b.rmean[q]) * b.scale[q]) : 0.f;
+    const int par = fm_par(b, t.f, r);
+    (par ? M.r2[r] : M.r[r])[c] = fl ? (float)((b.r64[r][c3] - b.rmean[q]) * b.scale[q]) : 0.f;
     M.e[r][c] = 0.f;
-    M.p[r][c] = 0.f;
+    (par ? M.p2[r] : M.p[r])[c] = 0.f;
   }
 }
 
-// phi += e / scale in both layers on fluid cells, for the pairs in the set.
+// phi += (e + alpha p) / scale in both layers on fluid cells, for the pairs in
+// the set: the correction with the last iteration's alpha p, which the spmv
+// pass adds to e only in the iteration after (alpha is zero after a
+// breakdown and after a load).
 __global__ void k_fm_apply(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame, Batch2 b, FramesMg M) {
   const T0 t = t0_ref(fr, tile_frame, nullptr);
   if (!t.live) return;
@@ -512,7 +614,10 @@ __global__ void k_fm_apply(const Frame2* __restrict__ fr, const int* __restrict_
   for (int r = 0; r < kR; r++) {
     const int q = t.f * kR + r;
     if (!b.in_set[q]) continue;
-    const double d = (double)M.e[r][c] / b.scale[q];
+    const float a = (float)b.alpha[q];
+    const float* __restrict__ p = fm_par(b, t.f, r) ? M.p2[r] : M.p[r];
+    const float ec = a != 0.f ? fmaf(a, p[c], M.e[r][c]) : M.e[r][c];
+    const double d = (double)ec / b.scale[q];
     b.phi[r][p1] += d;
     b.phi[r][p1 + pl] += d;
   }
@@ -534,13 +639,13 @@ cudaError_t fm_setup(const Frame2* fr, const int* tf, int ntiles, const Batch2& 
 }
 
 // The preconditioner z = M r for the pairs selected by mode, ending in
-// k_fm_final0 (which also updates the PCG scalars).  nact: level-0 blocks
-// (the compacted tile list in b.tiles when b.tiles is set); ntiles_lv[l]:
-// tiles of the frames whose level l is not their coarsest (level l's list).
+// k_fm_final0 and the scalar update.  nact: level-0 blocks (the compacted tile
+// list in b.tiles when b.tiles is set); nrestrict_lv[l]: tiles of the frames
+// whose level l is not their coarsest (level l's list).
 static cudaError_t fm_cycle(const Frame2* fr, const int* tf, int nact, const Batch2& b, const FramesMg& M,
                             const int* nrestrict_lv, int nframes, int mode, cudaStream_t st) {
   const dim3 blk(32, 8);
-  k_fm_restrict<<<nact, blk, 0, st>>>(fr, tf, b, M, 0, mode); note_launch();
+  k_fm_restrict0<<<nact, blk, 0, st>>>(fr, tf, b, M, mode); note_launch();
   for (int l = 1; l + 1 < M.nlev; l++) {
     if (nrestrict_lv[l] == 0) break;
     k_fm_restrict<<<nrestrict_lv[l], blk, 0, st>>>(fr, tf, b, M, l, mode); note_launch();
@@ -551,6 +656,7 @@ static cudaError_t fm_cycle(const Frame2* fr, const int* tf, int nact, const Bat
     k_fm_prolong<<<nrestrict_lv[l], blk, 0, st>>>(b, M, l, mode); note_launch();
   }
   k_fm_final0<<<nact, blk, 0, st>>>(fr, tf, b, M, mode); note_launch();
+  k_fm_fin_final<<<nframes, dim3(32, kR), 0, st>>>(fr, b, mode); note_launch();
   return cudaGetLastError();
 }
 
@@ -560,21 +666,15 @@ cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, const Batch2& 
   Batch2 b0 = b;
   b0.tiles = nullptr;  // all level-0 tiles
   k_fm_load<<<ntiles, blk, 0, st>>>(fr, tf, b0, M); note_launch();
-  cudaError_t e = fm_cycle(fr, tf, ntiles, b0, M, nrestrict_lv, nframes, 1, st);
-  if (e != cudaSuccess) return e;
-  k_fm_direction<<<ntiles, blk, 0, st>>>(fr, tf, b0, M, 1); note_launch();
-  return cudaGetLastError();
+  return fm_cycle(fr, tf, ntiles, b0, M, nrestrict_lv, nframes, 1, st);
 }
 
 cudaError_t fm_iteration(const Frame2* fr, const int* tf, int nact, const Batch2& b, const FramesMg& M,
                          const int* nrestrict_lv, int nframes, cudaStream_t st) {
   const dim3 blk(32, 8);
   k_fm_spmv<<<nact, blk, 0, st>>>(fr, tf, b, M); note_launch();
-  k_fm_update<<<nact, blk, 0, st>>>(fr, tf, b, M); note_launch();
-  cudaError_t e = fm_cycle(fr, tf, nact, b, M, nrestrict_lv, nframes, 0, st);
-  if (e != cudaSuccess) return e;
-  k_fm_direction<<<nact, blk, 0, st>>>(fr, tf, b, M, 0); note_launch();
-  return cudaGetLastError();
+  k_fm_fin_spmv<<<nframes, dim3(32, kR), 0, st>>>(fr, b); note_launch();
+  return fm_cycle(fr, tf, nact, b, M, nrestrict_lv, nframes, 0, st);
 }
 
 cudaError_t fm_apply(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,

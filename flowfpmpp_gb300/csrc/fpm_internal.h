@@ -259,6 +259,7 @@ struct FramesMg {
   float *te[kFmMaxLevels], *tn[kFmMaxLevels], *dinv[kFmMaxLevels];  // faces east / north, omega / diag
   float *b[kFmMaxLevels][2], *xa[kFmMaxLevels][2], *xb[kFmMaxLevels][2];  // levels >= 1, per direction
   float *r[2], *z[2], *p[2], *q[2], *e[2];  // level 0 (2-D frame layout), per direction
+  float *r2[2], *p2[2];  // second r and p buffers (the current one: iterations & 1)
   float omega;
   float cscale;  // scale of the prolonged coarse correction (the cycle stays symmetric)
   int coarse_sweeps;
