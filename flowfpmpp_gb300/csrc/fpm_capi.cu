@@ -2466,6 +2466,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     FramesMg M;
     std::memset(&M, 0, sizeof(M));
     std::vector<int> nrestrict_lv(kFmMaxLevels, 0), nall_lv(kFmMaxLevels, 0);
+    int nbtiles = 0;
+    std::vector<int4> hbt_info;
     if (batched_mg) {
       Trace tm("frames: multigrid set-up");
       std::vector<int> nlev(nframes);
@@ -2530,6 +2532,19 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         M.r2[r] = A.get<float>(n2);
         M.p2[r] = A.get<float>(n2);
       }
+      // level-0 block tiles (32 x 32 cells) of the stencil passes
+      std::vector<int> bt_frame;
+      std::vector<int4> bt_info(nframes);
+      for (int f = 0; f < nframes; f++) {
+        const int bx = (fr[f].nx + 31) / 32, nbt = bx * ((fr[f].ny + 31) / 32);
+        bt_info[f] = make_int4((int)bt_frame.size(), nbt, bx, 0);
+        for (int t = 0; t < nbt; t++) bt_frame.push_back(f);
+      }
+      nbtiles = (int)bt_frame.size();
+      M.bt_frame = A.upload(bt_frame.data(), bt_frame.size());
+      M.bt_info = A.upload(bt_info.data(), bt_info.size());
+      M.bt_list = A.get<int>(nbtiles);
+      hbt_info = bt_info;
       CUDA_TRY(fm_setup(dfr, dtf, ntiles, b, M, nall_lv.data(), st));
     }
     if (frames_mg) {
@@ -2544,7 +2559,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       push_set();
       CUDA_TRY(cudaMemcpyAsync(b.scale, scale.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
       CUDA_TRY(cudaMemcpyAsync(b.pmul, pmul.data(), nq * sizeof(double), cudaMemcpyHostToDevice, st));
-      if (batched_mg) CUDA_TRY(fm_start(dfr, dtf, ntiles, b, M, nrestrict_lv.data(), nframes, st));
+      if (batched_mg) CUDA_TRY(fm_start(dfr, dtf, ntiles, nbtiles, b, M, nrestrict_lv.data(), nframes, st));
       else CUDA_TRY(launch_k_b2_start(dfr, dtf, ntiles, b, st));
     };
     if (any) push_start();
@@ -2555,7 +2570,8 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
     std::vector<char> frame_on(nframes, 0);
     Batch2 bi = b;
     bi.tiles = dtiles;
-    int nact = 0;
+    int nact = 0, nbact = 0;
+    std::vector<int> act_bt;
     auto rebuild_tiles = [&]() {
       bool changed = false;
       for (int f = 0; f < nframes; f++) {
@@ -2570,6 +2586,15 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
           for (int t = 0; t < fr[f].ntiles; t++) act_tiles.push_back(fr[f].tile0 + t);
       nact = (int)act_tiles.size();
       if (nact) CUDA_TRY(cudaMemcpyAsync(dtiles, act_tiles.data(), nact * sizeof(int), cudaMemcpyHostToDevice, st));
+      if (batched_mg) {
+        act_bt.clear();
+        for (int f = 0; f < nframes; f++)
+          if (frame_on[f])
+            for (int t = 0; t < hbt_info[f].y; t++) act_bt.push_back(hbt_info[f].x + t);
+        nbact = (int)act_bt.size();
+        if (nbact)
+          CUDA_TRY(cudaMemcpyAsync(M.bt_list, act_bt.data(), nbact * sizeof(int), cudaMemcpyHostToDevice, st));
+      }
       graphs.clear();
     };
     rebuild_tiles();
@@ -2592,7 +2617,7 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
       {
         TimedRun t(FPM_TIMER_FRAMES_ITER, chunk, st);
         graphs.run(chunk, st, [&](cudaStream_t s2) {
-          if (batched_mg) CUDA_TRY(fm_iteration(dfr, dtf, nact, bi, M, nrestrict_lv.data(), nframes, s2));
+          if (batched_mg) CUDA_TRY(fm_iteration(dfr, nbact, bi, M, nrestrict_lv.data(), nframes, s2));
           else CUDA_TRY(launch_b2_iteration(dfr, dtf, nact, bi, s2));
         });
       }

@@ -60,20 +60,22 @@ struct Sum2 {
   __device__ __forceinline__ double value() const { return (double)s + (double)e; }
 };
 
-// The level-0 operand tile with its halo: cell (i0 - 1 + x, j0 - 1 + y) of the
-// frame at [y][x]; threads 0 .. kHalo - 1 fill the halo.
-constexpr int kHX = 34, kHY = 10, kHalo = 2 * kHX + 2 * 8;
-__device__ __forceinline__ void halo_pos(int tid, int& x, int& y) {
-  if (tid < kHX) {
+// Level-0 stencil passes work on block tiles of 32 x 32 cells (a thread owns
+// column x and rows y, y + 8, y + 16, y + 24) with the operand and its
+// one-cell halo in shared memory: cell (i0 - 1 + x, j0 - 1 + y) of the frame
+// at [y][x]; threads 0 .. kBHalo - 1 fill the halo.
+constexpr int kBT = 32, kBH = kBT + 2, kBRows = kBT / 8, kBHalo = 4 * kBT + 4;
+__device__ __forceinline__ void bhalo_pos(int tid, int& x, int& y) {
+  if (tid < kBH) {
     x = tid;
     y = 0;
-  } else if (tid < 2 * kHX) {
-    x = tid - kHX;
-    y = kHY - 1;
+  } else if (tid < 2 * kBH) {
+    x = tid - kBH;
+    y = kBH - 1;
   } else {
-    const int k = tid - 2 * kHX;
+    const int k = tid - 2 * kBH;
     y = 1 + (k >> 1);
-    x = (k & 1) ? kHX - 1 : 0;
+    x = (k & 1) ? kBH - 1 : 0;
   }
 }
 
@@ -85,10 +87,10 @@ __device__ __forceinline__ void tile_partial(double (&s)[kR], int tile, double* 
     for (int n = 0; n < kR; n++) partials[(size_t)tile * kR + n] = s[n];
 }
 
-// Sum of direction r's tile partials of frame f in tile order (one warp).
-__device__ __forceinline__ double frame_sum(const Frame2& F, int r, const double* partials) {
+// Sum of direction r's block-tile partials of frame f in tile order (one warp).
+__device__ __forceinline__ double frame_sum(const int4 bi, int r, const double* partials) {
   double s = 0.0;
-  for (int t = (int)threadIdx.x; t < F.ntiles; t += 32) s += __ldcg(partials + (size_t)(F.tile0 + t) * kR + r);
+  for (int t = (int)threadIdx.x; t < bi.y; t += 32) s += __ldcg(partials + (size_t)(bi.x + t) * kR + r);
   return warp_sum(s);
 }
 
@@ -331,48 +333,60 @@ __global__ void __launch_bounds__(256) k_fm_prolong(Batch2 b, FramesMg M, int l,
 // The current r / p buffer of (frame f, direction r) and the other one.
 __device__ __forceinline__ int fm_par(const Batch2& b, int f, int r) { return b.iters[f * kR + r] & 1; }
 
-// Level-0 header of this block's tile.
-struct H0 {
-  T0 t;
-  int nx, ny, i0, j0, hx, hy;
-  long long o2, c;  // c: this thread's cell (valid when t.live)
+// Level-0 block tile of this block.
+struct B0 {
+  int tile, f, nx, ny, i0, j0, hx, hy;
+  long long o2;
   bool halo;
 };
-__device__ __forceinline__ H0 h0_ref(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame,
-                                     const int* __restrict__ tiles) {
-  H0 h;
-  h.t = t0_ref(fr, tile_frame, tiles);
-  const Frame2& F = fr[h.t.f];
+__device__ __forceinline__ B0 b0_ref(const Frame2* __restrict__ fr, const FramesMg& M, const int* __restrict__ list) {
+  B0 h;
+  h.tile = list ? list[blockIdx.x] : (int)blockIdx.x;
+  h.f = M.bt_frame[h.tile];
+  const int4 bi = M.bt_info[h.f];
+  const Frame2& F = fr[h.f];
   h.nx = F.nx;
   h.ny = F.ny;
   h.o2 = F.o2;
-  h.i0 = h.t.i - (int)threadIdx.x;
-  h.j0 = h.t.j - (int)threadIdx.y;
-  h.c = h.o2 + h.t.i + (long long)h.nx * h.t.j;
+  const int idx = h.tile - bi.x;
+  h.i0 = (idx % bi.z) * kBT;
+  h.j0 = (idx / bi.z) * kBT;
   const int tid = lin_tid();
-  h.halo = tid < kHalo;
+  h.halo = tid < kBHalo;
   h.hx = h.hy = 0;
-  if (h.halo) halo_pos(tid, h.hx, h.hy);
+  if (h.halo) bhalo_pos(tid, h.hx, h.hy);
   return h;
 }
-// The frame cell of halo slot (hx, hy), or -1 outside the frame.
-__device__ __forceinline__ long long halo_cell(const H0& h) {
+// Frame cell of row k of this thread (-1 outside the frame), and of its halo slot.
+__device__ __forceinline__ long long own_cell(const B0& h, int k) {
+  const int i = h.i0 + (int)threadIdx.x, j = h.j0 + (int)threadIdx.y + 8 * k;
+  return (i < h.nx && j < h.ny) ? h.o2 + i + (long long)h.nx * j : -1;
+}
+__device__ __forceinline__ long long halo_cell(const B0& h) {
   const int i = h.i0 - 1 + h.hx, j = h.j0 - 1 + h.hy;
   return (i >= 0 && i < h.nx && j >= 0 && j < h.ny) ? h.o2 + i + (long long)h.nx * j : -1;
+}
+// Faces of an own cell: west, east, south, north.
+__device__ __forceinline__ float4 faces_of(const B0& h, const FramesMg& M, long long c, int k) {
+  const int i = h.i0 + (int)threadIdx.x, j = h.j0 + (int)threadIdx.y + 8 * k;
+  return make_float4(i > 0 ? M.te[0][c - 1] : 0.f, M.te[0][c], j > 0 ? M.tn[0][c - h.nx] : 0.f, M.tn[0][c]);
+}
+// A x at smem cell (x, y) of a haloed tile.
+__device__ __forceinline__ float apply_s(const float (&v)[kBH][kBH], int x, int y, float4 t) {
+  return apply4(v[y][x], v[y][x - 1], v[y][x + 1], v[y - 1][x], v[y + 1][x], t.x, t.y, t.z, t.w);
 }
 
 // q = A p with p = z + beta p_old formed on the fly (the direction update;
 // beta = 0 and p_old = 0 after a start); writes p and q, e += alpha_prev
-// p_old; p.q per tile.  The active pairs only.
-__global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, const int* __restrict__ tile_frame,
-                                                 Batch2 b, FramesMg M) {
-  __shared__ float ps[kR][kHY][kHX];
-  const H0 h = h0_ref(fr, tile_frame, b.tiles);
-  const int f = h.t.f;
+// p_old; p.q per block tile.  The active pairs only.
+__global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, Batch2 b, FramesMg M) {
+  __shared__ float ps[kR][kBH][kBH];
+  const B0 h = b0_ref(fr, M, M.bt_list);
+  const int f = h.f;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = b.active[f * kR + r] != 0;
   if (!act[0] && !act[1]) return;
-  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+  const int x = threadIdx.x + 1;
   for (int r = 0; r < kR; r++) {
     if (!act[r]) continue;
     const int q = f * kR + r, par = fm_par(b, f, r);
@@ -380,44 +394,57 @@ __global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, 
     const float* __restrict__ pold = par ? M.p2[r] : M.p[r];
     float* __restrict__ pnew = par ? M.p[r] : M.p2[r];
     const float* __restrict__ z = M.z[r];
-    float pn = 0.f;
-    if (h.t.live) {
-      const float po = pold[h.c];
-      pn = fmaf(beta, po, z[h.c]);
-      pnew[h.c] = pn;
-      M.e[r][h.c] = fmaf(aprev, po, M.e[r][h.c]);
+    float* __restrict__ e = M.e[r];
+    // all loads of the pass first (own rows and the halo slot), then the stores
+    long long cc[kBRows];
+    float po[kBRows], zz[kBRows], ee[kBRows];
+#pragma unroll
+    for (int k = 0; k < kBRows; k++) {
+      cc[k] = own_cell(h, k);
+      po[k] = cc[k] >= 0 ? pold[cc[k]] : 0.f;
+      zz[k] = cc[k] >= 0 ? z[cc[k]] : 0.f;
+      ee[k] = cc[k] >= 0 ? e[cc[k]] : 0.f;
     }
-    ps[r][y][x] = pn;
-    if (h.halo) {
-      const long long c = halo_cell(h);
-      ps[r][h.hy][h.hx] = c >= 0 ? fmaf(beta, pold[c], z[c]) : 0.f;
+    const long long ch = h.halo ? halo_cell(h) : -1;
+    const float hp = ch >= 0 ? pold[ch] : 0.f, hz = ch >= 0 ? z[ch] : 0.f;
+#pragma unroll
+    for (int k = 0; k < kBRows; k++) {
+      const float pn = fmaf(beta, po[k], zz[k]);
+      if (cc[k] >= 0) {
+        pnew[cc[k]] = pn;
+        e[cc[k]] = fmaf(aprev, po[k], ee[k]);
+      }
+      ps[r][threadIdx.y + 1 + 8 * k][x] = cc[k] >= 0 ? pn : 0.f;
     }
+    if (h.halo) ps[r][h.hy][h.hx] = ch >= 0 ? fmaf(beta, hp, hz) : 0.f;
   }
   __syncthreads();
-  double s[kR] = {0.0, 0.0};
-  if (h.t.live) {
-    const long long c = h.c;
-    const float tw = h.t.i > 0 ? M.te[0][c - 1] : 0.f, te = M.te[0][c];
-    const float ts = h.t.j > 0 ? M.tn[0][c - h.nx] : 0.f, tn = M.tn[0][c];
+  Sum2 acc[kR];
+#pragma unroll
+  for (int k = 0; k < kBRows; k++) {
+    const long long c = own_cell(h, k);
+    if (c < 0) continue;
+    const float4 t = faces_of(h, M, c, k);
+    const int y = threadIdx.y + 1 + 8 * k;
     for (int r = 0; r < kR; r++) {
       if (!act[r]) continue;
       const float pc = ps[r][y][x];
-      const float qv = apply4(pc, ps[r][y][x - 1], ps[r][y][x + 1], ps[r][y - 1][x], ps[r][y + 1][x], tw, te, ts, tn);
+      const float qv = apply_s(ps[r], x, y, t);
       M.q[r][c] = qv;
-      Sum2 acc;
-      acc.add_prod(pc, qv);
-      s[r] = acc.value();
+      acc[r].add_prod(pc, qv);
     }
   }
-  tile_partial(s, h.t.tile, b.partials);
+  double s[kR];
+  for (int r = 0; r < kR; r++) s[r] = acc[r].value();
+  tile_partial(s, h.tile, b.partials);
 }
 
 // alpha = rz / p.q per active pair (a breakdown stops the pair).  One warp
 // per direction, one block per frame.
-__global__ void k_fm_fin_spmv(const Frame2* __restrict__ fr, Batch2 b) {
+__global__ void k_fm_fin_spmv(FramesMg M, Batch2 b) {
   const int f = blockIdx.x, r = threadIdx.y, q = f * kR + r;
   if (!b.active[q]) return;
-  const double pq = frame_sum(fr[f], r, b.partials);
+  const double pq = frame_sum(M.bt_info[f], r, b.partials);
   if (threadIdx.x != 0) return;
   if (!(pq > 0) || !(b.rz[q] > 0)) {
     b.active[q] = 0;
@@ -430,125 +457,139 @@ __global__ void k_fm_fin_spmv(const Frame2* __restrict__ fr, Batch2 b) {
 // Level-0 restriction: r = r_old - alpha q (iteration mode; written to the
 // other r buffer), t = dinv r (the first smoothing sweep from zero),
 // b_1 = sum over each 2 x 2 aggregate of r - A t.
-__global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__ fr,
-                                                      const int* __restrict__ tile_frame, Batch2 b, FramesMg M,
-                                                      int mode) {
-  __shared__ float ts_s[kR][kHY][kHX];
-  __shared__ float res_s[kR][8][33];
-  const H0 h = h0_ref(fr, tile_frame, b.tiles);
-  const int f = h.t.f;
+__global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__ fr, Batch2 b, FramesMg M,
+                                                      const int* __restrict__ list, int mode) {
+  __shared__ float ts_s[kR][kBH][kBH];
+  __shared__ float res_s[kR][kBT][kBT + 1];
+  const B0 h = b0_ref(fr, M, list);
+  const int f = h.f;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
   if (!act[0] && !act[1]) return;
   const float* __restrict__ dv = M.dinv[0];
-  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
-  float rown[kR] = {0.f, 0.f};
+  const int x = threadIdx.x + 1;
+  float rown[kR][kBRows];
   for (int r = 0; r < kR; r++) {
     if (!act[r]) continue;
     const int par = fm_par(b, f, r);
     const float alpha = mode ? 0.f : (float)b.alpha[f * kR + r];
     const float* __restrict__ rold = par ? M.r2[r] : M.r[r];
+    float* __restrict__ rnew = par ? M.r[r] : M.r2[r];
     const float* __restrict__ qv = M.q[r];
-    auto rn_at = [&](long long c) { return mode ? rold[c] : fmaf(-alpha, qv[c], rold[c]); };
-    float tc = 0.f;
-    if (h.t.live) {
-      const float rn = rn_at(h.c);
-      if (!mode) (par ? M.r[r] : M.r2[r])[h.c] = rn;
-      rown[r] = rn;
-      tc = dv[h.c] * rn;
+    // all loads of the pass first (own rows and the halo slot), then the stores
+    long long cc[kBRows];
+    float ro[kBRows], qq[kBRows], dd[kBRows];
+#pragma unroll
+    for (int k = 0; k < kBRows; k++) {
+      cc[k] = own_cell(h, k);
+      ro[k] = cc[k] >= 0 ? rold[cc[k]] : 0.f;
+      qq[k] = cc[k] >= 0 && !mode ? qv[cc[k]] : 0.f;
+      dd[k] = cc[k] >= 0 ? dv[cc[k]] : 0.f;
     }
-    ts_s[r][y][x] = tc;
-    if (h.halo) {
-      const long long c = halo_cell(h);
-      ts_s[r][h.hy][h.hx] = c >= 0 ? dv[c] * rn_at(c) : 0.f;
+    const long long ch = h.halo ? halo_cell(h) : -1;
+    const float hr = ch >= 0 ? rold[ch] : 0.f, hq = ch >= 0 && !mode ? qv[ch] : 0.f, hd = ch >= 0 ? dv[ch] : 0.f;
+#pragma unroll
+    for (int k = 0; k < kBRows; k++) {
+      const float rn = mode ? ro[k] : fmaf(-alpha, qq[k], ro[k]);
+      if (cc[k] >= 0 && !mode) rnew[cc[k]] = rn;
+      rown[r][k] = cc[k] >= 0 ? rn : 0.f;
+      ts_s[r][threadIdx.y + 1 + 8 * k][x] = cc[k] >= 0 ? dd[k] * rn : 0.f;
+    }
+    if (h.halo) ts_s[r][h.hy][h.hx] = ch >= 0 ? hd * (mode ? hr : fmaf(-alpha, hq, hr)) : 0.f;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kBRows; k++) {
+    const long long c = own_cell(h, k);
+    const int y = threadIdx.y + 1 + 8 * k;
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c >= 0) t = faces_of(h, M, c, k);
+    for (int r = 0; r < kR; r++) {
+      float res = 0.f;
+      if (c >= 0 && act[r]) res = rown[r][k] - apply_s(ts_s[r], x, y, t);
+      res_s[r][y - 1][threadIdx.x] = res;
     }
   }
   __syncthreads();
-  float tw = 0.f, te = 0.f, tS = 0.f, tN = 0.f;
-  if (h.t.live) {
-    const long long c = h.c;
-    tw = h.t.i > 0 ? M.te[0][c - 1] : 0.f;
-    te = M.te[0][c];
-    tS = h.t.j > 0 ? M.tn[0][c - h.nx] : 0.f;
-    tN = M.tn[0][c];
-  }
-  for (int r = 0; r < kR; r++) {
-    float res = 0.f;
-    if (h.t.live && act[r]) {
-      const float a =
-          apply4(ts_s[r][y][x], ts_s[r][y][x - 1], ts_s[r][y][x + 1], ts_s[r][y - 1][x], ts_s[r][y + 1][x], tw, te,
-                 tS, tN);
-      res = rown[r] - a;
-    }
-    res_s[r][threadIdx.y][threadIdx.x] = res;
-  }
-  __syncthreads();
-  if ((threadIdx.x & 1) || (threadIdx.y & 1) || !h.t.live) return;
+  // one 2 x 2 aggregate per thread
+  const int tid = lin_tid(), ax = tid & 15, ay = tid >> 4;
+  const int i = h.i0 + 2 * ax, j = h.j0 + 2 * ay;
+  if (i >= h.nx || j >= h.ny) return;
   const FmLevel C = M.lv[(size_t)f * kFmMaxLevels + 1];
-  const int ci = h.t.i >> 1, cj = h.t.j >> 1;
-  const int tx = threadIdx.x, ty = threadIdx.y;
   for (int r = 0; r < kR; r++) {
     if (!act[r]) continue;
-    const float sm = (res_s[r][ty][tx] + res_s[r][ty][tx + 1]) + (res_s[r][ty + 1][tx] + res_s[r][ty + 1][tx + 1]);
-    M.b[1][r][C.off + ci + (long long)C.nx * cj] = sm;
+    const float sm = (res_s[r][2 * ay][2 * ax] + res_s[r][2 * ay][2 * ax + 1]) +
+                     (res_s[r][2 * ay + 1][2 * ax] + res_s[r][2 * ay + 1][2 * ax + 1]);
+    M.b[1][r][C.off + (i >> 1) + (long long)C.nx * (j >> 1)] = sm;
   }
 }
 
-// Level 0: y = dinv r + P xb_1, z = y + dinv (r - A y); r.z per tile.  The
-// pairs selected by mode (start: those in the set, reading the r that the load
-// pass wrote; iteration: the active ones, reading the r of the restriction).
-__global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr,
-                                                   const int* __restrict__ tile_frame, Batch2 b, FramesMg M,
-                                                   int mode) {
-  __shared__ float ys[kR][kHY][kHX];
-  const H0 h = h0_ref(fr, tile_frame, b.tiles);
-  const int f = h.t.f;
+// Level 0: y = dinv r + P xb_1, z = y + dinv (r - A y); r.z per block tile.
+// The pairs selected by mode (start: those in the set, reading the r that the
+// load pass wrote; iteration: the active ones, reading the r of the
+// restriction).
+__global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr, Batch2 b, FramesMg M,
+                                                   const int* __restrict__ list, int mode) {
+  __shared__ float ys[kR][kBH][kBH];
+  const B0 h = b0_ref(fr, M, list);
+  const int f = h.f;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
   if (!act[0] && !act[1]) return;
   const FmLevel C = M.lv[(size_t)f * kFmMaxLevels + 1];
   const float* __restrict__ dv = M.dinv[0];
   const float cs = M.cscale;
-  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
-  float rown[kR] = {0.f, 0.f};
-  const float dvc = h.t.live ? dv[h.c] : 0.f;
+  const int x = threadIdx.x + 1;
+  float rown[kR][kBRows], dvc[kBRows];
+#pragma unroll
+  for (int k = 0; k < kBRows; k++) {
+    const long long c = own_cell(h, k);
+    dvc[k] = c >= 0 ? dv[c] : 0.f;
+  }
   for (int r = 0; r < kR; r++) {
     if (!act[r]) continue;
     const int par = fm_par(b, f, r) ^ (mode ? 0 : 1);
     const float* __restrict__ rr = par ? M.r2[r] : M.r[r];
     const float* __restrict__ xc1 = M.xb[1][r] + C.off;
-    float yc = 0.f;
-    if (h.t.live) {
-      rown[r] = rr[h.c];
-      yc = fmaf(dvc, rown[r], cs * xc1[(h.t.i >> 1) + (long long)C.nx * (h.t.j >> 1)]);
+    auto parent = [&](int i, int j) { return cs * xc1[(i >> 1) + (long long)C.nx * (j >> 1)]; };
+    // all loads of the pass first (own rows and the halo slot), then the stores
+    float pa[kBRows];
+#pragma unroll
+    for (int k = 0; k < kBRows; k++) {
+      const long long c = own_cell(h, k);
+      rown[r][k] = c >= 0 ? rr[c] : 0.f;
+      pa[k] = c >= 0 ? parent(h.i0 + (int)threadIdx.x, h.j0 + (int)threadIdx.y + 8 * k) : 0.f;
     }
-    ys[r][y][x] = yc;
-    if (h.halo) {
-      const long long c = halo_cell(h);
-      const int i = h.i0 - 1 + h.hx, j = h.j0 - 1 + h.hy;
-      ys[r][h.hy][h.hx] = c >= 0 ? fmaf(dv[c], rr[c], cs * xc1[(i >> 1) + (long long)C.nx * (j >> 1)]) : 0.f;
-    }
+    const long long ch = h.halo ? halo_cell(h) : -1;
+    const float hr = ch >= 0 ? rr[ch] : 0.f, hd = ch >= 0 ? dv[ch] : 0.f;
+    const float hpa = ch >= 0 ? parent(h.i0 - 1 + h.hx, h.j0 - 1 + h.hy) : 0.f;
+#pragma unroll
+    for (int k = 0; k < kBRows; k++)
+      ys[r][threadIdx.y + 1 + 8 * k][x] = own_cell(h, k) >= 0 ? fmaf(dvc[k], rown[r][k], pa[k]) : 0.f;
+    if (h.halo) ys[r][h.hy][h.hx] = ch >= 0 ? fmaf(hd, hr, hpa) : 0.f;
   }
   __syncthreads();
-  double s[kR] = {0.0, 0.0};
-  if (h.t.live) {
-    const long long c = h.c;
-    const float tw = h.t.i > 0 ? M.te[0][c - 1] : 0.f, te = M.te[0][c];
-    const float tS = h.t.j > 0 ? M.tn[0][c - h.nx] : 0.f, tN = M.tn[0][c];
+  Sum2 acc[kR];
+#pragma unroll
+  for (int k = 0; k < kBRows; k++) {
+    const long long c = own_cell(h, k);
+    if (c < 0) continue;
+    const float4 t = faces_of(h, M, c, k);
+    const int y = threadIdx.y + 1 + 8 * k;
     for (int r = 0; r < kR; r++) {
       if (!act[r]) continue;
       const float yc = ys[r][y][x];
-      const float a = apply4(yc, ys[r][y][x - 1], ys[r][y][x + 1], ys[r][y - 1][x], ys[r][y + 1][x], tw, te, tS, tN);
+      const float a = apply_s(ys[r], x, y, t);
       // cells without a fluid face (solid) keep z = 0, so p, e and phi stay
       // zero there as the reference's operator requires
-      const float zv = dvc > 0.f ? fmaf(dvc, rown[r] - a, yc) : 0.f;
+      const float zv = dvc[k] > 0.f ? fmaf(dvc[k], rown[r][k] - a, yc) : 0.f;
       M.z[r][c] = zv;
-      Sum2 acc;
-      acc.add_prod(zv, rown[r]);
-      s[r] = acc.value();
+      acc[r].add_prod(zv, rown[r][k]);
     }
   }
-  tile_partial(s, h.t.tile, b.partials);
+  double s[kR];
+  for (int r = 0; r < kR; r++) s[r] = acc[r].value();
+  tile_partial(s, h.tile, b.partials);
 }
 
 // The PCG scalars after the preconditioner: start mode (the pairs in the set):
@@ -556,10 +597,10 @@ __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr
 // active pairs): the scalar update of the reference's pcg_iterate with this
 // preconditioner -- beta = rz_new / rz, and the pair stops when rz has
 // dropped by the inner tolerance.
-__global__ void k_fm_fin_final(const Frame2* __restrict__ fr, Batch2 b, int mode) {
+__global__ void k_fm_fin_final(FramesMg M, Batch2 b, int mode) {
   const int f = blockIdx.x, r = threadIdx.y, q = f * kR + r;
   if (!on(b, f, r, mode)) return;
-  const double rz = frame_sum(fr[f], r, b.partials);
+  const double rz = frame_sum(M.bt_info[f], r, b.partials);
   if (threadIdx.x != 0) return;
   if (mode) {
     b.rz[q] = rz;
@@ -639,42 +680,40 @@ cudaError_t fm_setup(const Frame2* fr, const int* tf, int ntiles, const Batch2& 
 }
 
 // The preconditioner z = M r for the pairs selected by mode, ending in
-// k_fm_final0 and the scalar update.  nact: level-0 blocks (the compacted tile
-// list in b.tiles when b.tiles is set); nrestrict_lv[l]: tiles of the frames
-// whose level l is not their coarsest (level l's list).
-static cudaError_t fm_cycle(const Frame2* fr, const int* tf, int nact, const Batch2& b, const FramesMg& M,
+// k_fm_final0 and the scalar update.  Level 0: nblocks block tiles of list
+// (NULL: all); nrestrict_lv[l]: tiles of the frames whose level l is not their
+// coarsest (level l's list).
+static cudaError_t fm_cycle(const Frame2* fr, int nblocks, const int* list, const Batch2& b, const FramesMg& M,
                             const int* nrestrict_lv, int nframes, int mode, cudaStream_t st) {
   const dim3 blk(32, 8);
-  k_fm_restrict0<<<nact, blk, 0, st>>>(fr, tf, b, M, mode); note_launch();
+  k_fm_restrict0<<<nblocks, blk, 0, st>>>(fr, b, M, list, mode); note_launch();
   for (int l = 1; l + 1 < M.nlev; l++) {
     if (nrestrict_lv[l] == 0) break;
-    k_fm_restrict<<<nrestrict_lv[l], blk, 0, st>>>(fr, tf, b, M, l, mode); note_launch();
+    k_fm_restrict<<<nrestrict_lv[l], blk, 0, st>>>(fr, nullptr, b, M, l, mode); note_launch();
   }
   k_fm_coarse<<<nframes, kFmMaxCoarse, 0, st>>>(b, M, M.coarse_sweeps, mode); note_launch();
   for (int l = M.nlev - 2; l >= 1; l--) {
     if (nrestrict_lv[l] == 0) continue;
     k_fm_prolong<<<nrestrict_lv[l], blk, 0, st>>>(b, M, l, mode); note_launch();
   }
-  k_fm_final0<<<nact, blk, 0, st>>>(fr, tf, b, M, mode); note_launch();
-  k_fm_fin_final<<<nframes, dim3(32, kR), 0, st>>>(fr, b, mode); note_launch();
+  k_fm_final0<<<nblocks, blk, 0, st>>>(fr, b, M, list, mode); note_launch();
+  k_fm_fin_final<<<nframes, dim3(32, kR), 0, st>>>(M, b, mode); note_launch();
   return cudaGetLastError();
 }
 
-cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
+cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, int nbtiles, const Batch2& b, const FramesMg& M,
                      const int* nrestrict_lv, int nframes, cudaStream_t st) {
-  const dim3 blk(32, 8);
   Batch2 b0 = b;
-  b0.tiles = nullptr;  // all level-0 tiles
-  k_fm_load<<<ntiles, blk, 0, st>>>(fr, tf, b0, M); note_launch();
-  return fm_cycle(fr, tf, ntiles, b0, M, nrestrict_lv, nframes, 1, st);
+  b0.tiles = nullptr;  // all 32 x 8 tiles
+  k_fm_load<<<ntiles, dim3(32, 8), 0, st>>>(fr, tf, b0, M); note_launch();
+  return fm_cycle(fr, nbtiles, nullptr, b0, M, nrestrict_lv, nframes, 1, st);
 }
 
-cudaError_t fm_iteration(const Frame2* fr, const int* tf, int nact, const Batch2& b, const FramesMg& M,
-                         const int* nrestrict_lv, int nframes, cudaStream_t st) {
-  const dim3 blk(32, 8);
-  k_fm_spmv<<<nact, blk, 0, st>>>(fr, tf, b, M); note_launch();
-  k_fm_fin_spmv<<<nframes, dim3(32, kR), 0, st>>>(fr, b); note_launch();
-  return fm_cycle(fr, tf, nact, b, M, nrestrict_lv, nframes, 0, st);
+cudaError_t fm_iteration(const Frame2* fr, int nbact, const Batch2& b, const FramesMg& M, const int* nrestrict_lv,
+                         int nframes, cudaStream_t st) {
+  k_fm_spmv<<<nbact, dim3(32, 8), 0, st>>>(fr, b, M); note_launch();
+  k_fm_fin_spmv<<<nframes, dim3(32, kR), 0, st>>>(M, b); note_launch();
+  return fm_cycle(fr, nbact, M.bt_list, b, M, nrestrict_lv, nframes, 0, st);
 }
 
 cudaError_t fm_apply(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,

@@ -260,16 +260,22 @@ struct FramesMg {
   float *b[kFmMaxLevels][2], *xa[kFmMaxLevels][2], *xb[kFmMaxLevels][2];  // levels >= 1, per direction
   float *r[2], *z[2], *p[2], *q[2], *e[2];  // level 0 (2-D frame layout), per direction
   float *r2[2], *p2[2];  // second r and p buffers (the current one: iterations & 1)
+  // level-0 blocks of the stencil passes: 32 x 32 cells of one frame
+  const int* bt_frame;   // frame of each block tile
+  const int4* bt_info;   // per frame: first block tile, block tiles, block tiles along x
+  int* bt_list;          // the block tiles of the frames still iterating (compacted by the host)
   float omega;
   float cscale;  // scale of the prolonged coarse correction (the cycle stays symmetric)
   int coarse_sweeps;
 };
 cudaError_t fm_setup(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
                      const int* ntiles_lv, cudaStream_t st);
-cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
+// fm_start: every block tile and the 32 x 8 load tiles (ntiles, nbtiles);
+// fm_iteration: the nbact block tiles of M.bt_list.
+cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, int nbtiles, const Batch2& b, const FramesMg& M,
                      const int* nrestrict_lv, int nframes, cudaStream_t st);
-cudaError_t fm_iteration(const Frame2* fr, const int* tf, int nact, const Batch2& b, const FramesMg& M,
-                         const int* nrestrict_lv, int nframes, cudaStream_t st);
+cudaError_t fm_iteration(const Frame2* fr, int nbact, const Batch2& b, const FramesMg& M, const int* nrestrict_lv,
+                         int nframes, cudaStream_t st);
 cudaError_t fm_apply(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,
                      cudaStream_t st);
 
