@@ -394,10 +394,11 @@ def densities(args, lib, f, out, head, dsolid, dax, faces_dev, bgs, stream):
 
 def run_learned(args):
     """The committed trained network on unseen random bodies at 256x256x128
-    (the training set was 128x128x64): FP64 PCG to 1e-10 from phi = 0, from
-    the learned initial guess, and the flexible CG with the network as
-    preconditioner (plus the guess); iterations, time and fallbacks over
-    `steps` bodies (after `warmup` bodies)."""
+    (the training set was 128x128x64): FP64 PCG to 1e-10 from phi = 0 and from
+    the learned initial guess, the multigrid-preconditioned refinement from
+    phi = 0 and from the guess, and (with --arms naming fcg_learned) the
+    flexible CG with the network as preconditioner; iterations, time and
+    fallbacks over `steps` bodies (after `warmup` bodies)."""
     import torch
     from flowfpmpp_gb300 import build as fbuild
     fbuild.build()
@@ -427,8 +428,16 @@ def run_learned(args):
             _, sw2, r2, _ = p.solve("fcg_learned", tol=1e-10, net=net)
         torch.cuda.synchronize()
         t4 = time.perf_counter()
+        # the multigrid-preconditioned refinement from phi = 0 and from the guess
+        _, sw3, r3, _ = p.solve("pcg_mg", tol=1e-10)
+        torch.cuda.synchronize()
+        t5 = time.perf_counter()
+        _, sw4, r4, fb4 = p.solve("pcg_mg", tol=1e-10, net=net)
+        torch.cuda.synchronize()
+        t6 = time.perf_counter()
         if s_ >= args.warmup:
-            rows.append((sw0, t2 - t1, r0, sw1, t3 - t2, r1, fb, sw2, t4 - t3, r2))
+            rows.append((sw0, t2 - t1, r0, sw1, t3 - t2, r1, fb, sw2, t4 - t3, r2, sw3, t5 - t4, r3, sw4, t6 - t5, r4,
+                         fb4))
     a = np.array(rows, dtype=np.float64)
     line = {"metric": "FP64 PCG solve time to 1e-10 with the learned initial guess vs from phi = 0",
             "value": float(a[:, 4].mean()), "unit": "s per body", "higher_is_better": False, "n_gpus": 1,
@@ -439,7 +448,14 @@ def run_learned(args):
             "learned": {"seconds": float(a[:, 4].mean()), "iterations": float(a[:, 3].mean()),
                         "fallbacks": int(a[:, 6].sum()), "max_residual": float(a[:, 5].max())},
             "iteration_ratio": float(a[:, 0].sum() / a[:, 3].sum()),
-            "time_ratio": float(a[:, 1].sum() / a[:, 4].sum())}
+            "time_ratio": float(a[:, 1].sum() / a[:, 4].sum()),
+            "mg": {"seconds": float(a[:, 11].mean()), "iterations": float(a[:, 10].mean()),
+                   "max_residual": float(a[:, 12].max())},
+            "learned_mg": {"seconds": float(a[:, 14].mean()), "iterations": float(a[:, 13].mean()),
+                           "fallbacks": int(a[:, 16].sum()), "max_residual": float(a[:, 15].max()),
+                           "iteration_ratio_vs_mg": float(a[:, 10].sum() / a[:, 13].sum()),
+                           "time_ratio_vs_mg": float(a[:, 11].sum() / a[:, 14].sum())},
+            "mg_vs_plain_time_ratio": float(a[:, 1].sum() / a[:, 11].sum())}
     if fcg:
         line["fcg_learned"] = {"seconds": float(a[:, 8].mean()), "iterations": float(a[:, 7].mean()),
                                "max_residual": float(a[:, 9].max()),
