@@ -72,6 +72,8 @@ def parse():
                     help="pcg_sphere / pcg_ellipsoids: skip the force densities on the solved potentials")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="pcg_ellipsoids / densities: a smaller grid of the same generator (profiling runs)")
+    ap.add_argument("--frames", type=int, default=256,
+                    help="foil_frames: the first N frames of the 256-frame generator (profiling runs)")
     ap.add_argument("--arms", default="fp64,mixed,mg,learned_mixed,learned_mg",
                     help="pcg_sphere / pcg_ellipsoids: comma-separated solver arms to time (profiling runs take "
                          "one); learned_guess: add fcg_learned for the flexible CG with the network")
@@ -473,7 +475,7 @@ def run_frames(args):
     fbuild.build()
     from flowfpmpp_gb300 import partition as pt
     from flowfpmpp_gb300 import workloads
-    frames = workloads.foil_frames()
+    frames = workloads.foil_frames(nframes=args.frames)
     cells = sum(f["nx"] * f["ny"] for f in frames)
     for _ in range(args.warmup):
         pt.partition_frames_2d(frames, tolerance=1e-10)
@@ -492,7 +494,7 @@ def run_frames(args):
     line = {"metric": "batched 2-D frames: phi_x, phi_y to 1e-10 and the four FPM terms",
             "value": len(frames) / el, "unit": "frames/s", "higher_is_better": True, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "seconds_per_batch": el, "data": "synthetic (seeded)",
-            "config": {"workload": "256 foil frames 96^2..512^2, ratio 1.02", "frames": len(frames),
+            "config": {"workload": f"{len(frames)} foil frames 96^2..512^2, ratio 1.02", "frames": len(frames),
                        "cells_2d": int(cells), "tolerance": 1e-10},
             "cell_potentials_per_s": 2 * cells / el, "max_residual": float(np.max(res)),
             "fp32_iterations": {"max": int(sweeps.max()), "mean": float(sweeps.mean())},
