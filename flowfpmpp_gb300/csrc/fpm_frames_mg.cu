@@ -468,6 +468,12 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
   if (!act[0] && !act[1]) return;
   const float* __restrict__ dv = M.dinv[0];
   const int x = threadIdx.x + 1;
+  float4 fc[kBRows];  // faces of the own rows, loaded with the operands
+#pragma unroll
+  for (int k = 0; k < kBRows; k++) {
+    const long long c = own_cell(h, k);
+    fc[k] = c >= 0 ? faces_of(h, M, c, k) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   float rown[kR][kBRows];
   for (int r = 0; r < kR; r++) {
     if (!act[r]) continue;
@@ -502,8 +508,7 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
   for (int k = 0; k < kBRows; k++) {
     const long long c = own_cell(h, k);
     const int y = threadIdx.y + 1 + 8 * k;
-    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (c >= 0) t = faces_of(h, M, c, k);
+    const float4 t = fc[k];
     for (int r = 0; r < kR; r++) {
       float res = 0.f;
       if (c >= 0 && act[r]) res = rown[r][k] - apply_s(ts_s[r], x, y, t);
@@ -540,6 +545,12 @@ __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr
   const float* __restrict__ dv = M.dinv[0];
   const float cs = M.cscale;
   const int x = threadIdx.x + 1;
+  float4 fc[kBRows];  // faces of the own rows, loaded with the operands
+#pragma unroll
+  for (int k = 0; k < kBRows; k++) {
+    const long long c = own_cell(h, k);
+    fc[k] = c >= 0 ? faces_of(h, M, c, k) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   float rown[kR][kBRows], dvc[kBRows];
 #pragma unroll
   for (int k = 0; k < kBRows; k++) {
@@ -574,7 +585,7 @@ __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr
   for (int k = 0; k < kBRows; k++) {
     const long long c = own_cell(h, k);
     if (c < 0) continue;
-    const float4 t = faces_of(h, M, c, k);
+    const float4 t = fc[k];
     const int y = threadIdx.y + 1 + 8 * k;
     for (int r = 0; r < kR; r++) {
       if (!act[r]) continue;
