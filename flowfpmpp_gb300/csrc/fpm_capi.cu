@@ -2532,11 +2532,14 @@ int fpm_partition_frames_2d(int nframes, const int* nx, const int* ny, const dou
         M.r2[r] = A.get<float>(n2);
         M.p2[r] = A.get<float>(n2);
       }
-      // level-0 block tiles (32 x 32 cells) of the stencil passes
+      // level-0 block tiles (32 x 8 rows cells, rows 2, 4 or 8 per thread) of the stencil passes
+      const int brows = (int)env_double("FPM_FRAMES_ROWS", 4);
+      M.bt_rows = brows == 2 || brows == 8 ? brows : 4;
+      const int bh = 8 * M.bt_rows;
       std::vector<int> bt_frame;
       std::vector<int4> bt_info(nframes);
       for (int f = 0; f < nframes; f++) {
-        const int bx = (fr[f].nx + 31) / 32, nbt = bx * ((fr[f].ny + 31) / 32);
+        const int bx = (fr[f].nx + 31) / 32, nbt = bx * ((fr[f].ny + bh - 1) / bh);
         bt_info[f] = make_int4((int)bt_frame.size(), nbt, bx, 0);
         for (int t = 0; t < nbt; t++) bt_frame.push_back(f);
       }

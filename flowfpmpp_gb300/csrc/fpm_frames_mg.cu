@@ -60,22 +60,30 @@ struct Sum2 {
   __device__ __forceinline__ double value() const { return (double)s + (double)e; }
 };
 
-// Level-0 stencil passes work on block tiles of 32 x 32 cells (a thread owns
-// column x and rows y, y + 8, y + 16, y + 24) with the operand and its
-// one-cell halo in shared memory: cell (i0 - 1 + x, j0 - 1 + y) of the frame
-// at [y][x]; threads 0 .. kBHalo - 1 fill the halo.
-constexpr int kBT = 32, kBH = kBT + 2, kBRows = kBT / 8, kBHalo = 4 * kBT + 4;
+// Level-0 stencil passes work on block tiles (a thread owns column x and
+// rows y, y + 8, ...) with the operand and its one-cell halo in shared memory:
+// cell (i0 - 1 + x, j0 - 1 + y) of the frame at [y][x]; the first HALO threads
+// fill the halo.
+// A block tile is 32 cells wide and 8 ROWS high (ROWS = 2, 4 or 8 rows per
+// thread; FPM_FRAMES_ROWS, default 4).
+constexpr int kBW = 32, kBWH = kBW + 2;
+template <int ROWS>
+struct BT {
+  static constexpr int H = 8 * ROWS, HH = H + 2, HALO = 2 * kBWH + 2 * H;
+  static_assert(HALO <= 256, "one halo slot per thread");
+};
+template <int ROWS>
 __device__ __forceinline__ void bhalo_pos(int tid, int& x, int& y) {
-  if (tid < kBH) {
+  if (tid < kBWH) {
     x = tid;
     y = 0;
-  } else if (tid < 2 * kBH) {
-    x = tid - kBH;
-    y = kBH - 1;
+  } else if (tid < 2 * kBWH) {
+    x = tid - kBWH;
+    y = BT<ROWS>::HH - 1;
   } else {
-    const int k = tid - 2 * kBH;
+    const int k = tid - 2 * kBWH;
     y = 1 + (k >> 1);
-    x = (k & 1) ? kBH - 1 : 0;
+    x = (k & 1) ? kBWH - 1 : 0;
   }
 }
 
@@ -339,6 +347,7 @@ struct B0 {
   long long o2;
   bool halo;
 };
+template <int ROWS>
 __device__ __forceinline__ B0 b0_ref(const Frame2* __restrict__ fr, const FramesMg& M, const int* __restrict__ list) {
   B0 h;
   h.tile = list ? list[blockIdx.x] : (int)blockIdx.x;
@@ -349,12 +358,12 @@ __device__ __forceinline__ B0 b0_ref(const Frame2* __restrict__ fr, const Frames
   h.ny = F.ny;
   h.o2 = F.o2;
   const int idx = h.tile - bi.x;
-  h.i0 = (idx % bi.z) * kBT;
-  h.j0 = (idx / bi.z) * kBT;
+  h.i0 = (idx % bi.z) * kBW;
+  h.j0 = (idx / bi.z) * BT<ROWS>::H;
   const int tid = lin_tid();
-  h.halo = tid < kBHalo;
+  h.halo = tid < BT<ROWS>::HALO;
   h.hx = h.hy = 0;
-  if (h.halo) bhalo_pos(tid, h.hx, h.hy);
+  if (h.halo) bhalo_pos<ROWS>(tid, h.hx, h.hy);
   return h;
 }
 // Frame cell of row k of this thread (-1 outside the frame), and of its halo slot.
@@ -372,16 +381,19 @@ __device__ __forceinline__ float4 faces_of(const B0& h, const FramesMg& M, long 
   return make_float4(i > 0 ? M.te[0][c - 1] : 0.f, M.te[0][c], j > 0 ? M.tn[0][c - h.nx] : 0.f, M.tn[0][c]);
 }
 // A x at smem cell (x, y) of a haloed tile.
-__device__ __forceinline__ float apply_s(const float (&v)[kBH][kBH], int x, int y, float4 t) {
+template <int HH>
+__device__ __forceinline__ float apply_s(const float (&v)[HH][kBWH], int x, int y, float4 t) {
   return apply4(v[y][x], v[y][x - 1], v[y][x + 1], v[y - 1][x], v[y + 1][x], t.x, t.y, t.z, t.w);
 }
 
 // q = A p with p = z + beta p_old formed on the fly (the direction update;
 // beta = 0 and p_old = 0 after a start); writes p and q, e += alpha_prev
 // p_old; p.q per block tile.  The active pairs only.
+template <int ROWS>
 __global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, Batch2 b, FramesMg M) {
-  __shared__ float ps[kR][kBH][kBH];
-  const B0 h = b0_ref(fr, M, M.bt_list);
+  using T = BT<ROWS>;
+  __shared__ float ps[kR][T::HH][kBWH];
+  const B0 h = b0_ref<ROWS>(fr, M, M.bt_list);
   const int f = h.f;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = b.active[f * kR + r] != 0;
@@ -396,10 +408,10 @@ __global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, 
     const float* __restrict__ z = M.z[r];
     float* __restrict__ e = M.e[r];
     // all loads of the pass first (own rows and the halo slot), then the stores
-    long long cc[kBRows];
-    float po[kBRows], zz[kBRows], ee[kBRows];
+    long long cc[ROWS];
+    float po[ROWS], zz[ROWS], ee[ROWS];
 #pragma unroll
-    for (int k = 0; k < kBRows; k++) {
+    for (int k = 0; k < ROWS; k++) {
       cc[k] = own_cell(h, k);
       po[k] = cc[k] >= 0 ? pold[cc[k]] : 0.f;
       zz[k] = cc[k] >= 0 ? z[cc[k]] : 0.f;
@@ -408,7 +420,7 @@ __global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, 
     const long long ch = h.halo ? halo_cell(h) : -1;
     const float hp = ch >= 0 ? pold[ch] : 0.f, hz = ch >= 0 ? z[ch] : 0.f;
 #pragma unroll
-    for (int k = 0; k < kBRows; k++) {
+    for (int k = 0; k < ROWS; k++) {
       const float pn = fmaf(beta, po[k], zz[k]);
       if (cc[k] >= 0) {
         pnew[cc[k]] = pn;
@@ -421,7 +433,7 @@ __global__ void __launch_bounds__(256) k_fm_spmv(const Frame2* __restrict__ fr, 
   __syncthreads();
   Sum2 acc[kR];
 #pragma unroll
-  for (int k = 0; k < kBRows; k++) {
+  for (int k = 0; k < ROWS; k++) {
     const long long c = own_cell(h, k);
     if (c < 0) continue;
     const float4 t = faces_of(h, M, c, k);
@@ -457,24 +469,26 @@ __global__ void k_fm_fin_spmv(FramesMg M, Batch2 b) {
 // Level-0 restriction: r = r_old - alpha q (iteration mode; written to the
 // other r buffer), t = dinv r (the first smoothing sweep from zero),
 // b_1 = sum over each 2 x 2 aggregate of r - A t.
+template <int ROWS>
 __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__ fr, Batch2 b, FramesMg M,
                                                       const int* __restrict__ list, int mode) {
-  __shared__ float ts_s[kR][kBH][kBH];
-  __shared__ float res_s[kR][kBT][kBT + 1];
-  const B0 h = b0_ref(fr, M, list);
+  using T = BT<ROWS>;
+  __shared__ float ts_s[kR][T::HH][kBWH];
+  __shared__ float res_s[kR][T::H][kBW + 1];
+  const B0 h = b0_ref<ROWS>(fr, M, list);
   const int f = h.f;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
   if (!act[0] && !act[1]) return;
   const float* __restrict__ dv = M.dinv[0];
   const int x = threadIdx.x + 1;
-  float4 fc[kBRows];  // faces of the own rows, loaded with the operands
+  float4 fc[ROWS];  // faces of the own rows, loaded with the operands
 #pragma unroll
-  for (int k = 0; k < kBRows; k++) {
+  for (int k = 0; k < ROWS; k++) {
     const long long c = own_cell(h, k);
     fc[k] = c >= 0 ? faces_of(h, M, c, k) : make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  float rown[kR][kBRows];
+  float rown[kR][ROWS];
   for (int r = 0; r < kR; r++) {
     if (!act[r]) continue;
     const int par = fm_par(b, f, r);
@@ -483,10 +497,10 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
     float* __restrict__ rnew = par ? M.r[r] : M.r2[r];
     const float* __restrict__ qv = M.q[r];
     // all loads of the pass first (own rows and the halo slot), then the stores
-    long long cc[kBRows];
-    float ro[kBRows], qq[kBRows], dd[kBRows];
+    long long cc[ROWS];
+    float ro[ROWS], qq[ROWS], dd[ROWS];
 #pragma unroll
-    for (int k = 0; k < kBRows; k++) {
+    for (int k = 0; k < ROWS; k++) {
       cc[k] = own_cell(h, k);
       ro[k] = cc[k] >= 0 ? rold[cc[k]] : 0.f;
       qq[k] = cc[k] >= 0 && !mode ? qv[cc[k]] : 0.f;
@@ -495,7 +509,7 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
     const long long ch = h.halo ? halo_cell(h) : -1;
     const float hr = ch >= 0 ? rold[ch] : 0.f, hq = ch >= 0 && !mode ? qv[ch] : 0.f, hd = ch >= 0 ? dv[ch] : 0.f;
 #pragma unroll
-    for (int k = 0; k < kBRows; k++) {
+    for (int k = 0; k < ROWS; k++) {
       const float rn = mode ? ro[k] : fmaf(-alpha, qq[k], ro[k]);
       if (cc[k] >= 0 && !mode) rnew[cc[k]] = rn;
       rown[r][k] = cc[k] >= 0 ? rn : 0.f;
@@ -505,7 +519,7 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < kBRows; k++) {
+  for (int k = 0; k < ROWS; k++) {
     const long long c = own_cell(h, k);
     const int y = threadIdx.y + 1 + 8 * k;
     const float4 t = fc[k];
@@ -516,16 +530,18 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
     }
   }
   __syncthreads();
-  // one 2 x 2 aggregate per thread
-  const int tid = lin_tid(), ax = tid & 15, ay = tid >> 4;
-  const int i = h.i0 + 2 * ax, j = h.j0 + 2 * ay;
-  if (i >= h.nx || j >= h.ny) return;
+  // the 2 x 2 aggregates of the tile, one per thread at a time
   const FmLevel C = M.lv[(size_t)f * kFmMaxLevels + 1];
-  for (int r = 0; r < kR; r++) {
-    if (!act[r]) continue;
-    const float sm = (res_s[r][2 * ay][2 * ax] + res_s[r][2 * ay][2 * ax + 1]) +
-                     (res_s[r][2 * ay + 1][2 * ax] + res_s[r][2 * ay + 1][2 * ax + 1]);
-    M.b[1][r][C.off + (i >> 1) + (long long)C.nx * (j >> 1)] = sm;
+  for (int ag = lin_tid(); ag < 16 * (T::H / 2); ag += 256) {
+    const int ax = ag & 15, ay = ag >> 4;
+    const int i = h.i0 + 2 * ax, j = h.j0 + 2 * ay;
+    if (i >= h.nx || j >= h.ny) continue;
+    for (int r = 0; r < kR; r++) {
+      if (!act[r]) continue;
+      const float sm = (res_s[r][2 * ay][2 * ax] + res_s[r][2 * ay][2 * ax + 1]) +
+                       (res_s[r][2 * ay + 1][2 * ax] + res_s[r][2 * ay + 1][2 * ax + 1]);
+      M.b[1][r][C.off + (i >> 1) + (long long)C.nx * (j >> 1)] = sm;
+    }
   }
 }
 
@@ -533,10 +549,12 @@ __global__ void __launch_bounds__(256) k_fm_restrict0(const Frame2* __restrict__
 // The pairs selected by mode (start: those in the set, reading the r that the
 // load pass wrote; iteration: the active ones, reading the r of the
 // restriction).
+template <int ROWS>
 __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr, Batch2 b, FramesMg M,
                                                    const int* __restrict__ list, int mode) {
-  __shared__ float ys[kR][kBH][kBH];
-  const B0 h = b0_ref(fr, M, list);
+  using T = BT<ROWS>;
+  __shared__ float ys[kR][T::HH][kBWH];
+  const B0 h = b0_ref<ROWS>(fr, M, list);
   const int f = h.f;
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
@@ -545,15 +563,15 @@ __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr
   const float* __restrict__ dv = M.dinv[0];
   const float cs = M.cscale;
   const int x = threadIdx.x + 1;
-  float4 fc[kBRows];  // faces of the own rows, loaded with the operands
+  float4 fc[ROWS];  // faces of the own rows, loaded with the operands
 #pragma unroll
-  for (int k = 0; k < kBRows; k++) {
+  for (int k = 0; k < ROWS; k++) {
     const long long c = own_cell(h, k);
     fc[k] = c >= 0 ? faces_of(h, M, c, k) : make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  float rown[kR][kBRows], dvc[kBRows];
+  float rown[kR][ROWS], dvc[ROWS];
 #pragma unroll
-  for (int k = 0; k < kBRows; k++) {
+  for (int k = 0; k < ROWS; k++) {
     const long long c = own_cell(h, k);
     dvc[k] = c >= 0 ? dv[c] : 0.f;
   }
@@ -564,9 +582,9 @@ __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr
     const float* __restrict__ xc1 = M.xb[1][r] + C.off;
     auto parent = [&](int i, int j) { return cs * xc1[(i >> 1) + (long long)C.nx * (j >> 1)]; };
     // all loads of the pass first (own rows and the halo slot), then the stores
-    float pa[kBRows];
+    float pa[ROWS];
 #pragma unroll
-    for (int k = 0; k < kBRows; k++) {
+    for (int k = 0; k < ROWS; k++) {
       const long long c = own_cell(h, k);
       rown[r][k] = c >= 0 ? rr[c] : 0.f;
       pa[k] = c >= 0 ? parent(h.i0 + (int)threadIdx.x, h.j0 + (int)threadIdx.y + 8 * k) : 0.f;
@@ -575,14 +593,14 @@ __global__ void __launch_bounds__(256) k_fm_final0(const Frame2* __restrict__ fr
     const float hr = ch >= 0 ? rr[ch] : 0.f, hd = ch >= 0 ? dv[ch] : 0.f;
     const float hpa = ch >= 0 ? parent(h.i0 - 1 + h.hx, h.j0 - 1 + h.hy) : 0.f;
 #pragma unroll
-    for (int k = 0; k < kBRows; k++)
+    for (int k = 0; k < ROWS; k++)
       ys[r][threadIdx.y + 1 + 8 * k][x] = own_cell(h, k) >= 0 ? fmaf(dvc[k], rown[r][k], pa[k]) : 0.f;
     if (h.halo) ys[r][h.hy][h.hx] = ch >= 0 ? fmaf(hd, hr, hpa) : 0.f;
   }
   __syncthreads();
   Sum2 acc[kR];
 #pragma unroll
-  for (int k = 0; k < kBRows; k++) {
+  for (int k = 0; k < ROWS; k++) {
     const long long c = own_cell(h, k);
     if (c < 0) continue;
     const float4 t = fc[k];
@@ -694,10 +712,11 @@ cudaError_t fm_setup(const Frame2* fr, const int* tf, int ntiles, const Batch2& 
 // k_fm_final0 and the scalar update.  Level 0: nblocks block tiles of list
 // (NULL: all); nrestrict_lv[l]: tiles of the frames whose level l is not their
 // coarsest (level l's list).
+template <int ROWS>
 static cudaError_t fm_cycle(const Frame2* fr, int nblocks, const int* list, const Batch2& b, const FramesMg& M,
                             const int* nrestrict_lv, int nframes, int mode, cudaStream_t st) {
   const dim3 blk(32, 8);
-  k_fm_restrict0<<<nblocks, blk, 0, st>>>(fr, b, M, list, mode); note_launch();
+  k_fm_restrict0<ROWS><<<nblocks, blk, 0, st>>>(fr, b, M, list, mode); note_launch();
   for (int l = 1; l + 1 < M.nlev; l++) {
     if (nrestrict_lv[l] == 0) break;
     k_fm_restrict<<<nrestrict_lv[l], blk, 0, st>>>(fr, nullptr, b, M, l, mode); note_launch();
@@ -707,7 +726,7 @@ static cudaError_t fm_cycle(const Frame2* fr, int nblocks, const int* list, cons
     if (nrestrict_lv[l] == 0) continue;
     k_fm_prolong<<<nrestrict_lv[l], blk, 0, st>>>(b, M, l, mode); note_launch();
   }
-  k_fm_final0<<<nblocks, blk, 0, st>>>(fr, b, M, list, mode); note_launch();
+  k_fm_final0<ROWS><<<nblocks, blk, 0, st>>>(fr, b, M, list, mode); note_launch();
   k_fm_fin_final<<<nframes, dim3(32, kR), 0, st>>>(M, b, mode); note_launch();
   return cudaGetLastError();
 }
@@ -717,14 +736,27 @@ cudaError_t fm_start(const Frame2* fr, const int* tf, int ntiles, int nbtiles, c
   Batch2 b0 = b;
   b0.tiles = nullptr;  // all 32 x 8 tiles
   k_fm_load<<<ntiles, dim3(32, 8), 0, st>>>(fr, tf, b0, M); note_launch();
-  return fm_cycle(fr, nbtiles, nullptr, b0, M, nrestrict_lv, nframes, 1, st);
+  switch (M.bt_rows) {
+    case 2: return fm_cycle<2>(fr, nbtiles, nullptr, b0, M, nrestrict_lv, nframes, 1, st);
+    case 8: return fm_cycle<8>(fr, nbtiles, nullptr, b0, M, nrestrict_lv, nframes, 1, st);
+    default: return fm_cycle<4>(fr, nbtiles, nullptr, b0, M, nrestrict_lv, nframes, 1, st);
+  }
 }
 
 cudaError_t fm_iteration(const Frame2* fr, int nbact, const Batch2& b, const FramesMg& M, const int* nrestrict_lv,
                          int nframes, cudaStream_t st) {
-  k_fm_spmv<<<nbact, dim3(32, 8), 0, st>>>(fr, b, M); note_launch();
+  switch (M.bt_rows) {
+    case 2: k_fm_spmv<2><<<nbact, dim3(32, 8), 0, st>>>(fr, b, M); break;
+    case 8: k_fm_spmv<8><<<nbact, dim3(32, 8), 0, st>>>(fr, b, M); break;
+    default: k_fm_spmv<4><<<nbact, dim3(32, 8), 0, st>>>(fr, b, M); break;
+  }
+  note_launch();
   k_fm_fin_spmv<<<nframes, dim3(32, kR), 0, st>>>(M, b); note_launch();
-  return fm_cycle(fr, nbact, M.bt_list, b, M, nrestrict_lv, nframes, 0, st);
+  switch (M.bt_rows) {
+    case 2: return fm_cycle<2>(fr, nbact, M.bt_list, b, M, nrestrict_lv, nframes, 0, st);
+    case 8: return fm_cycle<8>(fr, nbact, M.bt_list, b, M, nrestrict_lv, nframes, 0, st);
+    default: return fm_cycle<4>(fr, nbact, M.bt_list, b, M, nrestrict_lv, nframes, 0, st);
+  }
 }
 
 cudaError_t fm_apply(const Frame2* fr, const int* tf, int ntiles, const Batch2& b, const FramesMg& M,

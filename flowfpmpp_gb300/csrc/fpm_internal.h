@@ -260,10 +260,11 @@ struct FramesMg {
   float *b[kFmMaxLevels][2], *xa[kFmMaxLevels][2], *xb[kFmMaxLevels][2];  // levels >= 1, per direction
   float *r[2], *z[2], *p[2], *q[2], *e[2];  // level 0 (2-D frame layout), per direction
   float *r2[2], *p2[2];  // second r and p buffers (the current one: iterations & 1)
-  // level-0 blocks of the stencil passes: 32 x 32 cells of one frame
+  // level-0 blocks of the stencil passes: 32 x (8 bt_rows) cells of one frame
   const int* bt_frame;   // frame of each block tile
   const int4* bt_info;   // per frame: first block tile, block tiles, block tiles along x
   int* bt_list;          // the block tiles of the frames still iterating (compacted by the host)
+  int bt_rows;           // rows per thread of a block tile: 2, 4 or 8 (32 x 8 bt_rows cells)
   float omega;
   float cscale;  // scale of the prolonged coarse correction (the cycle stays symmetric)
   int coarse_sweeps;
