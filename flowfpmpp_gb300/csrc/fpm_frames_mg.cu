@@ -235,21 +235,43 @@ __global__ void __launch_bounds__(256) k_fm_restrict(const Frame2* __restrict__ 
   bool act[kR];
   for (int r = 0; r < kR; r++) act[r] = on(b, f, r, mode);
   if (!act[0] && !act[1]) return;
-  const float* te = M.te[l] + L.off;
-  const float* tn = M.tn[l] + L.off;
-  const float* dv = M.dinv[l] + L.off;
+  const float* __restrict__ te = M.te[l] + L.off;
+  const float* __restrict__ tn = M.tn[l] + L.off;
+  const float* __restrict__ dv = M.dinv[l] + L.off;
   const long long c = i + (long long)L.nx * j;
+  // every load of both directions first (the cell, its four neighbours, the faces)
+  const bool w = i > 0, e = i + 1 < L.nx, so = j > 0, no = j + 1 < L.ny;
+  float fw = 0.f, fe = 0.f, fs = 0.f, fn = 0.f, d[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, v[kR][5];
+  if (live) {
+    fw = w ? te[c - 1] : 0.f;
+    fe = te[c];
+    fs = so ? tn[c - L.nx] : 0.f;
+    fn = tn[c];
+    d[0] = dv[c];
+    d[1] = w ? dv[c - 1] : 0.f;
+    d[2] = e ? dv[c + 1] : 0.f;
+    d[3] = so ? dv[c - L.nx] : 0.f;
+    d[4] = no ? dv[c + L.nx] : 0.f;
+  }
+  for (int r = 0; r < kR; r++) {
+    const float* __restrict__ bb = M.b[l][r] + L.off;
+    const bool ld = live && act[r];
+    v[r][0] = ld ? bb[c] : 0.f;
+    v[r][1] = ld && w ? bb[c - 1] : 0.f;
+    v[r][2] = ld && e ? bb[c + 1] : 0.f;
+    v[r][3] = ld && so ? bb[c - L.nx] : 0.f;
+    v[r][4] = ld && no ? bb[c + L.nx] : 0.f;
+  }
   for (int r = 0; r < kR; r++) {
     float res = 0.f;
     if (live && act[r]) {
-      const float* bb = M.b[l][r] + L.off;
-      const float tc = dv[c] * bb[c];
-      const float tw = i > 0 ? dv[c - 1] * bb[c - 1] : 0.f;
-      const float tE = i + 1 < L.nx ? dv[c + 1] * bb[c + 1] : 0.f;
-      const float ts = j > 0 ? dv[c - L.nx] * bb[c - L.nx] : 0.f;
-      const float tN = j + 1 < L.ny ? dv[c + L.nx] * bb[c + L.nx] : 0.f;
-      const float a = apply4(tc, tw, tE, ts, tN, i > 0 ? te[c - 1] : 0.f, te[c], j > 0 ? tn[c - L.nx] : 0.f, tn[c]);
-      res = bb[c] - a;
+      const float tc = d[0] * v[r][0];
+      const float tw = w ? d[1] * v[r][1] : 0.f;
+      const float tE = e ? d[2] * v[r][2] : 0.f;
+      const float ts = so ? d[3] * v[r][3] : 0.f;
+      const float tN = no ? d[4] * v[r][4] : 0.f;
+      const float a = apply4(tc, tw, tE, ts, tN, fw, fe, fs, fn);
+      res = v[r][0] - a;
       M.xa[l][r][L.off + c] = tc;
     }
     res_s[r][threadIdx.y][threadIdx.x] = res;
@@ -318,22 +340,32 @@ __global__ void __launch_bounds__(256) k_fm_prolong(Batch2 b, FramesMg M, int l,
   const FmLevel C = M.lv[(size_t)t.f * kFmMaxLevels + l + 1];
   const int i = t.i, j = t.j;
   const long long c = i + (long long)L.nx * j;
-  const float* te = M.te[l] + L.off;
-  const float* tn = M.tn[l] + L.off;
-  const float* dv = M.dinv[l] + L.off;
+  const float* __restrict__ te = M.te[l] + L.off;
+  const float* __restrict__ tn = M.tn[l] + L.off;
+  const float* __restrict__ dv = M.dinv[l] + L.off;
+  const bool w = i > 0, e = i + 1 < L.nx, so = j > 0, no = j + 1 < L.ny;
+  // every load of both directions first
+  const float fw = w ? te[c - 1] : 0.f, fe = te[c], fs = so ? tn[c - L.nx] : 0.f, fn = tn[c], dc = dv[c];
+  const float cs = M.cscale;
+  float yv[kR][5], bc[kR];
   for (int r = 0; r < kR; r++) {
-    if (!act[r]) continue;
-    const float* xa = M.xa[l][r] + L.off;
-    const float* xc1 = M.xb[l + 1][r] + C.off;
-    const float cs = M.cscale;
+    const float* __restrict__ xa = M.xa[l][r] + L.off;
+    const float* __restrict__ xc1 = M.xb[l + 1][r] + C.off;
     auto y = [&](int ii, int jj) {
       return fmaf(cs, xc1[(ii >> 1) + (long long)C.nx * (jj >> 1)], xa[ii + (long long)L.nx * jj]);
     };
-    const float yc = y(i, j);
-    const float a = apply4(yc, i > 0 ? y(i - 1, j) : 0.f, i + 1 < L.nx ? y(i + 1, j) : 0.f, j > 0 ? y(i, j - 1) : 0.f,
-                           j + 1 < L.ny ? y(i, j + 1) : 0.f, i > 0 ? te[c - 1] : 0.f, te[c], j > 0 ? tn[c - L.nx] : 0.f,
-                           tn[c]);
-    M.xb[l][r][L.off + c] = fmaf(dv[c], M.b[l][r][L.off + c] - a, yc);
+    const bool ld = act[r];
+    yv[r][0] = ld ? y(i, j) : 0.f;
+    yv[r][1] = ld && w ? y(i - 1, j) : 0.f;
+    yv[r][2] = ld && e ? y(i + 1, j) : 0.f;
+    yv[r][3] = ld && so ? y(i, j - 1) : 0.f;
+    yv[r][4] = ld && no ? y(i, j + 1) : 0.f;
+    bc[r] = ld ? M.b[l][r][L.off + c] : 0.f;
+  }
+  for (int r = 0; r < kR; r++) {
+    if (!act[r]) continue;
+    const float a = apply4(yv[r][0], yv[r][1], yv[r][2], yv[r][3], yv[r][4], fw, fe, fs, fn);
+    M.xb[l][r][L.off + c] = fmaf(dc, bc[r] - a, yv[r][0]);
   }
 }
 
