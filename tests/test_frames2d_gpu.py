@@ -46,3 +46,25 @@ def test_batched_frames_match_oracle(gpu_lib):
             scale = np.abs(ophi[r]).max()
             assert np.abs(phis[f][r] - ophi[r]).max() <= 1e-9 * scale, (f, r)
             assert np.abs(terms[f, r] - ot[r]).max() <= 1e-8 * np.abs(ot[r]).max(), (f, r, terms[f, r], ot[r])
+
+
+@pytest.mark.parametrize("rows", [2, 8])
+def test_batched_frames_block_tile_heights(gpu_lib, monkeypatch, rows):
+    """The frame multigrid's level-0 block tiles of 32 x 16 and 32 x 64 cells
+    (FPM_FRAMES_ROWS) reach the tolerance and the potentials of the default
+    32 x 32 tiles (1e-9 relative), on frames from 40^2 to 150^2 cells (several
+    block tiles, ragged edges)."""
+    from flowfpmpp_gb300 import partition as pt
+    from flowfpmpp_gb300 import workloads
+    frames = workloads.foil_frames(nframes=4, seed=23, nmin=40, nmax=150)
+    tol = 1e-11
+    monkeypatch.delenv("FPM_FRAMES_ROWS", raising=False)
+    t4, _, r4, p4 = pt.partition_frames_2d(frames, tolerance=tol, return_phi=True)
+    monkeypatch.setenv("FPM_FRAMES_ROWS", str(rows))
+    t, _, res, p = pt.partition_frames_2d(frames, tolerance=tol, return_phi=True)
+    assert np.all(res <= 2 * tol) and np.all(r4 <= 2 * tol), (res, r4)
+    for f in range(len(frames)):
+        for d in range(2):
+            scale = np.abs(p4[f][d]).max()
+            assert np.abs(p[f][d] - p4[f][d]).max() <= 1e-9 * scale, (rows, f, d)
+            assert np.abs(t[f, d] - t4[f, d]).max() <= 1e-8 * np.abs(t4[f, d]).max(), (rows, f, d)
