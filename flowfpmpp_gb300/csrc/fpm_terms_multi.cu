@@ -122,10 +122,14 @@ __global__ void k_terms_tables(Dims d, Axes ax, double b0, double b1, double b2,
 // outer face value | body_grad at a solid neighbour | (phi_nb - phi) /
 // (c_nb - c).  (One warp per potential with the flow shared through L1 was
 // measured slower for three potentials: 1.89 against 1.59 ms at 256^2 x 128.)
+// Four blocks per SM (64 registers, a few spilled) instead of the compiler's
+// 122 registers at two: the cell's long arithmetic phase runs with no loads
+// in flight, so more resident warps pay (three potentials at 384^2 x 192:
+// 4.71 -> 3.81 ms; three and five blocks measured 4.10 and 4.26 ms).
 constexpr int kTermsRows = 8;
 
 template <int NP>
-__global__ void __launch_bounds__(256) k_terms_multi(Dims d, TermsMultiArgs A, Flow fl,
+__global__ void __launch_bounds__(256, 4) k_terms_multi(Dims d, TermsMultiArgs A, Flow fl,
                                                       const int32_t* __restrict__ solid, TermsTables t,
                                                       double* partials, unsigned int* ticket, double* totals) {
   const int i = blockIdx.x * 32 + threadIdx.x + 1;
