@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth4(MgLevel L, Vec4 xv, Vec4 bv,
 // omega dinv b.  scale > 1 over-corrects with the coarse solution (the
 // cycle stays linear and symmetric).
 template <bool FIRST>
-__global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bcv,
+__global__ void __launch_bounds__(256, 4) k_mg_resrestrict4(MgLevel F, MgLevel C, Vec4 xv, Vec4 bv, Vec4 bcv,
                                                          float scale, const MgScalars* S, unsigned mask,
                                                          float omega) {
   MG_RHS(C);
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(256) k_mg_resrestrict4(MgLevel F, MgLevel C, V
 // parents 2g, 2g, 2g+1, 2g+1 (a float2 of the coarse row: 2g is even and
 // the row starts on 16 bytes).
 template <bool FIRST>
-__global__ void __launch_bounds__(256, 3) k_mg_prolong_smooth4(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv,
+__global__ void __launch_bounds__(256, 4) k_mg_prolong_smooth4(MgLevel F, MgLevel C, Vec4 xv, Vec4 xcv, Vec4 bv,
                                                             Vec4 xov, float omega, const MgScalars* S,
                                                             unsigned mask) {
   MG_RHS(F);
