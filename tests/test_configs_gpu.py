@@ -5,7 +5,7 @@ oracle on the same seeded inputs (no comparison of the CUDA path with itself):
       plain FP64 PCG and the multigrid-preconditioned refinement, then the
       force densities in the C1 flow: potentials within 1e-9 relative
       max-norm, density fields and their integrals within 1e-8 relative
-      (the benchmark spec's tolerances).
+      (the required tolerances).
   C2  256^3 boxes, exactly 2000 weighted-Jacobi sweeps: the FP64
       (fused multiply-add) and double-float sweeps within 1e-12 relative of
       the oracle's 2000 sweeps (the configuration's own check).

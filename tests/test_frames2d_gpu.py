@@ -1,6 +1,6 @@
 """Batched uneven 2-D frames on the GPU against the oracle run frame by frame
 (compatibility, FP64 PCG to the same tolerance, four-term partition), on a
-small batch of the config-4 generator (elliptic foils, Lamb-Oseen vortices,
+small batch of the 256-frame foil generator (elliptic foils, Lamb-Oseen vortices,
 noisy outer ring).  Potentials within 1e-9 relative max-norm; force terms
 within 1e-8 relative to the frame's largest term."""
 import numpy as np

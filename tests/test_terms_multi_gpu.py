@@ -3,7 +3,7 @@
 arithmetic) against the oracle's FP64 compute_stairstep_fpm_terms_3d
 (src/fpm_stairstep_mpi_3d.f90:426-497) run on each potential: density fields
 within 1e-12 relative max-norm (the double-float arithmetic carries a 48-bit
-significand; the benchmark spec asks 1e-8) and integrals within 1e-12 of the
+significand; the required bound is 1e-8) and integrals within 1e-12 of the
 largest integral, on the C1 sphere (three potentials) and on a random
 stretched grid with interior bounds and random fields (one to four
 potentials)."""
