@@ -337,7 +337,6 @@ constexpr unsigned kTcSpin = 1u << 20;
 template <int COUT>
 struct TcTile {
   static constexpr bool on = false;
-  static constexpr int TJ = 1, TK = 1, CS = 16;
 };
 template <>
 struct TcTile<16> { static constexpr bool on = true; static constexpr int TJ = 4, TK = 2, CS = 16; };
