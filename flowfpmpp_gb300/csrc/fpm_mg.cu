@@ -16,10 +16,11 @@
 // valid preconditioner for CG.
 //
 // Level 0 uses the FP32 layout of the mixed solver (16-byte aligned rows,
-// zero x-y halo, see MixedGrid): its stencil passes stream planes through
-// shared memory with TMA, its vector updates are float4 kernels that march
-// through k.  The coarse levels are compact (x fastest) and use one thread
-// per cell.  All right-hand sides share each launch.
+// zero x-y halo, see MixedGrid): its three stencil passes stream planes
+// through shared memory with TMA and also carry the PCG vector updates (no
+// pointwise pass).  The coarse levels are compact (x fastest, rows padded to
+// 16 bytes) and take four cells per thread (float4).  All right-hand sides
+// share each launch.
 #include "fpm_internal.h"
 #include "fpm_tma.cuh"
 
